@@ -1,0 +1,483 @@
+// C ABI of the device plans: creation (upload of the discretisation,
+// node adjacency, tables), data slots, assembly and result access.
+#include <cub/cub.cuh>
+
+#include <algorithm>
+#include <cstring>
+#include <exception>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "host/refelem.h"
+#include "plan.h"
+
+namespace gfgpu {
+void set_last_error(const std::string &s);
+}
+
+using namespace gfgpu;
+
+struct gfgpu_plan_s : public Plan {};
+
+namespace {
+
+#define GF_CUDA(call)                                                          \
+  do {                                                                         \
+    cudaError_t ce_ = (call);                                                  \
+    if (ce_ != cudaSuccess) {                                                  \
+      set_last_error(std::string(#call) + ": " + cudaGetErrorString(ce_));     \
+      return ce_ == cudaErrorMemoryAllocation ? GFGPU_E_NOMEM : GFGPU_E_CUDA;  \
+    }                                                                          \
+  } while (0)
+
+template <class T>
+int dalloc(T **p, size_t n) {
+  *p = nullptr;
+  if (n == 0) n = 1;
+  GF_CUDA(cudaMalloc(reinterpret_cast<void **>(p), n * sizeof(T)));
+  return GFGPU_OK;
+}
+
+template <class T>
+void dfree(T *&p) {
+  if (p) cudaFree(const_cast<void *>(reinterpret_cast<const void *>(p)));
+  p = nullptr;
+}
+
+// The forms the affine-simplex element pass lowers: GRADGRAD / MASS with
+// constant or per-element coefficients, SOURCE with a field on the
+// variable's mesh_fem and a constant factor.
+bool simplex_form_supported(const gfgpu_form &f, int qdim, int dim, std::string &why) {
+  if (f.n_terms < 1 || f.n_terms > GFGPU_MAX_TERMS) {
+    why = "empty form";
+    return false;
+  }
+  int nsrc = 0;
+  for (int t = 0; t < f.n_terms; ++t) {
+    const gfgpu_term &T = f.terms[t];
+    if (T.kind == GFGPU_TERM_GRADGRAD || T.kind == GFGPU_TERM_MASS) {
+      int nc = T.kind == GFGPU_TERM_GRADGRAD ? 3 : 1;
+      for (int k = 0; k < nc; ++k)
+        if (T.c[k].kind == GFGPU_COEF_NODAL) {
+          why = "nodal coefficient fields need the Gauss-point path (not built for simplices)";
+          return false;
+        }
+      if (T.kind == GFGPU_TERM_GRADGRAD && qdim == 1 &&
+          (T.c[0].kind != GFGPU_COEF_NONE || T.c[2].kind != GFGPU_COEF_NONE)) {
+        why = "div/transpose couplings need a vector field with qdim == dim";
+        return false;
+      }
+      if (T.kind == GFGPU_TERM_GRADGRAD && qdim > 1 && qdim != dim) {
+        why = "qdim must equal the mesh dimension";
+        return false;
+      }
+    } else if (T.kind == GFGPU_TERM_SOURCE) {
+      if (++nsrc > 1) {
+        why = "at most one source term";
+        return false;
+      }
+      if (T.c[0].kind != GFGPU_COEF_NONE && T.c[0].kind != GFGPU_COEF_CONST) {
+        why = "source factor must be constant";
+        return false;
+      }
+      if (T.field_slot <= 0 || T.field_slot >= GFGPU_MAX_SLOTS) {
+        why = "bad source field slot";
+        return false;
+      }
+    } else {
+      why = "term kind not lowered on simplices";
+      return false;
+    }
+  }
+  return true;
+}
+
+int status_from_err(int e) {
+  if (e & ERR_JACOBIAN) {
+    set_last_error("Non invertible matrix (det of the geometric transformation is 0)");
+    return GFGPU_E_JACOBIAN;
+  }
+  if (e & ERR_NAN) {
+    set_last_error("non-finite value in assembly");
+    return GFGPU_E_NAN;
+  }
+  if (e & ERR_CAPACITY) {
+    set_last_error("a DOF node couples to more nodes than the kernel holds");
+    return GFGPU_E_UNSUPPORTED;
+  }
+  if (e & ERR_TIMEOUT) {
+    set_last_error("device wait timed out");
+    return GFGPU_E_TIMEOUT;
+  }
+  return GFGPU_OK;
+}
+
+int build_pattern(Plan &P) {
+  // counts per row and per node
+  GF_CUDA(cudaMemsetAsync(P.d_count, 0, (P.n_dof + 1) * sizeof(int32_t), P.stream));
+  GF_CUDA(cudaMemsetAsync(P.d_ncount, 0, (P.n_nodes + 1) * sizeof(int32_t), P.stream));
+  GF_CUDA(launch_pattern_count(P));
+  size_t need = 0, need2 = 0, need3 = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, need, P.d_count, P.d_rowptr, P.n_dof + 1);
+  cub::DeviceScan::ExclusiveSum(nullptr, need2, P.d_ncount, P.d_nptr, P.n_nodes + 1);
+  int32_t *d_max = nullptr;
+  cub::DeviceReduce::Max(nullptr, need3, P.d_ncount, d_max, P.n_nodes + 1);
+  need = std::max(need, std::max(need2, need3 + 16));
+  if (need > P.cub_bytes) {
+    dfree(P.d_cub);
+    GF_CUDA(cudaMalloc(&P.d_cub, need));
+    P.cub_bytes = need;
+  }
+  GF_CUDA(cub::DeviceScan::ExclusiveSum(P.d_cub, P.cub_bytes, P.d_count, P.d_rowptr, P.n_dof + 1,
+                                        P.stream));
+  GF_CUDA(cub::DeviceScan::ExclusiveSum(P.d_cub, P.cub_bytes, P.d_ncount, P.d_nptr,
+                                        P.n_nodes + 1, P.stream));
+  P.launches += 2;
+  int64_t nnz = 0, nn = 0;
+  GF_CUDA(cudaMemcpyAsync(&nnz, P.d_rowptr + P.n_dof, sizeof(int64_t), cudaMemcpyDeviceToHost,
+                          P.stream));
+  GF_CUDA(cudaMemcpyAsync(&nn, P.d_nptr + P.n_nodes, sizeof(int64_t), cudaMemcpyDeviceToHost,
+                          P.stream));
+  // max slots per node
+  int32_t *d_mx = reinterpret_cast<int32_t *>(P.d_count);  // reuse: counts are consumed
+  GF_CUDA(cub::DeviceReduce::Max(P.d_cub, P.cub_bytes, P.d_ncount, d_mx, P.n_nodes + 1, P.stream));
+  P.launches++;
+  int32_t mx = 0;
+  GF_CUDA(cudaMemcpyAsync(&mx, d_mx, sizeof(int32_t), cudaMemcpyDeviceToHost, P.stream));
+  GF_CUDA(cudaStreamSynchronize(P.stream));
+  int herr = 0;
+  GF_CUDA(cudaMemcpy(&herr, P.d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (herr) return status_from_err(herr);
+  dfree(P.d_colidx);
+  dfree(P.d_vals);
+  dfree(P.d_ncol);
+  int rc;
+  if ((rc = dalloc(&P.d_colidx, size_t(nnz)))) return rc;
+  if ((rc = dalloc(&P.d_vals, size_t(nnz)))) return rc;
+  if ((rc = dalloc(&P.d_ncol, size_t(nn)))) return rc;
+  P.nnz = nnz;
+  P.max_slots = mx;
+  GF_CUDA(launch_pattern_fill(P));
+  return GFGPU_OK;
+}
+
+int check_err(Plan &P) {
+  int herr = 0;
+  GF_CUDA(cudaStreamSynchronize(P.stream));
+  GF_CUDA(cudaMemcpy(&herr, P.d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  return status_from_err(herr);
+}
+
+}  // namespace
+
+extern "C" {
+
+int gfgpu_plan_create(const gfgpu_space *space, const gfgpu_form *form, void *cuda_stream,
+                      gfgpu_plan **out) {
+  if (!space || !form || !out) {
+    set_last_error("null argument");
+    return GFGPU_E_INVALID;
+  }
+  *out = nullptr;
+  const gfgpu_space &S = *space;
+  if (S.dim < 2 || S.dim > 3 || (S.kind != GFGPU_SIMPLEX && S.kind != GFGPU_HEX) ||
+      S.degree < 1 || S.qdim < 1 || S.qdim > 3 || S.n_elements < 0 || S.n_points < 0 ||
+      S.n_dof < 0 || S.n_dof % S.qdim || !S.im) {
+    set_last_error("gfgpu_plan_create: bad space");
+    return GFGPU_E_INVALID;
+  }
+  if (S.n_elements > 0 && (!S.points || !S.cvpts || !S.dofs)) {
+    set_last_error("gfgpu_plan_create: missing arrays");
+    return GFGPU_E_INVALID;
+  }
+  int dev_count = 0;
+  if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0) {
+    set_last_error("no CUDA device");
+    return GFGPU_E_CUDA;
+  }
+  gfgpu_plan *P = new (std::nothrow) gfgpu_plan();
+  if (!P) return GFGPU_E_NOMEM;
+  int rc = GFGPU_OK;
+  try {
+    P->dim = S.dim;
+    P->kind = S.kind;
+    P->degree = S.degree;
+    P->qdim = S.qdim;
+    P->im = S.im;
+    P->form = *form;
+    P->stream = static_cast<cudaStream_t>(cuda_stream);
+    P->n_points = S.n_points;
+    P->n_elements = S.n_elements;
+    P->n_dof = S.n_dof;
+    P->n_nodes = S.n_dof / S.qdim;
+    RefElement fe(S.dim, S.kind, S.degree);
+    P->nb = fe.nb;
+    P->nbg = S.kind == GFGPU_SIMPLEX ? S.dim + 1 : (1 << S.dim);
+    std::string why;
+    if (S.kind != GFGPU_SIMPLEX || S.degree > 2) {
+      set_last_error("element not lowered: only GT_PK + FEM_PK(dim,1|2) in this build");
+      delete P;
+      return GFGPU_E_UNSUPPORTED;
+    }
+    if (!simplex_form_supported(P->form, S.qdim, S.dim, why)) {
+      set_last_error("form not supported: " + why);
+      delete P;
+      return GFGPU_E_UNSUPPORTED;
+    }
+    P->affine_simplex = true;
+    std::string err;
+    if ((rc = build_simplex_tables(*P, err)) != GFGPU_OK) {
+      set_last_error(err);
+      delete P;
+      return rc;
+    }
+    const int64_t E = S.n_elements, nb = P->nb, nbg = P->nbg;
+    // validate and convert indices
+    std::vector<int32_t> cv(size_t(E * nbg)), en(size_t(E * nb));
+    for (int64_t k = 0; k < E * nbg; ++k) {
+      if (S.cvpts[k] < 0 || S.cvpts[k] >= S.n_points) throw std::runtime_error("bad convex point index");
+      cv[k] = int32_t(S.cvpts[k]);
+    }
+    for (int64_t k = 0; k < E * nb; ++k) {
+      if (S.dofs[k] < 0 || S.dofs[k] >= S.n_dof || S.dofs[k] % S.qdim)
+        throw std::runtime_error("bad DOF index");
+      en[k] = int32_t(S.dofs[k] / S.qdim);
+    }
+    // node -> (element, local node) adjacency, element order within a node
+    std::vector<int32_t> aptr(size_t(P->n_nodes + 1), 0), adj(size_t(E * nb));
+    for (int64_t k = 0; k < E * nb; ++k) aptr[en[k] + 1]++;
+    for (int64_t i = 0; i < P->n_nodes; ++i) {
+      P->max_adj = std::max(P->max_adj, aptr[i + 1]);
+      aptr[i + 1] += aptr[i];
+    }
+    {
+      std::vector<int32_t> fill(aptr.begin(), aptr.end() - 1);
+      for (int64_t e = 0; e < E; ++e)
+        for (int li = 0; li < nb; ++li) adj[fill[en[e * nb + li]]++] = int32_t(e * nb + li);
+    }
+    P->max_cand = int32_t(P->max_adj * nb);
+    if (P->max_cand > 4096) throw std::runtime_error("node valence too large for the pattern kernel");
+#define CHK(x)                   \
+  if ((rc = (x)) != GFGPU_OK) { \
+    gfgpu_plan_destroy(P);       \
+    return rc;                   \
+  }
+    CHK(dalloc(&P->d_points, size_t(S.n_points * S.dim)));
+    CHK(dalloc(&P->d_cv, cv.size()));
+    CHK(dalloc(&P->d_enode, en.size()));
+    CHK(dalloc(&P->d_adj_ptr, aptr.size()));
+    CHK(dalloc(&P->d_adj, adj.size()));
+    CHK(dalloc(&P->d_stab, 1));
+    CHK(dalloc(&P->d_elem, size_t(E * P->lay.stride)));
+    CHK(dalloc(&P->d_vec, size_t(S.n_dof)));
+    CHK(dalloc(&P->d_pot, 1));
+    CHK(dalloc(&P->d_err, 1));
+    CHK(dalloc(&P->d_count, size_t(S.n_dof + 1)));
+    CHK(dalloc(&P->d_ncount, size_t(P->n_nodes + 1)));
+    CHK(dalloc(&P->d_rowptr, size_t(S.n_dof + 1)));
+    CHK(dalloc(&P->d_nptr, size_t(P->n_nodes + 1)));
+    auto up = [&](void *dst, const void *src, size_t bytes) -> int {
+      GF_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
+      return GFGPU_OK;
+    };
+    CHK(up(P->d_points, S.points, size_t(S.n_points * S.dim) * sizeof(double)));
+    CHK(up(P->d_cv, cv.data(), cv.size() * sizeof(int32_t)));
+    CHK(up(P->d_enode, en.data(), en.size() * sizeof(int32_t)));
+    CHK(up(P->d_adj_ptr, aptr.data(), aptr.size() * sizeof(int32_t)));
+    CHK(up(P->d_adj, adj.data(), adj.size() * sizeof(int32_t)));
+    CHK(up(P->d_stab, &P->stab, sizeof(SimplexTables)));
+    GF_CUDA(cudaMemset(P->d_err, 0, sizeof(int)));
+    GF_CUDA(cudaMemset(P->d_vec, 0, size_t(S.n_dof) * sizeof(double)));
+#undef CHK
+  } catch (const std::exception &e) {
+    set_last_error(e.what());
+    gfgpu_plan_destroy(P);
+    return GFGPU_E_INVALID;
+  }
+  *out = P;
+  return GFGPU_OK;
+}
+
+void gfgpu_plan_destroy(gfgpu_plan *P) {
+  if (!P) return;
+  dfree(P->d_points);
+  dfree(P->d_cv);
+  dfree(P->d_enode);
+  dfree(P->d_adj_ptr);
+  dfree(P->d_adj);
+  dfree(P->d_stab);
+  dfree(P->d_elem);
+  dfree(P->d_rowptr);
+  dfree(P->d_colidx);
+  dfree(P->d_vals);
+  dfree(P->d_nptr);
+  dfree(P->d_ncol);
+  dfree(P->d_vec);
+  dfree(P->d_pot);
+  dfree(P->d_err);
+  dfree(P->d_count);
+  dfree(P->d_ncount);
+  dfree(P->d_cub);
+  for (int i = 0; i < GFGPU_MAX_SLOTS; ++i) dfree(P->slot_own[i]);
+  delete P;
+}
+
+int gfgpu_set_data(gfgpu_plan *P, int32_t slot, const double *values, int64_t n,
+                   int32_t on_device) {
+  if (!P || slot < 0 || slot >= GFGPU_MAX_SLOTS || n < 0 || (n > 0 && !values)) {
+    set_last_error("gfgpu_set_data: bad arguments");
+    return GFGPU_E_INVALID;
+  }
+  if (on_device) {
+    dfree(P->slot_own[slot]);
+    P->slot_ptr[slot] = values;
+    P->slot_n[slot] = n;
+    return GFGPU_OK;
+  }
+  if (!P->slot_own[slot] || P->slot_n[slot] != n) {
+    dfree(P->slot_own[slot]);
+    int rc = dalloc(&P->slot_own[slot], size_t(n));
+    if (rc) return rc;
+  }
+  P->slot_n[slot] = n;
+  P->slot_ptr[slot] = P->slot_own[slot];
+  if (n) GF_CUDA(cudaMemcpyAsync(P->slot_own[slot], values, size_t(n) * sizeof(double),
+                                 cudaMemcpyHostToDevice, P->stream));
+  return GFGPU_OK;
+}
+
+static int check_slots(Plan &P, bool need_u) {
+  if (need_u && (!P.slot_ptr[GFGPU_SLOT_U] || P.slot_n[GFGPU_SLOT_U] != P.n_dof)) {
+    set_last_error("variable u (slot 0) not set or of wrong size");
+    return GFGPU_E_STATE;
+  }
+  for (int t = 0; t < P.form.n_terms; ++t) {
+    const gfgpu_term &T = P.form.terms[t];
+    for (int k = 0; k < 3; ++k)
+      if (T.c[k].kind == GFGPU_COEF_ELEMENT &&
+          (!P.slot_ptr[T.c[k].slot] || P.slot_n[T.c[k].slot] != P.n_elements)) {
+        set_last_error("per-element coefficient slot not set or of wrong size");
+        return GFGPU_E_STATE;
+      }
+    if (T.kind == GFGPU_TERM_SOURCE &&
+        (!P.slot_ptr[T.field_slot] || P.slot_n[T.field_slot] != P.n_dof)) {
+      set_last_error("source field slot not set or of wrong size");
+      return GFGPU_E_STATE;
+    }
+  }
+  return GFGPU_OK;
+}
+
+int gfgpu_assemble(gfgpu_plan *P, int32_t order, int32_t flags, double *potential) {
+  if (!P || order < 0 || order > 2) {
+    set_last_error("gfgpu_assemble: bad arguments");
+    return GFGPU_E_INVALID;
+  }
+  if (order == 0) {
+    set_last_error("order 0 is not lowered for this form");
+    return GFGPU_E_UNSUPPORTED;
+  }
+  (void)potential;
+  const bool want_K = order == 2;
+  const bool want_R = order == 1 || (flags & 2);
+  int rc = check_slots(*P, want_R);
+  if (rc) return rc;
+  GF_CUDA(cudaMemsetAsync(P->d_err, 0, sizeof(int), P->stream));
+  GF_CUDA(launch_simplex_element_pass(*P));
+  if (want_K && (P->nnz < 0 || (flags & GFGPU_REBUILD_PATTERN))) {
+    if ((rc = build_pattern(*P))) return rc;
+  }
+  if (want_R && !want_K && P->nnz < 0) {
+    // the gather walks the node-level pattern; build it once
+    if ((rc = build_pattern(*P))) return rc;
+  }
+  GF_CUDA(launch_gather(*P, want_K, want_R));
+  return GFGPU_OK;
+}
+
+int gfgpu_sync(gfgpu_plan *P) {
+  if (!P) return GFGPU_E_INVALID;
+  return check_err(*P);
+}
+
+int gfgpu_assemble_host(gfgpu_plan *P, const double *u, double *vals, double *vec) {
+  if (!P) return GFGPU_E_INVALID;
+  int rc;
+  if (u && (rc = gfgpu_set_data(P, GFGPU_SLOT_U, u, P->n_dof, 0))) return rc;
+  if ((rc = gfgpu_assemble(P, 2, vec ? 2 : 0, nullptr))) return rc;
+  if (vals) GF_CUDA(cudaMemcpyAsync(vals, P->d_vals, size_t(P->nnz) * sizeof(double),
+                                    cudaMemcpyDeviceToHost, P->stream));
+  if (vec) GF_CUDA(cudaMemcpyAsync(vec, P->d_vec, size_t(P->n_dof) * sizeof(double),
+                                   cudaMemcpyDeviceToHost, P->stream));
+  return check_err(*P);
+}
+
+int gfgpu_pattern_size(gfgpu_plan *P, int64_t *n_rows, int64_t *nnz) {
+  if (!P) return GFGPU_E_INVALID;
+  if (P->nnz < 0) {
+    set_last_error("no pattern yet: assemble order 2 first");
+    return GFGPU_E_STATE;
+  }
+  *n_rows = P->n_dof;
+  *nnz = P->nnz;
+  return GFGPU_OK;
+}
+
+int gfgpu_pattern_copy(gfgpu_plan *P, int64_t *rowptr, int32_t *colidx) {
+  if (!P) return GFGPU_E_INVALID;
+  if (P->nnz < 0) {
+    set_last_error("no pattern yet: assemble order 2 first");
+    return GFGPU_E_STATE;
+  }
+  GF_CUDA(cudaStreamSynchronize(P->stream));
+  if (rowptr) GF_CUDA(cudaMemcpy(rowptr, P->d_rowptr, size_t(P->n_dof + 1) * sizeof(int64_t),
+                                 cudaMemcpyDeviceToHost));
+  if (colidx) GF_CUDA(cudaMemcpy(colidx, P->d_colidx, size_t(P->nnz) * sizeof(int32_t),
+                                 cudaMemcpyDeviceToHost));
+  return GFGPU_OK;
+}
+
+int gfgpu_device_csr(gfgpu_plan *P, const int64_t **rowptr, const int32_t **colidx,
+                     double **vals) {
+  if (!P) return GFGPU_E_INVALID;
+  if (P->nnz < 0) {
+    set_last_error("no pattern yet: assemble order 2 first");
+    return GFGPU_E_STATE;
+  }
+  if (rowptr) *rowptr = P->d_rowptr;
+  if (colidx) *colidx = P->d_colidx;
+  if (vals) *vals = P->d_vals;
+  return GFGPU_OK;
+}
+
+int gfgpu_device_vector(gfgpu_plan *P, double **vec) {
+  if (!P || !vec) return GFGPU_E_INVALID;
+  *vec = P->d_vec;
+  return GFGPU_OK;
+}
+
+int64_t gfgpu_launch_count(gfgpu_plan *P) { return P ? P->launches : -1; }
+
+int gfgpu_copy_result(gfgpu_plan *P, int32_t which, void *dst) {
+  if (!P || !dst || which < 0 || which > 3) {
+    set_last_error("gfgpu_copy_result: bad arguments");
+    return GFGPU_E_INVALID;
+  }
+  if (which != GFGPU_RESULT_VECTOR && P->nnz < 0) {
+    set_last_error("no pattern yet: assemble order 2 first");
+    return GFGPU_E_STATE;
+  }
+  const void *src = nullptr;
+  size_t bytes = 0;
+  switch (which) {
+    case GFGPU_RESULT_ROWPTR: src = P->d_rowptr, bytes = size_t(P->n_dof + 1) * 8; break;
+    case GFGPU_RESULT_COLIDX: src = P->d_colidx, bytes = size_t(P->nnz) * 4; break;
+    case GFGPU_RESULT_VALUES: src = P->d_vals, bytes = size_t(P->nnz) * 8; break;
+    default: src = P->d_vec, bytes = size_t(P->n_dof) * 8; break;
+  }
+  if (bytes) GF_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, P->stream));
+  return check_err(*P);
+}
+
+}  // extern "C"

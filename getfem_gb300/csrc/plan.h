@@ -1,0 +1,113 @@
+// Internal plan structure shared by the C-ABI layer and the kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/gfgpu.h"
+
+namespace gfgpu {
+
+// device error word bits
+enum : int {
+  ERR_JACOBIAN = 1,   // det K == 0
+  ERR_NAN = 2,        // non-finite value
+  ERR_CAPACITY = 4,   // a node touches more DOF nodes than the kernel holds
+  ERR_TIMEOUT = 8
+};
+
+// Terms of the sparse barycentric reference tensor of a P_K simplex:
+// grad phi_i = sum_v c_iv grad lambda_v with c_iv = 0 unless vertex v
+// carries weight in node i, so
+//   int grad_a phi_i grad_b phi_j = |J| sum_{v,w} G[i,j,v,w] g_v[a] g_w[b].
+// For each local pair (i,j) the nonzero (v,w) are listed.
+constexpr int kMaxNb = 10;      // P2 tetrahedron
+constexpr int kMaxPairTerms = 4;  // |supp(i)| * |supp(j)| for degree <= 2
+
+struct SimplexTables {
+  int nb, nv, dim;
+  // per (i,j): count, packed (v*nv+w), values
+  int8_t nterm[kMaxNb * kMaxNb];
+  int8_t vw[kMaxNb * kMaxNb * kMaxPairTerms];
+  double gval[kMaxNb * kMaxNb * kMaxPairTerms];
+  double mass[kMaxNb * kMaxNb];  // reference mass matrix sum_q w_q phi_i phi_j
+};
+
+// Per-element layout of the simplex element pass output (doubles):
+//   T[qd*qd*nv*nv]  (a, b, v, w)   |J| (c0 g_va g_wb + c1 d_ab g_v.g_w + c2 g_vb g_wa)
+//   cm              |J| * mass coefficient
+//   jw              |J|
+//   thr             1e-14 * max |elem|
+struct SimplexLayout {
+  int nT, off_cm, off_jw, off_thr, stride;
+};
+
+struct SlotPtrs {
+  const double *p[GFGPU_MAX_SLOTS];
+};
+
+struct DeviceBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+};
+
+struct Plan {
+  // discretisation
+  int dim = 0, kind = 0, degree = 0, qdim = 0, nb = 0, nbg = 0, nq = 0;
+  int64_t n_points = 0, n_elements = 0, n_dof = 0, n_nodes = 0;
+  std::string im;
+  gfgpu_form form{};
+  cudaStream_t stream = nullptr;
+  bool affine_simplex = false;  // simplex element pass applies
+  bool psd = true;
+
+  // device arrays
+  double *d_points = nullptr;   // n_points x dim
+  int32_t *d_cv = nullptr;      // E x nbg
+  int32_t *d_enode = nullptr;   // E x nb  (DOF node ids)
+  int32_t *d_adj_ptr = nullptr; // n_nodes + 1
+  int32_t *d_adj = nullptr;     // (e*nb + li), sorted by e within a node
+  int32_t max_adj = 0;          // largest adjacency
+  int32_t max_cand = 0;         // largest sum of nb over a node's elements
+
+  // data slots
+  const double *slot_ptr[GFGPU_MAX_SLOTS] = {};
+  double *slot_own[GFGPU_MAX_SLOTS] = {};
+  int64_t slot_n[GFGPU_MAX_SLOTS] = {};
+
+  // tables
+  SimplexTables stab{};
+  SimplexTables *d_stab = nullptr;
+  SimplexLayout lay{};
+
+  // element pass scratch
+  double *d_elem = nullptr;     // E x lay.stride
+  // outputs
+  int64_t *d_rowptr = nullptr;  // n_dof + 1
+  int32_t *d_colidx = nullptr;  // nnz
+  double *d_vals = nullptr;     // nnz
+  int64_t nnz = -1;
+  int64_t *d_nptr = nullptr;    // node-level pattern: n_nodes + 1
+  int32_t *d_ncol = nullptr;
+  int32_t max_slots = 0;
+  double *d_vec = nullptr;      // n_dof
+  double *d_pot = nullptr;      // 1
+  int *d_err = nullptr;
+  int32_t *d_count = nullptr;   // scratch counters (n_dof)
+  int32_t *d_ncount = nullptr;  // (n_nodes)
+  void *d_cub = nullptr;
+  size_t cub_bytes = 0;
+  int64_t launches = 0;
+};
+
+// kernels (k_simplex.cu)
+cudaError_t launch_simplex_element_pass(Plan &P);
+cudaError_t launch_pattern_count(Plan &P);
+cudaError_t launch_pattern_fill(Plan &P);
+cudaError_t launch_gather(Plan &P, bool want_K, bool want_R);
+cudaError_t launch_potential(Plan &P);
+int build_simplex_tables(Plan &P, std::string &err);
+
+}  // namespace gfgpu

@@ -1,0 +1,230 @@
+/*
+ * gfgpu — GB300 (sm_103a) backend for GetFEM's generic assembly hot path.
+ *
+ * C ABI only: plain pointers and sizes, no C++ or torch types, no
+ * exceptions.  Every entry point returns a gfgpu_status (0 = success); the
+ * text of the last error of the calling thread is available from
+ * gfgpu_last_error().
+ *
+ * The hot path this library replaces is the execution of compiled GWFL
+ * instructions over every element and Gauss point:
+ *   ga_workspace::assembly           src/getfem_generic_assembly_workspace.cc:791
+ *   ga_exec                          src/getfem_generic_assembly_compile_and_exec.cc:8750-9047
+ * A host-side shim in ga_workspace::assembly lowers the analysed GWFL tree to
+ * a gfgpu_form (the point where ga_compile starts,
+ * compile_and_exec.cc:8030-8047), creates one plan per (mesh_im, region,
+ * expression set) and calls gfgpu_assemble*; unsupported trees are rejected
+ * with GFGPU_E_UNSUPPORTED at plan creation.  There is no CPU fallback.
+ */
+#ifndef GFGPU_H
+#define GFGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  GFGPU_OK = 0,
+  GFGPU_E_INVALID = 1,     /* bad argument (the GMM_ASSERT1 size checks) */
+  GFGPU_E_UNSUPPORTED = 2, /* element / integration / expression not lowered */
+  GFGPU_E_CUDA = 3,        /* CUDA runtime error or no device */
+  GFGPU_E_JACOBIAN = 4,    /* det of the geometric transformation is 0
+                              ("Non invertible matrix",
+                              bgeot_geometric_trans.cc:380) */
+  GFGPU_E_NAN = 5,         /* non-finite value produced on the device */
+  GFGPU_E_TIMEOUT = 6,     /* a bounded device-side wait gave up */
+  GFGPU_E_NOMEM = 7,       /* device allocation failed */
+  GFGPU_E_STATE = 8        /* call out of sequence (e.g. no pattern yet) */
+} gfgpu_status;
+
+/* Element families: GT_PK(dim,1) + FEM_PK(dim,degree) and
+   GT_QK(dim,1) + FEM_QK(dim,degree). */
+typedef enum { GFGPU_SIMPLEX = 0, GFGPU_HEX = 1 } gfgpu_elem_kind;
+
+/* ------------------------------------------------------------------ */
+/* Form descriptor: the lowered GWFL expression                        */
+/* ------------------------------------------------------------------ */
+
+/* Where a scalar coefficient comes from. */
+typedef enum {
+  GFGPU_COEF_NONE = 0,
+  GFGPU_COEF_CONST = 1,   /* a fixed-size constant (add_fixed_size_constant) */
+  GFGPU_COEF_ELEMENT = 2, /* one value per element: a FEM_PK/QK(dim,0)
+                             constant (add_fem_constant on a P0 mesh_fem) */
+  GFGPU_COEF_NODAL = 3    /* a scalar field on the variable's scalar mesh_fem,
+                             interpolated at each Gauss point */
+} gfgpu_coef_kind;
+
+typedef struct {
+  int32_t kind;  /* gfgpu_coef_kind */
+  int32_t slot;  /* data slot for ELEMENT / NODAL (gfgpu_set_data) */
+  double value;  /* CONST value; multiplies ELEMENT / NODAL values */
+} gfgpu_coef;
+
+typedef enum {
+  /* int D(x) : Grad_u (x) Grad_Test_u with the isotropic tensor
+     D[a,k,b,l] = c0 d_ak d_bl + c1 d_ab d_kl + c2 d_al d_kb
+     (test component a, derivative k; trial component b, derivative l).
+     Scalar Laplacian: c1.  Linear elasticity (lambda*Div_u*Id+2*mu*Sym(Grad_u)):
+     c0 = lambda, c1 = c2 = mu. */
+  GFGPU_TERM_GRADGRAD = 1,
+  /* int c u.Test_u */
+  GFGPU_TERM_MASS = 2,
+  /* int f.Test_u with f a field on the variable's mesh_fem (qdim
+     components, slot `field_slot`), scaled by c[0] (CONST 1 if NONE) */
+  GFGPU_TERM_SOURCE = 3,
+  /* int ((Id+Grad_u)*Compressible_Neo_Hookean_PK2(Grad_u,[C1;D1])):Grad_Test_u
+     (getfem_nonlinear_elasticity.cc:2319-2320, law :503-600), C1 = c[0],
+     D1 = c[1]; dim 3 only */
+  GFGPU_TERM_NEOHOOKEAN = 4
+} gfgpu_term_kind;
+
+typedef struct {
+  int32_t kind;       /* gfgpu_term_kind */
+  int32_t field_slot; /* SOURCE only */
+  double scale;       /* overall factor of the term (e.g. -1) */
+  gfgpu_coef c[3];
+} gfgpu_term;
+
+#define GFGPU_MAX_TERMS 8
+typedef struct {
+  int32_t n_terms;
+  gfgpu_term terms[GFGPU_MAX_TERMS];
+} gfgpu_form;
+
+/* Data slots.  Slot 0 is the variable u (n_dof values). */
+#define GFGPU_SLOT_U 0
+#define GFGPU_MAX_SLOTS 8
+
+/* The discretisation: mesh, mesh_fem DOF map and mesh_im.  All arrays are
+   host memory and are copied at plan creation. */
+typedef struct {
+  int32_t dim;        /* 2 or 3 */
+  int32_t kind;       /* gfgpu_elem_kind */
+  int32_t degree;     /* K of FEM_PK/FEM_QK */
+  int32_t qdim;       /* 1 or dim */
+  const char *im;     /* "IM_TRIANGLE(2)", "IM_TETRAHEDRON(5)",
+                         "IM_GAUSS_PARALLELEPIPED(3,5)", ... */
+  int64_t n_points;
+  int64_t n_elements;
+  int64_t n_dof;
+  const double *points;  /* n_points x dim */
+  const int64_t *cvpts;  /* n_elements x (dim+1 | 2^dim) */
+  const int64_t *dofs;   /* n_elements x nb: first-component DOF of each
+                            local node (mesh_fem::ind_scalar_basic_dof_of_element,
+                            getfem/getfem_mesh_fem.h:461) */
+} gfgpu_space;
+
+typedef struct gfgpu_plan_s gfgpu_plan;
+
+/* ------------------------------------------------------------------ */
+/* Library                                                              */
+/* ------------------------------------------------------------------ */
+const char *gfgpu_version(void);
+const char *gfgpu_last_error(void);
+
+/* ------------------------------------------------------------------ */
+/* Input builders (host only).  These mirror the reference routines a
+   caller without GetFEM needs to produce a gfgpu_space.               */
+/* ------------------------------------------------------------------ */
+
+/* getfem::regular_unit_mesh (src/getfem_regular_meshes.cc:237) with
+   GT_PK(dim,1) (kind SIMPLEX) or GT_QK(dim,1) (kind HEX).  Call with
+   points == NULL to get the sizes.  jitter (optional) holds
+   (nx+1)^dim x dim offsets in lattice order, applied to interior vertices. */
+int gfgpu_regular_unit_mesh(int32_t dim, int32_t kind, int32_t nx, const double *jitter,
+                            int64_t *n_points, int64_t *n_elements,
+                            double *points, int64_t *cvpts);
+
+/* mesh_fem::enumerate_dof (src/getfem_mesh_fem.cc:320) for FEM_PK/QK(dim,degree)
+   with qdim components.  dofs: n_elements x nb (see gfgpu_space.dofs). */
+int gfgpu_enumerate_dofs(int32_t dim, int32_t kind, int32_t degree, int32_t qdim,
+                         int64_t n_elements, const int64_t *cvpts,
+                         int64_t *dofs, int64_t *n_dof);
+
+/* Number of local scalar basis functions of FEM_PK/QK(dim,degree). */
+int gfgpu_nb_basis(int32_t dim, int32_t kind, int32_t degree, int32_t *nb);
+
+/* Integration method tables (approx_integration points and weights,
+   src/getfem_integration.cc): call with pts == NULL to get nq. */
+int gfgpu_quadrature(const char *im, int32_t *dim, int32_t *nq, double *pts, double *w);
+
+/* Base values (nq x nb) and reference gradients (nq x nb x dim) of
+   FEM_PK/QK(dim,degree) at the points of `im` (fem_precomp_,
+   getfem/getfem_fem.h:653-700). */
+int gfgpu_basis_tables(int32_t dim, int32_t kind, int32_t degree, const char *im,
+                       double *val, double *grad);
+
+/* ------------------------------------------------------------------ */
+/* Plans: one per (discretisation, form).  One GPU, one stream per plan;
+   a plan is not shared between host threads.                          */
+/* ------------------------------------------------------------------ */
+
+/* Uploads the mesh, DOF map and tables; lowers the form.  Returns
+   GFGPU_E_UNSUPPORTED for element/integration/form combinations the
+   kernels do not implement.  cuda_stream is a cudaStream_t (NULL = the
+   default stream). */
+int gfgpu_plan_create(const gfgpu_space *space, const gfgpu_form *form, void *cuda_stream,
+                      gfgpu_plan **plan);
+void gfgpu_plan_destroy(gfgpu_plan *plan);
+
+/* Sets data slot `slot` (n values).  on_device != 0: `values` is a device
+   pointer that the plan reads in place at each assembly (no copy); else
+   the host values are copied to a plan-owned device buffer now. */
+int gfgpu_set_data(gfgpu_plan *plan, int32_t slot, const double *values, int64_t n,
+                   int32_t on_device);
+
+/* Sparsity pattern (CSR, rows = test DOFs, columns ascending).  Built on
+   the device at the first order-2 assembly with the reference's rule: an
+   element entry e is inserted only if |e| > 1e-14 * max|elem|
+   (compile_and_exec.cc:4889, :5453), the union over elements is kept, and
+   entries that sum to zero stay stored. */
+int gfgpu_pattern_size(gfgpu_plan *plan, int64_t *n_rows, int64_t *nnz);
+int gfgpu_pattern_copy(gfgpu_plan *plan, int64_t *rowptr, int32_t *colidx);
+/* Device pointers of the plan's CSR (valid until the plan is destroyed or
+   the pattern is rebuilt). */
+int gfgpu_device_csr(gfgpu_plan *plan, const int64_t **rowptr, const int32_t **colidx,
+                     double **vals);
+/* Device pointer of the plan's assembled vector (n_dof). */
+int gfgpu_device_vector(gfgpu_plan *plan, double **vec);
+
+#define GFGPU_REBUILD_PATTERN 1 /* rebuild the CSR pattern at this call */
+
+/* Assembles on the device.  order 2: K values into the plan's CSR (the
+   pattern is built at the first call, or when GFGPU_REBUILD_PATTERN);
+   order 1: the residual vector; order 0: the potential (*potential, host).
+   Results overwrite the plan's buffers; a caller that accumulates (as
+   GetFEM does into an external K, workspace.cc:803-845) adds them. */
+int gfgpu_assemble(gfgpu_plan *plan, int32_t order, int32_t flags, double *potential);
+
+/* Assembly from and to host memory, for callers holding host buffers:
+   copies u (slot 0, n_dof doubles) to the device, assembles order 2 and
+   order 1, and copies the K values (nnz) and the residual (n_dof) back.
+   Any of u / vals / vec may be NULL to skip that copy. */
+int gfgpu_assemble_host(gfgpu_plan *plan, const double *u, double *vals, double *vec);
+
+/* Copies a result of the plan into caller memory (host or device; the
+   copy direction is inferred from the pointer):
+   which = 0: row pointers (n_dof+1 int64), 1: column indices (nnz int32),
+   2: K values (nnz double), 3: assembled vector (n_dof double).
+   Waits for the copy to finish. */
+#define GFGPU_RESULT_ROWPTR 0
+#define GFGPU_RESULT_COLIDX 1
+#define GFGPU_RESULT_VALUES 2
+#define GFGPU_RESULT_VECTOR 3
+int gfgpu_copy_result(gfgpu_plan *plan, int32_t which, void *dst);
+
+/* Waits for the plan's stream and reports the device error word
+   (GFGPU_E_JACOBIAN / GFGPU_E_NAN) of the last assembly. */
+int gfgpu_sync(gfgpu_plan *plan);
+
+/* Number of kernel launches issued by the plan since creation. */
+int64_t gfgpu_launch_count(gfgpu_plan *plan);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GFGPU_H */

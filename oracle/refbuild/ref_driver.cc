@@ -1,0 +1,241 @@
+// Fixture and timing driver for the reference GetFEM build (test
+// infrastructure only).  It runs the reference's own generic assembly
+// (ga_workspace::add_expression + ga_workspace::assembly, see
+// src/getfem_generic_assembly_workspace.cc:545 and :791) on a structured
+// unit mesh built by getfem::regular_unit_mesh
+// (src/getfem_regular_meshes.cc:237), with input vectors read from files,
+// and dumps the mesh, the DOF maps and the assembled K (as CSR), R and
+// potential as raw little-endian binaries.
+//
+// usage: ref_driver key=value ...
+//   dim=2|3 nx=N gt=PK|QK fem=K qdim=Q im=IM_NAME in=DIR out=DIR
+//   expr=GWFL  orders=2,1,0  reps=R  jitter=0|1
+//   consts=name:KIND,...   KIND = P0 (one value per element),
+//                                 S  (scalar field on the same FEM),
+//                                 V  (field on the variable's FEM, qdim Q),
+//                                 C  (fixed-size constant, file length)
+// The variable is always "u" (file in/u.bin, zeros when absent).
+// Jitter: when jitter=1, in/jitter.bin holds (nx+1)^dim x dim doubles in
+// lattice order (x index fastest); interior vertices are moved by it.
+#include "getfem/getfem_generic_assembly.h"
+#include "getfem/getfem_regular_meshes.h"
+#include "getfem/getfem_mesh_fem.h"
+#include "getfem/getfem_mesh_im.h"
+#include <chrono>
+#include <cstdio>
+#include <fstream>
+#include <map>
+#include <algorithm>
+
+using bgeot::size_type;
+using bgeot::scalar_type;
+
+static std::map<std::string, std::string> args;
+
+static std::string arg(const std::string &k, const std::string &d = "") {
+  auto it = args.find(k);
+  return it == args.end() ? d : it->second;
+}
+
+static bool read_file(const std::string &path, std::vector<double> &v) {
+  std::ifstream f(path, std::ios::binary | std::ios::ate);
+  if (!f) return false;
+  std::streamsize n = f.tellg();
+  f.seekg(0);
+  v.resize(size_t(n) / sizeof(double));
+  f.read(reinterpret_cast<char *>(v.data()), n);
+  return true;
+}
+
+template <typename T>
+static void write_file(const std::string &path, const std::vector<T> &v) {
+  std::ofstream f(path, std::ios::binary);
+  f.write(reinterpret_cast<const char *>(v.data()), v.size() * sizeof(T));
+}
+
+static std::vector<std::string> split(const std::string &s, char c) {
+  std::vector<std::string> out;
+  std::string cur;
+  for (char ch : s) {
+    if (ch == c) { out.push_back(cur); cur.clear(); }
+    else cur += ch;
+  }
+  if (!cur.empty()) out.push_back(cur);
+  return out;
+}
+
+static double median(std::vector<double> v) {
+  if (v.empty()) return 0;
+  std::sort(v.begin(), v.end());
+  return v[v.size() / 2];
+}
+
+int main(int argc, char **argv) {
+  for (int i = 1; i < argc; ++i) {
+    std::string a(argv[i]);
+    size_t p = a.find('=');
+    if (p != std::string::npos) args[a.substr(0, p)] = a.substr(p + 1);
+  }
+  int dim = std::stoi(arg("dim", "2"));
+  size_type nx = std::stoul(arg("nx", "4"));
+  std::string gt = arg("gt", "PK");
+  int deg = std::stoi(arg("fem", "1"));
+  int qdim = std::stoi(arg("qdim", "1"));
+  std::string imname = arg("im", "IM_TRIANGLE(2)");
+  std::string in = arg("in", "."), out = arg("out", ".");
+  std::string expr = arg("expr", "Grad_u.Grad_Test_u");
+  int reps = std::stoi(arg("reps", "1"));
+  bool jitter = arg("jitter", "0") == "1";
+
+  char buf[128];
+  snprintf(buf, sizeof buf, "GT_%s(%d,1)", gt.c_str(), dim);
+  bgeot::pgeometric_trans pgt = bgeot::geometric_trans_descriptor(buf);
+  getfem::mesh m;
+  std::vector<size_type> nsubdiv(dim, nx);
+  getfem::regular_unit_mesh(m, nsubdiv, pgt);
+
+  if (jitter) {
+    std::vector<double> J;
+    if (!read_file(in + "/jitter.bin", J)) { fprintf(stderr, "no jitter.bin\n"); return 2; }
+    for (dal::bv_visitor ip(m.points().index()); !ip.finished(); ++ip) {
+      bgeot::base_node &P = m.points()[ip];
+      size_type flat = 0, stride = 1;
+      bool interior = true;
+      for (int d = 0; d < dim; ++d) {
+        long l = lround(P[d] * double(nx));
+        if (l <= 0 || l >= long(nx)) interior = false;
+        flat += size_type(l) * stride;
+        stride *= (nx + 1);
+      }
+      if (interior)
+        for (int d = 0; d < dim; ++d) P[d] += J[flat * dim + d];
+    }
+  }
+
+  snprintf(buf, sizeof buf, "FEM_%s(%d,%d)", gt.c_str(), dim, deg);
+  getfem::pfem pf = getfem::fem_descriptor(buf);
+  snprintf(buf, sizeof buf, "FEM_%s(%d,0)", gt.c_str(), dim);
+  getfem::pfem pf0 = getfem::fem_descriptor(buf);
+
+  getfem::mesh_fem mf(m, bgeot::dim_type(qdim));
+  mf.set_finite_element(m.convex_index(), pf);
+  getfem::mesh_fem mfs(m, 1);
+  mfs.set_finite_element(m.convex_index(), pf);
+  getfem::mesh_fem mf0(m, 1);
+  mf0.set_finite_element(m.convex_index(), pf0);
+  getfem::mesh_im mim(m);
+  mim.set_integration_method(m.convex_index(), getfem::int_method_descriptor(imname));
+
+  size_type ndof = mf.nb_dof();
+  size_type E = m.nb_convex();
+
+  // reference-element tables: integration points, weights, and the FEM's
+  // base values / reference gradients at those points
+  {
+    getfem::pintegration_method pim = getfem::int_method_descriptor(imname);
+    const getfem::papprox_integration pai = pim->approx_method();
+    std::vector<double> ipts, iw, bval, bgrad;
+    size_type nq = pai->nb_points_on_convex();
+    for (size_type q = 0; q < nq; ++q) {
+      for (int d = 0; d < dim; ++d) ipts.push_back(pai->point(q)[d]);
+      iw.push_back(pai->coeff(q));
+      getfem::base_tensor t;
+      pf->base_value(pai->point(q), t);
+      for (size_type k = 0; k < t.size(); ++k) bval.push_back(t[k]);
+      pf->grad_base_value(pai->point(q), t);
+      for (size_type k = 0; k < t.size(); ++k) bgrad.push_back(t[k]);
+    }
+    write_file(out + "/im_points.bin", ipts);
+    write_file(out + "/im_weights.bin", iw);
+    write_file(out + "/base_val.bin", bval);
+    write_file(out + "/base_grad.bin", bgrad);
+    std::vector<double> nodes;
+    for (size_type i = 0; i < pf->nb_dof(0); ++i)
+      for (int d = 0; d < dim; ++d) nodes.push_back(pf->node_of_dof(0, i)[d]);
+    write_file(out + "/fem_nodes.bin", nodes);
+  }
+
+  // mesh and DOF maps
+  {
+    std::vector<double> pts;
+    for (size_type ip = 0; ip < m.points().size(); ++ip)
+      for (int d = 0; d < dim; ++d) pts.push_back(m.points()[ip][d]);
+    write_file(out + "/points.bin", pts);
+    std::vector<int64_t> cvp, dofs, dofs0;
+    for (size_type cv = 0; cv < E; ++cv) {
+      for (size_type p : m.ind_points_of_convex(cv)) cvp.push_back(int64_t(p));
+      for (size_type d : mf.ind_scalar_basic_dof_of_element(cv)) dofs.push_back(int64_t(d));
+      { auto ct0 = mf0.ind_basic_dof_of_element(cv); for (size_type d : ct0) dofs0.push_back(int64_t(d)); }
+    }
+    write_file(out + "/cvpts.bin", cvp);
+    write_file(out + "/dofs.bin", dofs);
+    write_file(out + "/dofs0.bin", dofs0);
+  }
+
+  getfem::ga_workspace ws;
+  std::vector<double> U(ndof, 0.0);
+  read_file(in + "/u.bin", U);
+  if (U.size() != ndof) { fprintf(stderr, "u.bin has %zu values, need %zu\n", U.size(), size_t(ndof)); return 2; }
+  ws.add_fem_variable("u", mf, gmm::sub_interval(0, ndof), U);
+  std::map<std::string, std::vector<double>> cst;
+  for (const std::string &c : split(arg("consts", ""), ',')) {
+    std::vector<std::string> kv = split(c, ':');
+    std::vector<double> &v = cst[kv[0]];
+    if (!read_file(in + "/" + kv[0] + ".bin", v)) { fprintf(stderr, "missing %s\n", kv[0].c_str()); return 2; }
+    const std::string &k = kv[1];
+    size_type need = k == "P0" ? mf0.nb_dof() : k == "S" ? mfs.nb_dof() : k == "V" ? ndof : v.size();
+    if (v.size() != need) { fprintf(stderr, "%s has %zu values, need %zu\n", kv[0].c_str(), v.size(), size_t(need)); return 2; }
+    if (k == "P0") ws.add_fem_constant(kv[0], mf0, v);
+    else if (k == "S") ws.add_fem_constant(kv[0], mfs, v);
+    else if (k == "V") ws.add_fem_constant(kv[0], mf, v);
+    else ws.add_fixed_size_constant(kv[0], v);
+  }
+  ws.add_expression(expr, mim);
+
+  FILE *info = fopen((out + "/info.json").c_str(), "w");
+  fprintf(info, "{\"n_dof\": %zu, \"n_elements\": %zu, \"n_points\": %zu", size_t(ndof), size_t(E), size_t(m.points().size()));
+
+  for (const std::string &o : split(arg("orders", "2,1"), ',')) {
+    int order = std::stoi(o);
+    std::vector<double> times;
+    for (int r = 0; r < std::max(reps, 1); ++r) {
+      if (order == 1) {
+        ws.assembled_vector().clear();
+      }
+      auto t0 = std::chrono::steady_clock::now();
+      ws.assembly(size_type(order));
+      auto t1 = std::chrono::steady_clock::now();
+      times.push_back(std::chrono::duration<double>(t1 - t0).count());
+    }
+    fprintf(info, ", \"t_order%d\": %.6e", order, median(times));
+    if (order == 2) {
+      const auto &K = ws.assembled_matrix();
+      size_type n = gmm::mat_nrows(K);
+      // column-major rsvector -> CSR (rows sorted, columns ascending)
+      std::vector<int64_t> rowptr(n + 1, 0);
+      for (size_type j = 0; j < gmm::mat_ncols(K); ++j)
+        for (const auto &e : K.col(j)) rowptr[e.c + 1]++;
+      for (size_type i = 0; i < n; ++i) rowptr[i + 1] += rowptr[i];
+      std::vector<int64_t> colidx(rowptr[n]), fill(rowptr.begin(), rowptr.end() - 1);
+      std::vector<double> vals(rowptr[n]);
+      for (size_type j = 0; j < gmm::mat_ncols(K); ++j)
+        for (const auto &e : K.col(j)) {
+          int64_t k = fill[e.c]++;
+          colidx[k] = int64_t(j);
+          vals[k] = e.e;
+        }
+      write_file(out + "/K_rowptr.bin", rowptr);
+      write_file(out + "/K_colidx.bin", colidx);
+      write_file(out + "/K_vals.bin", vals);
+      fprintf(info, ", \"nnz\": %lld", (long long)rowptr[n]);
+    } else if (order == 1) {
+      write_file(out + "/R.bin", ws.assembled_vector());
+    } else {
+      std::vector<double> e(1, ws.assembled_potential());
+      write_file(out + "/E.bin", e);
+    }
+  }
+  fprintf(info, "}\n");
+  fclose(info);
+  return 0;
+}

@@ -1,0 +1,146 @@
+"""Generates the golden fixtures under tests/golden/ from the reference GetFEM
+build (oracle/_ref/ref_driver, made by `make -C oracle/refbuild`).
+
+Each case builds a structured unit mesh with getfem::regular_unit_mesh,
+feeds seeded input vectors to the reference's own ga_workspace
+(add_expression + assembly), and stores inputs and outputs: mesh points and
+convexes, DOF maps, integration points and weights, base values and
+gradients, the assembled K as CSR (rows = test DOFs) and R.
+
+Run from the repository root:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
+OUT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NH = "((Id(meshdim)+Grad_u)*(Compressible_Neo_Hookean_PK2(Grad_u,[0.5*mu;D1]))):Grad_Test_u"
+
+# name, dim, gt, degree, qdim, im, nx, expr, consts{name: kind}, jitter, u kind
+CASES = [
+    ("p1tri_poisson", 2, "PK", 1, 1, "IM_TRIANGLE(2)", 8,
+     "Grad_u.Grad_Test_u - f*Test_u", {"f": "V"}, False, "normal"),
+    ("p2tri_poisson_kappa", 2, "PK", 2, 1, "IM_TRIANGLE(4)", 5,
+     "kappa*Grad_u.Grad_Test_u - f*Test_u", {"kappa": "P0", "f": "V"}, True, "normal"),
+    ("p1tri_mass_laplace", 2, "PK", 1, 1, "IM_TRIANGLE(2)", 6,
+     "2*u*Test_u + Grad_u.Grad_Test_u", {}, False, "normal"),
+    ("p2tri_elastic", 2, "PK", 2, 2, "IM_TRIANGLE(4)", 4,
+     "(lambda*Div_u*Id(2)+2*mu*Sym(Grad_u)):Grad_Test_u - f.Test_u",
+     {"lambda": "P0", "mu": "P0", "f": "V"}, True, "normal"),
+    ("p1tet_elastic", 3, "PK", 1, 3, "IM_TETRAHEDRON(2)", 3,
+     "(lambda*Div_u*Id(3)+2*mu*Sym(Grad_u)):Grad_Test_u - f.Test_u",
+     {"lambda": "P0", "mu": "P0", "f": "V"}, True, "normal"),
+    ("p2tet_elastic", 3, "PK", 2, 3, "IM_TETRAHEDRON(5)", 3,
+     "(lambda*Div_u*Id(3)+2*mu*Sym(Grad_u)):Grad_Test_u - f.Test_u",
+     {"lambda": "P0", "mu": "P0", "f": "V"}, True, "normal"),
+    ("p2tet_elastic_alt", 3, "PK", 2, 3, "IM_TETRAHEDRON(5)", 3,
+     "lambda*Div_u*Div_Test_u + mu*(Grad_u + Grad_u'):Grad_Test_u - f.Test_u",
+     {"lambda": "P0", "mu": "P0", "f": "V"}, True, "normal"),
+    ("p2tet_poisson", 3, "PK", 2, 1, "IM_TETRAHEDRON(5)", 3,
+     "Grad_u.Grad_Test_u", {}, True, "normal"),
+    ("q2hex_neohookean", 3, "QK", 2, 3, "IM_GAUSS_PARALLELEPIPED(3,5)", 2,
+     NH, {"mu": "P0", "D1": "C"}, False, "modes"),
+    ("q4hex_laplace", 3, "QK", 4, 1, "IM_GAUSS_PARALLELEPIPED(3,9)", 2,
+     "kappa*Grad_u.Grad_Test_u", {"kappa": "P0"}, False, "normal"),
+]
+
+
+def sinusoid_modes(xyz: np.ndarray, qdim: int, rng) -> np.ndarray:
+    """u_a(x) = sum of 8 modes 0.05 sin(k.x + phi), k ~ U[-pi,pi]^3."""
+    u = np.zeros((xyz.shape[0], qdim))
+    for a in range(qdim):
+        for _ in range(8):
+            k = rng.uniform(-np.pi, np.pi, xyz.shape[1])
+            ph = rng.uniform(0, 2 * np.pi)
+            u[:, a] += 0.05 * np.sin(xyz @ k + ph)
+    return u.ravel()
+
+
+def make_case(case, seed):
+    name, dim, gt, deg, qdim, im, nx, expr, consts, jitter, ukind = case
+    import getfem_gb300 as g
+    rng = np.random.default_rng(seed)
+    kind = "simplex" if gt == "PK" else "hex"
+    h = 1.0 / nx
+    jit = None
+    if jitter:
+        jit = rng.uniform(-0.1 * h, 0.1 * h, ((nx + 1) ** dim, dim))
+    mesh = g.Mesh.regular_unit(dim, nx, kind, jitter=jit)
+    mf = g.MeshFem(mesh, qdim, degree=deg)
+    ndof = mf.nb_dof()
+    E = mesh.nb_convex()
+    inputs = {}
+    if ukind == "modes":
+        inputs["u"] = sinusoid_modes(mf.basic_dof_nodes(), qdim, rng)
+    else:
+        inputs["u"] = rng.standard_normal(ndof) * 0.1
+    for cname, ck in consts.items():
+        if ck == "P0":
+            sigma = 0.3 if cname == "mu" and ukind == "modes" else 0.2
+            inputs[cname] = np.exp(rng.normal(0.0, sigma, E))
+        elif ck == "V":
+            inputs[cname] = rng.standard_normal(ndof) if qdim > 1 else rng.uniform(-1, 1, ndof)
+        elif ck == "C":
+            inputs[cname] = np.array([1.5])
+    with tempfile.TemporaryDirectory() as td:
+        ind = os.path.join(td, "in")
+        outd = os.path.join(td, "out")
+        os.makedirs(ind)
+        os.makedirs(outd)
+        for k, v in inputs.items():
+            np.asarray(v, dtype=np.float64).tofile(os.path.join(ind, k + ".bin"))
+        if jit is not None:
+            jit.astype(np.float64).tofile(os.path.join(ind, "jitter.bin"))
+        cs = ",".join(f"{k}:{v}" for k, v in consts.items())
+        cmd = [DRIVER, f"dim={dim}", f"nx={nx}", f"gt={gt}", f"fem={deg}", f"qdim={qdim}",
+               f"im={im}", f"in={ind}", f"out={outd}", f"expr={expr}", "orders=2,1",
+               f"jitter={1 if jit is not None else 0}", f"consts={cs}"]
+        subprocess.run(cmd, check=True)
+        info = json.load(open(os.path.join(outd, "info.json")))
+
+        def rd(fn, dt=np.float64):
+            return np.fromfile(os.path.join(outd, fn), dtype=dt)
+        rec = dict(
+            points=rd("points.bin").reshape(-1, dim),
+            cvpts=rd("cvpts.bin", np.int64).reshape(E, -1),
+            dofs=rd("dofs.bin", np.int64).reshape(E, -1),
+            dofs0=rd("dofs0.bin", np.int64),
+            im_points=rd("im_points.bin").reshape(-1, dim),
+            im_weights=rd("im_weights.bin"),
+            base_val=rd("base_val.bin"),
+            base_grad=rd("base_grad.bin"),
+            K_rowptr=rd("K_rowptr.bin", np.int64),
+            K_colidx=rd("K_colidx.bin", np.int64).astype(np.int32),
+            K_vals=rd("K_vals.bin"),
+            R=rd("R.bin"),
+        )
+    for k, v in inputs.items():
+        rec["in_" + k] = np.asarray(v, dtype=np.float64)
+    if jit is not None:
+        rec["jitter"] = jit
+    meta = dict(name=name, dim=dim, gt=gt, degree=deg, qdim=qdim, im=im, nx=nx, expr=expr,
+                consts=consts, n_dof=info["n_dof"], nnz=info["nnz"], seed=seed)
+    rec["meta"] = np.array(json.dumps(meta))
+    np.savez_compressed(os.path.join(OUT, name + ".npz"), **rec)
+    print(name, "ndof", info["n_dof"], "nnz", info["nnz"])
+
+
+def main():
+    if not os.path.exists(DRIVER):
+        sys.exit(f"{DRIVER} missing: make -C oracle/refbuild REF=/root/reference")
+    for i, case in enumerate(CASES):
+        make_case(case, 1000 + i)
+
+
+if __name__ == "__main__":
+    main()
