@@ -1,0 +1,338 @@
+#!/usr/bin/env python3
+"""Benchmark of the generic-assembly hot path on GB300.
+
+Workload (one step): value re-assembly of the tangent matrix K and the
+residual R of 3-D linear elasticity on a unit cube split into 40^3 x 6
+P2 tetrahedra (384 000 elements, 1 594 323 DOFs, IM_TETRAHEDRON(5)), interior
+vertices jittered by U[-0.1h, 0.1h], Lame coefficients lambda = mu = 1 each
+scaled per element by lognormal(0, 0.2), nodal load N(0, 1):
+    (lambda*Div_u*Id(3)+2*mu*Sym(Grad_u)):Grad_Test_u - f.Test_u
+with the sparsity pattern cached (built once, at warm-up).  Synthetic
+seeded data stand in for the reference's configuration.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gfgpu|reference]
+
+One JSON line on rank 0.  value = elements/s with inputs resident in HBM;
+e2e = the same through the C ABI call with host buffers
+(gfgpu_assemble_host: u copied in, K values and R copied out every step).
+With N > 1 each rank assembles its own copy of the mesh (replicas: the
+path has no exchange step on one node); value sums the ranks' elements over
+the slowest rank's time.  --impl reference times the CPU implementation of
+the same path (the oracle restatement of the reference's exec loop,
+OpenMP over all host cores) on a bounded sub-mesh per step.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+EXPR = "(lambda*Div_u*Id(3)+2*mu*Sym(Grad_u)):Grad_Test_u - f.Test_u"
+METRIC = "elements/s assembled (K + residual), P2 tet elasticity"
+
+
+def make_problem(nx: int, seed: int = 2026):
+    import getfem_gb300 as g
+    rng = np.random.default_rng(seed)
+    h = 1.0 / nx
+    jit = rng.uniform(-0.1 * h, 0.1 * h, ((nx + 1) ** 3, 3))
+    mesh = g.Mesh.regular_unit(3, nx, "simplex", jitter=jit)
+    mf = g.MeshFem(mesh, 3, degree=2)
+    mf0 = g.MeshFem(mesh, 1, degree=0)
+    mim = g.MeshIm(mesh, "IM_TETRAHEDRON(5)")
+    E = mesh.nb_convex()
+    data = dict(u=rng.standard_normal(mf.nb_dof()) * 1e-3,
+                lam=np.exp(rng.normal(0.0, 0.2, E)), mu=np.exp(rng.normal(0.0, 0.2, E)),
+                f=rng.standard_normal(mf.nb_dof()))
+    ws = g.GaWorkspace()
+    ws.add_fem_variable("u", mf, U=data["u"])
+    ws.add_fem_constant("lambda", mf0, data["lam"])
+    ws.add_fem_constant("mu", mf0, data["mu"])
+    ws.add_fem_constant("f", mf, data["f"])
+    ws.add_expression(EXPR, mim)
+    return mesh, mf, mim, ws, data
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out = ""
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (self.out or "").splitlines():
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = max(mx, float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def algorithmic_bytes(mesh, mf, nnz):
+    """Bytes a value re-assembly must move at minimum (pattern cached):
+    K values written, R written, u and f read, DOF map and vertex
+    connectivity read, coordinates read, two per-element coefficients."""
+    E, nb = mf.dofs.shape
+    ndof = mf.nb_dof()
+    return dict(K=8 * nnz, R=8 * ndof, u=8 * ndof, f=8 * ndof, dofmap=4 * nb * E,
+                conn=4 * mesh.cvpts.shape[1] * E, coords=8 * mesh.points.size, coef=2 * 8 * E)
+
+
+def cpu_time_oracle(nx, nthreads, reps=1):
+    """One K + R assembly of the sub-mesh with the oracle; returns (seconds,
+    elements)."""
+    from oracle import gfref
+    mesh, mf, mim, ws, data = make_problem(nx, seed=7)
+    grp = ws.groups[0]
+    slots = {d.slot: np.asarray(d.values, dtype=float) for d in ws.data.values() if d.slot >= 0}
+    P2 = gfref.Problem(3, mesh.kind, 2, 3, mim.im, mesh.points, mesh.cvpts, mf.dofs, mf.nb_dof(),
+                       grp.order2, slots)
+    P1 = gfref.Problem(3, mesh.kind, 2, 3, mim.im, mesh.points, mesh.cvpts, mf.dofs, mf.nb_dof(),
+                       grp.order1, slots)
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        P2.matrix(nthreads)
+        P1.vector(nthreads)
+        ts.append(time.perf_counter() - t0)
+    return min(ts), mesh.nb_convex()
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    from oracle import gfref
+    gfref.build()
+    nthreads = os.cpu_count() or 1
+    nx = args.ref_nx
+    _, E = cpu_time_oracle(nx, nthreads)  # warm-up (also builds tables)
+    for _ in range(max(args.warmup - 1, 0)):
+        cpu_time_oracle(nx, nthreads)
+    total_t, total_e = 0.0, 0
+    for _ in range(args.steps):
+        t, E = cpu_time_oracle(nx, nthreads)
+        total_t += t
+        total_e += E
+    v = total_e / total_t
+    sample = f"regular_unit_mesh 3-D P2 tet elasticity, nx={nx} ({E} elements) per step, K + R"
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "elements/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * total_t / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": "P2 tet elasticity sub-mesh (CPU sample)", "nx": nx,
+                       "elements_per_step": E},
+            "cpu_baseline": {"value": v, "unit": "elements/s", "cores": nthreads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": v, "unit": "elements/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gfgpu", choices=["gfgpu", "reference"])
+    ap.add_argument("--nx", type=int, default=40)
+    ap.add_argument("--ref-nx", type=int, default=12)
+    ap.add_argument("--cpu-nx", type=int, default=16)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    from getfem_gb300 import _lib as L
+    lib = L.lib()
+    mesh, mf, mim, ws, data = make_problem(args.nx)
+    grp = ws.groups[0]
+    h = ws._plan(grp, grp.order1)
+    ws._upload(h, grp.order1, need_u=True)
+    E = mesh.nb_convex()
+    flags = L.WITH_VECTOR
+    L.check(lib.gfgpu_assemble(h, 2, flags, None))  # builds the pattern
+    L.check(lib.gfgpu_sync(h))
+    nr, nnz = C.c_int64(), C.c_int64()
+    L.check(lib.gfgpu_pattern_size(h, C.byref(nr), C.byref(nnz)))
+    nnz = nnz.value
+    for _ in range(args.warmup):
+        L.check(lib.gfgpu_assemble(h, 2, flags, None))
+    L.check(lib.gfgpu_sync(h))
+
+    # device-resident timing (inputs, T scratch and K all exceed the 129 MB L2)
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+    launches0 = lib.gfgpu_launch_count(h)
+    sampler = ClockSampler(local)
+    with sampler:
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            L.check(lib.gfgpu_assemble(h, 2, flags, None))
+        e1.record()
+        barrier()
+    launches = lib.gfgpu_launch_count(h) - launches0
+    L.check(lib.gfgpu_sync(h))
+    ms = e0.elapsed_time(e1) / args.steps
+
+    # per-kernel durations (CUDA events on the plan's stream)
+    kt = np.zeros(2)
+    nprof = min(args.steps, 20)
+    for _ in range(nprof):
+        L.check(lib.gfgpu_assemble(h, 2, flags | L.PROFILE, None))
+        t = (C.c_float * 2)()
+        L.check(lib.gfgpu_kernel_times(h, t, 2))
+        kt += np.array([t[0], t[1]])
+    kt /= nprof
+
+    # end to end through the C ABI with pinned host buffers
+    u_h = torch.from_numpy(np.ascontiguousarray(data["u"])).pin_memory()
+    vals_h = torch.empty(nnz, dtype=torch.float64).pin_memory()
+    vec_h = torch.empty(mf.nb_dof(), dtype=torch.float64).pin_memory()
+    e2e_steps = max(3, min(args.steps, 20))
+    for _ in range(2):
+        L.check(lib.gfgpu_assemble_host(h, C.c_void_p(u_h.data_ptr()), C.c_void_p(vals_h.data_ptr()),
+                                        C.c_void_p(vec_h.data_ptr())))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        L.check(lib.gfgpu_assemble_host(h, C.c_void_p(u_h.data_ptr()), C.c_void_p(vals_h.data_ptr()),
+                                        C.c_void_p(vec_h.data_ptr())))
+    barrier()
+    e2e_ms = 1e3 * (time.perf_counter() - t0) / e2e_steps
+
+    if dist is not None:
+        tt = torch.tensor([ms, e2e_ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms, e2e_ms = float(tt[0]), float(tt[1])
+    value = world * E / (ms * 1e-3)
+    e2e = world * E / (e2e_ms * 1e-3)
+    if rank != 0:
+        dist.destroy_process_group()
+        return
+
+    import json as _json
+    peaks = {}
+    try:
+        peaks = _json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    ab = algorithmic_bytes(mesh, mf, nnz)
+    gather_bytes = ab["K"] + ab["R"] + ab["u"] + ab["f"] + ab["dofmap"]
+    step_bytes = sum(ab.values())
+    gather_gbs = gather_bytes / (kt[1] * 1e-3) / 1e9
+    fp64_peak = C.c_double()
+    L.check(lib.gfgpu_fp64_peak(0, C.byref(fp64_peak)))
+    # FP64 flops executed by the gather: 2 per reference-tensor term per
+    # element entry, 2 for the residual product, 2 for the load term
+    from getfem_gb300.tables import simplex_term_count
+    nterm_sum, nb = simplex_term_count(3, 2, "IM_TETRAHEDRON(5)")
+    qd = 3
+    gflop = E * (2.0 * nterm_sum * qd * qd + 2.0 * nb * nb * qd + 2.0 * nb * nb * qd * qd
+                 + 3.0 * nb * nb * qd) / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "gather_p2tet_traffic.json")
+    if os.path.exists(prof):
+        try:
+            traffic = _json.load(open(prof)).get("bytes_per_element") * E
+        except (ValueError, TypeError):
+            traffic = None
+    cpu = None
+    if not args.no_cpu:
+        nthreads = os.cpu_count() or 1
+        t, Es = cpu_time_oracle(args.cpu_nx, nthreads, reps=2)
+        cpu = {"value": Es / t, "unit": "elements/s", "cores": nthreads, "kind": "port",
+               "sample": f"oracle (CPU restatement of the reference exec loop), OpenMP "
+                         f"{nthreads} threads, K + R of the same problem at nx={args.cpu_nx} "
+                         f"({Es} elements), best of 2"}
+    line = {
+        "metric": METRIC, "value": value, "unit": "elements/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded jittered mesh, lognormal coefficients, N(0,1) load)",
+        "config": {"workload": f"3-D P2 tet linear elasticity, regular_unit_mesh {args.nx}^3 x 6 tets, "
+                               "IM_TETRAHEDRON(5), K + R value re-assembly, pattern cached",
+                   "elements": E, "n_dof": mf.nb_dof(), "nnz": nnz,
+                   "l2": "inputs larger than L2 (K values, scratch and DOF data >> 129 MB)",
+                   "dofs_per_s": value * mf.nb_dof() / E},
+        "kernels_ms": {"element_pass": float(kt[0]), "row_gather": float(kt[1])},
+        "roofline": {"bound": "hbm", "kernel": "row_gather", "achieved": gather_gbs,
+                     "peak": hbm_peak, "unit": "GB/s", "frac": gather_gbs / hbm_peak,
+                     "traffic": traffic, "algorithmic_bytes": gather_bytes,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
+        "fp64": {"achieved_tflops": gflop / (kt[1] * 1e-3) / 1e3,
+                 "peak_tflops": fp64_peak.value,
+                 "frac": gflop / (kt[1] * 1e-3) / 1e3 / fp64_peak.value,
+                 "peak_source": "gfgpu_fp64_peak FMA microbenchmark, this run"},
+        "step_hbm_frac": step_bytes / (ms * 1e-3) / 1e9 / hbm_peak,
+        "e2e": {"value": e2e, "unit": "elements/s", "h2d_bytes_per_step": 8 * mf.nb_dof(),
+                "d2h_bytes_per_step": 8 * nnz + 8 * mf.nb_dof(), "ms_per_step": e2e_ms},
+        "gpu_launches": int(launches), "cpu_baseline": cpu, "clocks": sampler.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -21,6 +21,7 @@ MAX_SLOTS = 8
 SLOT_U = 0
 REBUILD_PATTERN = 1
 WITH_VECTOR = 2
+PROFILE = 4
 
 _STATUS_NAMES = {
     E_INVALID: "GFGPU_E_INVALID", E_UNSUPPORTED: "GFGPU_E_UNSUPPORTED", E_CUDA: "GFGPU_E_CUDA",
@@ -92,6 +93,8 @@ _PROTOS = {
     "gfgpu_sync": (C.c_int, [C.c_void_p]),
     "gfgpu_launch_count": (C.c_int64, [C.c_void_p]),
     "gfgpu_copy_result": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "gfgpu_kernel_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int32]),
+    "gfgpu_fp64_peak": (C.c_int, [C.c_int32, C.POINTER(C.c_double)]),
 }
 
 

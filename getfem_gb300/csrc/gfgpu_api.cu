@@ -115,7 +115,7 @@ int status_from_err(int e) {
 
 int build_pattern(Plan &P) {
   // counts per row and per node
-  GF_CUDA(cudaMemsetAsync(P.d_count, 0, (P.n_dof + 1) * sizeof(int32_t), P.stream));
+  GF_CUDA(cudaMemsetAsync(P.d_count, 0, (P.n_dof + 1) * sizeof(int64_t), P.stream));
   GF_CUDA(cudaMemsetAsync(P.d_ncount, 0, (P.n_nodes + 1) * sizeof(int32_t), P.stream));
   GF_CUDA(launch_pattern_count(P));
   size_t need = 0, need2 = 0, need3 = 0;
@@ -258,6 +258,7 @@ int gfgpu_plan_create(const gfgpu_space *space, const gfgpu_form *form, void *cu
     }
     P->max_cand = int32_t(P->max_adj * nb);
     if (P->max_cand > 4096) throw std::runtime_error("node valence too large for the pattern kernel");
+    if (P->nb > 128) throw std::runtime_error("more than 128 local nodes per element");
 #define CHK(x)                   \
   if ((rc = (x)) != GFGPU_OK) { \
     gfgpu_plan_destroy(P);       \
@@ -320,6 +321,8 @@ void gfgpu_plan_destroy(gfgpu_plan *P) {
   dfree(P->d_ncount);
   dfree(P->d_cub);
   for (int i = 0; i < GFGPU_MAX_SLOTS; ++i) dfree(P->slot_own[i]);
+  for (int i = 0; i < 4; ++i)
+    if (P->ev[i]) cudaEventDestroy(P->ev[i]);
   delete P;
 }
 
@@ -383,16 +386,22 @@ int gfgpu_assemble(gfgpu_plan *P, int32_t order, int32_t flags, double *potentia
   const bool want_R = order == 1 || (flags & 2);
   int rc = check_slots(*P, want_R);
   if (rc) return rc;
+  const bool prof = (flags & GFGPU_PROFILE) != 0;
+  if (prof && !P->ev[0])
+    for (int i = 0; i < 4; ++i) GF_CUDA(cudaEventCreate(&P->ev[i]));
   GF_CUDA(cudaMemsetAsync(P->d_err, 0, sizeof(int), P->stream));
+  if (prof) GF_CUDA(cudaEventRecord(P->ev[0], P->stream));
   GF_CUDA(launch_simplex_element_pass(*P));
-  if (want_K && (P->nnz < 0 || (flags & GFGPU_REBUILD_PATTERN))) {
+  if (prof) GF_CUDA(cudaEventRecord(P->ev[1], P->stream));
+  if ((want_K && (P->nnz < 0 || (flags & GFGPU_REBUILD_PATTERN))) || P->nnz < 0) {
+    // the pattern is built at the first order-2 assembly; an order-1
+    // assembly needs the node-level part of it for its row walk
     if ((rc = build_pattern(*P))) return rc;
   }
-  if (want_R && !want_K && P->nnz < 0) {
-    // the gather walks the node-level pattern; build it once
-    if ((rc = build_pattern(*P))) return rc;
-  }
+  if (prof) GF_CUDA(cudaEventRecord(P->ev[2], P->stream));
   GF_CUDA(launch_gather(*P, want_K, want_R));
+  if (prof) GF_CUDA(cudaEventRecord(P->ev[3], P->stream));
+  P->profiled = prof;
   return GFGPU_OK;
 }
 
@@ -405,7 +414,7 @@ int gfgpu_assemble_host(gfgpu_plan *P, const double *u, double *vals, double *ve
   if (!P) return GFGPU_E_INVALID;
   int rc;
   if (u && (rc = gfgpu_set_data(P, GFGPU_SLOT_U, u, P->n_dof, 0))) return rc;
-  if ((rc = gfgpu_assemble(P, 2, vec ? 2 : 0, nullptr))) return rc;
+  if ((rc = gfgpu_assemble(P, 2, vec ? GFGPU_WITH_VECTOR : 0, nullptr))) return rc;
   if (vals) GF_CUDA(cudaMemcpyAsync(vals, P->d_vals, size_t(P->nnz) * sizeof(double),
                                     cudaMemcpyDeviceToHost, P->stream));
   if (vec) GF_CUDA(cudaMemcpyAsync(vec, P->d_vec, size_t(P->n_dof) * sizeof(double),
@@ -458,6 +467,18 @@ int gfgpu_device_vector(gfgpu_plan *P, double **vec) {
 }
 
 int64_t gfgpu_launch_count(gfgpu_plan *P) { return P ? P->launches : -1; }
+
+int gfgpu_kernel_times(gfgpu_plan *P, float *times, int32_t n) {
+  if (!P || !times || n < 2) return GFGPU_E_INVALID;
+  if (!P->profiled) {
+    set_last_error("last assembly was not profiled (GFGPU_PROFILE)");
+    return GFGPU_E_STATE;
+  }
+  GF_CUDA(cudaEventSynchronize(P->ev[3]));
+  GF_CUDA(cudaEventElapsedTime(&times[0], P->ev[0], P->ev[1]));
+  GF_CUDA(cudaEventElapsedTime(&times[1], P->ev[2], P->ev[3]));
+  return GFGPU_OK;
+}
 
 int gfgpu_copy_result(gfgpu_plan *P, int32_t which, void *dst) {
   if (!P || !dst || which < 0 || which > 3) {

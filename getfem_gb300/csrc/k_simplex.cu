@@ -37,6 +37,7 @@ namespace gfgpu {
 namespace {
 
 constexpr int kWarp = 32;
+constexpr int kMaxLocal = 128;  // local nodes per element held in shared memory
 
 __device__ __forceinline__ void set_err(int *err, int bit) { atomicOr(err, bit); }
 
@@ -259,12 +260,12 @@ template <class Src, int MODE>
 __global__ void __launch_bounds__(128) pattern_kernel(
     int64_t n_nodes, int qd, int nb, const int32_t *__restrict__ adj_ptr,
     const int32_t *__restrict__ adj, const int32_t *__restrict__ enode, Src src, int cap,
-    int32_t *__restrict__ rowcount, int32_t *__restrict__ ncount,
+    int64_t *__restrict__ rowcount, int32_t *__restrict__ ncount,
     const int64_t *__restrict__ rowptr, int32_t *__restrict__ colidx,
     const int64_t *__restrict__ nptr, int32_t *__restrict__ ncol, int *__restrict__ err) {
   extern __shared__ int smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  int *cand = smem + wib * (2 * cap + 32);
+  int *cand = smem + wib * (2 * cap + kMaxLocal);
   unsigned *bits = reinterpret_cast<unsigned *>(cand + cap);
   int *ljs = reinterpret_cast<int *>(bits + cap);
   int64_t node = blockIdx.x * int64_t(blockDim.x >> 5) + wib;
@@ -317,6 +318,7 @@ __global__ void __launch_bounds__(128) pattern_kernel(
     for (int a = 0; a < qd; ++a) {
       unsigned am = ((1u << qd) - 1u) << (a * qd);
       int64_t base = rowptr[node * qd + a];
+      const int64_t rowend = rowptr[node * qd + a + 1];
       for (int j0 = 0; j0 < ns; j0 += kWarp) {
         int j = j0 + lane;
         unsigned m = j < ns ? (bits[j] & am) : 0u;
@@ -330,16 +332,26 @@ __global__ void __launch_bounds__(128) pattern_kernel(
         int pos = incl - c;
         if (j < ns)
           for (int b = 0; b < qd; ++b)
-            if (m & (1u << (a * qd + b))) colidx[base + pos++] = cand[j] * qd + b;
+            if (m & (1u << (a * qd + b))) {
+              // the count pass sized the row; never write past it
+              if (base + pos < rowend) colidx[base + pos] = cand[j] * qd + b;
+              else set_err(err, ERR_CAPACITY);
+              ++pos;
+            }
         base += total;
       }
     }
     int64_t nb0 = nptr[node];
+    const int64_t nend = nptr[node + 1];
     for (int j0 = 0; j0 < ns; j0 += kWarp) {
       int j = j0 + lane;
       bool keep = j < ns && bits[j] != 0u;
       unsigned m = __ballot_sync(0xffffffffu, keep);
-      if (keep) ncol[nb0 + __popc(m & ((1u << lane) - 1u))] = cand[j];
+      int64_t at = nb0 + __popc(m & ((1u << lane) - 1u));
+      if (keep) {
+        if (at < nend) ncol[at] = cand[j];
+        else set_err(err, ERR_CAPACITY);
+      }
       nb0 += __popc(m);
     }
   }
@@ -360,7 +372,7 @@ __global__ void __launch_bounds__(128) gather_kernel(
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int qq = qd * qd;
   // per warp: acc[ms*qq] doubles, then pos[ms*qq] ints, slots[ms] ints, ljs[nb]
-  const size_t per_warp = size_t(ms) * qq * 8 + size_t(ms) * qq * 4 + size_t(ms) * 4 + 4 * 128;
+  const size_t per_warp = size_t(ms) * qq * 8 + size_t(ms) * qq * 4 + size_t(ms) * 4 + 4 * kMaxLocal;
   char *base = reinterpret_cast<char *>(dsm) + wib * ((per_warp + 15) / 16 * 16);
   double *acc = reinterpret_cast<double *>(base);
   int *pos = reinterpret_cast<int *>(acc + size_t(ms) * qq);
@@ -464,9 +476,9 @@ SimplexSource make_simplex_source(Plan &P) {
 
 constexpr int kWarpsPerBlock = 4;
 
-size_t pattern_smem(int cap) { return size_t(kWarpsPerBlock) * (2 * cap + 32) * sizeof(int); }
+size_t pattern_smem(int cap) { return size_t(kWarpsPerBlock) * (2 * cap + kMaxLocal) * sizeof(int); }
 size_t gather_smem(int ms, int qd) {
-  size_t per = size_t(ms) * qd * qd * 12 + size_t(ms) * 4 + 4 * 128;
+  size_t per = size_t(ms) * qd * qd * 12 + size_t(ms) * 4 + 4 * kMaxLocal;
   return size_t(kWarpsPerBlock) * ((per + 15) / 16 * 16);
 }
 

@@ -95,11 +95,13 @@ struct Plan {
   double *d_vec = nullptr;      // n_dof
   double *d_pot = nullptr;      // 1
   int *d_err = nullptr;
-  int32_t *d_count = nullptr;   // scratch counters (n_dof)
+  int64_t *d_count = nullptr;   // scratch row counts (n_dof + 1)
   int32_t *d_ncount = nullptr;  // (n_nodes)
   void *d_cub = nullptr;
   size_t cub_bytes = 0;
   int64_t launches = 0;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  bool profiled = false;
 };
 
 // kernels (k_simplex.cu)

@@ -192,6 +192,10 @@ int gfgpu_device_csr(gfgpu_plan *plan, const int64_t **rowptr, const int32_t **c
 int gfgpu_device_vector(gfgpu_plan *plan, double **vec);
 
 #define GFGPU_REBUILD_PATTERN 1 /* rebuild the CSR pattern at this call */
+#define GFGPU_WITH_VECTOR 2     /* order 2: also produce the order-1 vector
+                                   in the same pass */
+#define GFGPU_PROFILE 4         /* record CUDA events around each kernel of
+                                   this call (gfgpu_kernel_times) */
 
 /* Assembles on the device.  order 2: K values into the plan's CSR (the
    pattern is built at the first call, or when GFGPU_REBUILD_PATTERN);
@@ -220,6 +224,16 @@ int gfgpu_copy_result(gfgpu_plan *plan, int32_t which, void *dst);
 /* Waits for the plan's stream and reports the device error word
    (GFGPU_E_JACOBIAN / GFGPU_E_NAN) of the last assembly. */
 int gfgpu_sync(gfgpu_plan *plan);
+
+/* Durations (ms, CUDA events on the plan's stream) of the kernels of the
+   last gfgpu_assemble call made with GFGPU_PROFILE: times[0] = element
+   pass, times[1] = row gather.  Waits for the stream. */
+int gfgpu_kernel_times(gfgpu_plan *plan, float *times, int32_t n);
+
+/* Throughput microbenchmark of this GPU's FP64 FMA pipe (kind 0) or FP64
+   tensor pipe (kind 1, mma.sync m8n8k4 f64), in TFLOP/s; used as the
+   compute roofline of the FP64 kernels. */
+int gfgpu_fp64_peak(int32_t kind, double *tflops);
 
 /* Number of kernel launches issued by the plan since creation. */
 int64_t gfgpu_launch_count(gfgpu_plan *plan);

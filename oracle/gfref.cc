@@ -401,18 +401,25 @@ void exec_range(Problem &P, int order, int64_t e0, int64_t e1, Outputs &out) {
           double c1 = coef_at(p, T.c[1], e, edofs, phi, nb) * sc;
           double c2 = coef_at(p, T.c[2], e, edofs, phi, nb) * sc;
           if (order == 2) {
-            for (int j = 0; j < nb; ++j)
-              for (int b = 0; b < qd; ++b)
-                for (int i = 0; i < nb; ++i)
-                  for (int a = 0; a < qd; ++a) {
-                    double v = 0;
-                    // c0 d_ak d_bl + c1 d_ab d_kl + c2 d_al d_kb
-                    if (qd > 1) v += c0 * g[i * dim + a] * g[j * dim + b];
-                    if (a == b)
-                      for (int k = 0; k < dim; ++k) v += c1 * g[i * dim + k] * g[j * dim + k];
-                    if (qd > 1) v += c2 * g[i * dim + b] * g[j * dim + a];
-                    t[size_t(j * qd + b) * s + i * qd + a] += v;
-                  }
+            // t[(i,a),(j,b)] = c0 g_ia g_jb + c1 d_ab g_i.g_j + c2 g_ib g_ja
+            for (int j = 0; j < nb; ++j) {
+              const double *gj = &g[j * dim];
+              for (int i = 0; i < nb; ++i) {
+                const double *gi = &g[i * dim];
+                double gg = 0;
+                for (int k = 0; k < dim; ++k) gg += gi[k] * gj[k];
+                gg *= c1;
+                if (qd == 1) {
+                  t[size_t(j) * s + i] += gg;
+                  continue;
+                }
+                for (int b = 0; b < qd; ++b) {
+                  double *tc = &t[size_t(j * qd + b) * s + i * qd];
+                  for (int a = 0; a < qd; ++a)
+                    tc[a] += c0 * gi[a] * gj[b] + c2 * gi[b] * gj[a] + (a == b ? gg : 0.0);
+                }
+              }
+            }
           } else {
             // Grad_u (qd x dim)
             double Gu[9] = {0};
