@@ -152,10 +152,14 @@ int build_pattern(Plan &P) {
   dfree(P.d_colidx);
   dfree(P.d_vals);
   dfree(P.d_ncol);
+  dfree(P.d_nbits);
+  dfree(P.d_slotmap);
   int rc;
   if ((rc = dalloc(&P.d_colidx, size_t(nnz)))) return rc;
   if ((rc = dalloc(&P.d_vals, size_t(nnz)))) return rc;
   if ((rc = dalloc(&P.d_ncol, size_t(nn)))) return rc;
+  if ((rc = dalloc(&P.d_nbits, size_t(nn)))) return rc;
+  if ((rc = dalloc(&P.d_slotmap, size_t(P.n_elements) * P.nb * P.nb))) return rc;
   P.nnz = nnz;
   P.max_slots = mx;
   GF_CUDA(launch_pattern_fill(P));
@@ -259,6 +263,7 @@ int gfgpu_plan_create(const gfgpu_space *space, const gfgpu_form *form, void *cu
     P->max_cand = int32_t(P->max_adj * nb);
     if (P->max_cand > 4096) throw std::runtime_error("node valence too large for the pattern kernel");
     if (P->nb > 128) throw std::runtime_error("more than 128 local nodes per element");
+    if (P->max_cand > 32767) throw std::runtime_error("row slot index exceeds int16");
 #define CHK(x)                   \
   if ((rc = (x)) != GFGPU_OK) { \
     gfgpu_plan_destroy(P);       \
@@ -314,6 +319,8 @@ void gfgpu_plan_destroy(gfgpu_plan *P) {
   dfree(P->d_vals);
   dfree(P->d_nptr);
   dfree(P->d_ncol);
+  dfree(P->d_nbits);
+  dfree(P->d_slotmap);
   dfree(P->d_vec);
   dfree(P->d_pot);
   dfree(P->d_err);
@@ -391,7 +398,7 @@ int gfgpu_assemble(gfgpu_plan *P, int32_t order, int32_t flags, double *potentia
     for (int i = 0; i < 4; ++i) GF_CUDA(cudaEventCreate(&P->ev[i]));
   GF_CUDA(cudaMemsetAsync(P->d_err, 0, sizeof(int), P->stream));
   if (prof) GF_CUDA(cudaEventRecord(P->ev[0], P->stream));
-  GF_CUDA(launch_simplex_element_pass(*P));
+  GF_CUDA(launch_simplex_element_pass(*P, want_R));
   if (prof) GF_CUDA(cudaEventRecord(P->ev[1], P->stream));
   if ((want_K && (P->nnz < 0 || (flags & GFGPU_REBUILD_PATTERN))) || P->nnz < 0) {
     // the pattern is built at the first order-2 assembly; an order-1

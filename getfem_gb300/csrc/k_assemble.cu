@@ -1,0 +1,381 @@
+// Sparsity pattern build and row gather over element matrices (sm_103a, FP64).
+//
+// Every element kernel of the backend writes, per element e, its element
+// matrix K_e (s x s, s = nb*qd, rows = test DOFs (li,a), row-major with an
+// even row stride), an element vector V_e (s) and the drop threshold
+// 1e-14 max|K_e| (compile_and_exec.cc:5453) into a scratch array.  The two
+// kernels here turn those into the global CSR matrix and vector:
+//
+//  * pattern (once per mesh): one warp per DOF node gathers the nodes of
+//    the node's elements, sorts and uniques them in shared memory, and marks
+//    the (row component, column component) pairs that at least one element
+//    inserts, i.e. |e| > threshold (add_elem_matrix, compile_and_exec.cc:
+//    4853-4936: an entry exists if any element inserted it; sums that cancel
+//    stay stored).  Row lengths, column indices, a node-level slot list with
+//    keep bits, and the slot of every local node of every adjacent element
+//    (slotmap) are written.
+//
+//  * gather (every assembly): one warp per DOF node walks the node's
+//    elements in ascending order.  The node's rows of K_e are double-buffered
+//    in shared memory with cp.async; lane (lj,b) adds K_e[(li,a),(lj,b)] to
+//    the row accumulator of slot(lj) when it is above the element's
+//    threshold and in the pattern.  Each CSR entry is therefore summed in
+//    element order, like the reference's column merge, without atomics:
+//    results are bit-reproducible.  The vector is R = sum V_e, where each
+//    element kernel has put its whole contribution (K_e u_e + load for a
+//    linear form, with no threshold as in the reference's vector assembly,
+//    or the element residual of a nonlinear form) into V_e.
+#include <cub/cub.cuh>
+
+#include "k_common.cuh"
+#include "plan.h"
+
+namespace gfgpu {
+
+namespace {
+
+constexpr int kMaxLocal = 128;  // local nodes per element held in shared memory
+constexpr int kWarpsPerBlock = 4;
+
+// ------------------------------------------------------------- pattern
+
+template <int MODE>
+__global__ void __launch_bounds__(128) pattern_kernel(
+    int64_t n_nodes, KeLayout L, const int32_t *__restrict__ adj_ptr,
+    const int32_t *__restrict__ adj, const int32_t *__restrict__ enode,
+    const double *__restrict__ elem, int cap, int64_t *__restrict__ rowcount,
+    int32_t *__restrict__ ncount, const int64_t *__restrict__ rowptr,
+    int32_t *__restrict__ colidx, const int64_t *__restrict__ nptr, int32_t *__restrict__ ncol,
+    uint16_t *__restrict__ nbits, int16_t *__restrict__ slotmap, int *__restrict__ err) {
+  extern __shared__ int smem[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  int *cand = smem + wib * (3 * cap + kMaxLocal);
+  unsigned *bits = reinterpret_cast<unsigned *>(cand + cap);
+  int *keptidx = reinterpret_cast<int *>(bits + cap);
+  int *ljs = keptidx + cap;
+  const int64_t node = blockIdx.x * int64_t(blockDim.x >> 5) + wib;
+  if (node >= n_nodes) return;
+  const int nb = L.nb, qd = L.qd;
+  const int a0 = adj_ptr[node], a1 = adj_ptr[node + 1];
+  int n = 0;
+  for (int k = a0; k < a1; ++k) {
+    const int el = adj[k] / nb;
+    if (n + nb > cap) {
+      if (lane == 0) set_err(err, ERR_CAPACITY);
+      return;
+    }
+    for (int j = lane; j < nb; j += kWarp) cand[n + j] = enode[int64_t(el) * nb + j];
+    n += nb;
+  }
+  int np = 1;
+  while (np < n) np <<= 1;
+  for (int j = n + lane; j < np; j += kWarp) cand[j] = 0x7fffffff;
+  __syncwarp();
+  warp_sort(cand, np);
+  const int ns = warp_unique(cand, n);
+  for (int j = lane; j < ns; j += kWarp) bits[j] = 0u;
+  __syncwarp();
+  for (int k = a0; k < a1; ++k) {
+    const int el = adj[k] / nb, li = adj[k] % nb;
+    const double *Ke = elem + int64_t(el) * L.stride;
+    const long long thr = __double_as_longlong(Ke[L.off_thr]);
+    for (int j = lane; j < nb; j += kWarp) ljs[j] = bsearch_slot(cand, ns, enode[int64_t(el) * nb + j]);
+    __syncwarp();
+    for (int c = lane; c < nb * qd; c += kWarp) {
+      const int lj = c / qd, b = c % qd;
+      unsigned m = 0u;
+      for (int a = 0; a < qd; ++a)
+        if (abs_greater(Ke[(li * qd + a) * L.rowstride + c], thr)) m |= 1u << (a * qd + b);
+      if (m) atomicOr(&bits[ljs[lj]], m);
+    }
+    __syncwarp();
+  }
+  if (MODE == 0) {
+    for (int a = 0; a < qd; ++a) {
+      const unsigned am = ((1u << qd) - 1u) << (a * qd);
+      int cnt = 0;
+      for (int j = lane; j < ns; j += kWarp) cnt += __popc(bits[j] & am);
+      for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+      if (lane == 0) rowcount[node * qd + a] = cnt;
+    }
+    int kept = 0;
+    for (int j = lane; j < ns; j += kWarp) kept += bits[j] != 0u;
+    for (int o = 16; o > 0; o >>= 1) kept += __shfl_xor_sync(0xffffffffu, kept, o);
+    if (lane == 0) ncount[node] = kept;
+    return;
+  }
+  for (int a = 0; a < qd; ++a) {
+    const unsigned am = ((1u << qd) - 1u) << (a * qd);
+    int64_t base = rowptr[node * qd + a];
+    const int64_t rowend = rowptr[node * qd + a + 1];
+    for (int j0 = 0; j0 < ns; j0 += kWarp) {
+      const int j = j0 + lane;
+      const unsigned m = j < ns ? (bits[j] & am) : 0u;
+      const int c = __popc(m);
+      int incl = c;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+      }
+      const int total = __shfl_sync(0xffffffffu, incl, 31);
+      int pos = incl - c;
+      if (j < ns)
+        for (int b = 0; b < qd; ++b)
+          if (m & (1u << (a * qd + b))) {
+            // the count pass sized the row; never write past it
+            if (base + pos < rowend) colidx[base + pos] = cand[j] * qd + b;
+            else set_err(err, ERR_CAPACITY);
+            ++pos;
+          }
+      base += total;
+    }
+  }
+  int64_t nb0 = nptr[node];
+  const int64_t nend = nptr[node + 1];
+  for (int j0 = 0; j0 < ns; j0 += kWarp) {
+    const int j = j0 + lane;
+    const bool keep = j < ns && bits[j] != 0u;
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    const int rank = int(nb0 - nptr[node]) + __popc(m & ((1u << lane) - 1u));
+    const int64_t at = nb0 + __popc(m & ((1u << lane) - 1u));
+    if (j < ns) keptidx[j] = keep ? rank : -1;
+    if (keep) {
+      if (at < nend) {
+        ncol[at] = cand[j];
+        nbits[at] = uint16_t(bits[j]);
+      } else {
+        set_err(err, ERR_CAPACITY);
+      }
+    }
+    nb0 += __popc(m);
+  }
+  __syncwarp();
+  for (int k = a0; k < a1; ++k) {
+    const int el = adj[k] / nb;
+    for (int j = lane; j < nb; j += kWarp) {
+      const int full = bsearch_slot(cand, ns, enode[int64_t(el) * nb + j]);
+      slotmap[int64_t(k) * nb + j] = int16_t(full >= 0 ? keptidx[full] : -1);
+    }
+  }
+}
+
+// -------------------------------------------------------------- gather
+
+__host__ __device__ __forceinline__ size_t gather_warp_bytes(int ms, int qd, int rowstride,
+                                                             int mad) {
+  const size_t b = size_t(2 * qd * rowstride) * 8 + size_t(ms) * qd * qd * 8 +
+                   size_t(mad) * 4 + size_t(ms) * 2;
+  return (b + 15) / 16 * 16;
+}
+
+// QD components, R = ceil(nb*qd/32) lane rounds over the columns of a row.
+template <int QD, int R>
+__global__ void __launch_bounds__(128) gather_kernel(
+    int64_t n_nodes, KeLayout L, const int32_t *__restrict__ adj_ptr,
+    const int32_t *__restrict__ adj, const int32_t *__restrict__ enode,
+    const double *__restrict__ elem, int ms, int mad, const int64_t *__restrict__ nptr,
+    const int32_t *__restrict__ ncol, const uint16_t *__restrict__ nbits,
+    const int16_t *__restrict__ slotmap, const int64_t *__restrict__ rowptr,
+    double *__restrict__ vals, bool want_K, bool want_R, double *__restrict__ vec,
+    int *__restrict__ err) {
+  constexpr int QQ = QD * QD;
+  extern __shared__ __align__(16) double dsm[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int nb = L.nb, S = L.s, rs = L.rowstride, blk = QD * rs;
+  char *base = reinterpret_cast<char *>(dsm) + wib * gather_warp_bytes(ms, QD, rs, mad);
+  double *Kbuf = reinterpret_cast<double *>(base);                // 2 x blk
+  double *acc = Kbuf + 2 * blk;                                    // ms * QQ
+  int *adjs = reinterpret_cast<int *>(acc + size_t(ms) * QQ);     // mad
+  uint16_t *bits = reinterpret_cast<uint16_t *>(adjs + mad);      // ms
+  const int64_t node = blockIdx.x * int64_t(blockDim.x >> 5) + wib;
+  if (node >= n_nodes) return;
+  const int64_t s0 = nptr[node];
+  const int ns = int(nptr[node + 1] - s0);
+  const int a0 = adj_ptr[node], nadj = adj_ptr[node + 1] - a0;
+  if (ns > ms || nadj > mad) {
+    if (lane == 0) set_err(err, ERR_CAPACITY);
+    return;
+  }
+  for (int j = lane; j < nadj; j += kWarp) adjs[j] = adj[a0 + j];
+  if (want_K) {
+    for (int j = lane; j < ns * QQ; j += kWarp) acc[j] = 0.0;
+    for (int j = lane; j < ns; j += kWarp) bits[j] = nbits[s0 + j];
+  }
+  __syncwarp();
+  const int nchunk = blk / 2;  // 16-byte chunks of the row block
+  auto issue = [&](int k) {
+    const int code = adjs[k];
+    const double *src = elem + int64_t(code / nb) * L.stride + int64_t(code % nb) * blk;
+    double *dst = Kbuf + (k & 1) * blk;
+    for (int c = lane; c < nchunk; c += kWarp) cp_async16(dst + 2 * c, src + 2 * c);
+  };
+  // per-lane data of an element: slots of the columns the lane handles,
+  // threshold, and the element vector entry of component `lane`
+  int sl[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) sl[r] = -1;
+  double thr_d = 0.0, ve = 0.0;
+  auto fetch = [&](int k, int (&s_)[R], double &t_, double &v_) {
+    const int code = adjs[k];
+    const int el = code / nb, li = code % nb;
+    const double *Ke = elem + int64_t(el) * L.stride;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int c = lane + 32 * r;
+      s_[r] = (c < S && want_K) ? slotmap[int64_t(a0 + k) * nb + c / QD] : -1;
+    }
+    t_ = Ke[L.off_thr];
+    v_ = (want_R && lane < QD) ? Ke[L.off_vec + li * QD + lane] : 0.0;
+  };
+  if (nadj > 0) {
+    if (want_K) issue(0);
+    fetch(0, sl, thr_d, ve);
+  }
+  cp_async_commit();
+  double rvec = 0.0;
+  for (int k = 0; k < nadj; ++k) {
+    int sl_n[R];
+    double thr_n = 0.0, ve_n = 0.0;
+    if (k + 1 < nadj) {
+      if (want_K) issue(k + 1);
+      fetch(k + 1, sl_n, thr_n, ve_n);
+    }
+    cp_async_commit();
+    cp_async_wait1();
+    __syncwarp();
+    rvec += ve;
+    if (want_K) {
+      const double *Kb = Kbuf + (k & 1) * blk;
+      const long long tb = __double_as_longlong(thr_d);
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int c = lane + 32 * r;
+        if (c < S && sl[r] >= 0) {
+          const int b = c % QD;
+          const unsigned sb = bits[sl[r]];
+#pragma unroll
+          for (int a = 0; a < QD; ++a) {
+            const double x = Kb[a * rs + c];
+            if (((sb >> (a * QD + b)) & 1u) && abs_greater(x, tb))
+              acc[(sl[r] * QD + a) * QD + b] += x;
+          }
+        }
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int r = 0; r < R; ++r) sl[r] = sl_n[r];
+    thr_d = thr_n, ve = ve_n;
+  }
+  if (want_K) {
+#pragma unroll
+    for (int a = 0; a < QD; ++a) {
+      const unsigned am = ((1u << QD) - 1u) << (a * QD);
+      int64_t p = rowptr[node * QD + a];
+      const int64_t pend = rowptr[node * QD + a + 1];
+      for (int j0 = 0; j0 < ns; j0 += kWarp) {
+        const int j = j0 + lane;
+        const unsigned m = j < ns ? (unsigned(bits[j]) & am) : 0u;
+        const int c = __popc(m);
+        int incl = c;
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += y;
+        }
+        int64_t q = p + incl - c;
+        if (m) {
+#pragma unroll
+          for (int b = 0; b < QD; ++b)
+            if (m & (1u << (a * QD + b))) {
+              if (q < pend) vals[q] = acc[(j * QD + a) * QD + b];
+              else set_err(err, ERR_CAPACITY);
+              ++q;
+            }
+        }
+        p += __shfl_sync(0xffffffffu, incl, 31);
+      }
+    }
+  }
+  if (want_R && lane < QD) {
+    if (!isfinite(rvec)) set_err(err, ERR_NAN);
+    vec[node * QD + lane] = rvec;
+  }
+}
+
+size_t pattern_smem(int cap) { return size_t(kWarpsPerBlock) * (3 * cap + kMaxLocal) * sizeof(int); }
+
+int pattern_cap(const Plan &P) {
+  int cap = P.max_cand < 32 ? 32 : P.max_cand;
+  int np = 1;
+  while (np < cap) np <<= 1;
+  return np;
+}
+
+template <int QD, int R>
+cudaError_t launch_gather_t(Plan &P, bool want_K, bool want_R) {
+  const int ms = P.max_slots < 1 ? 1 : P.max_slots;
+  const int mad = P.max_adj < 1 ? 1 : P.max_adj;
+  const size_t smem = size_t(kWarpsPerBlock) * gather_warp_bytes(ms, QD, P.lay.rowstride, mad);
+  cudaError_t ce = cudaFuncSetAttribute(gather_kernel<QD, R>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (ce != cudaSuccess) return ce;
+  const unsigned blocks = unsigned((P.n_nodes + kWarpsPerBlock - 1) / kWarpsPerBlock);
+  gather_kernel<QD, R><<<blocks, kWarpsPerBlock * 32, smem, P.stream>>>(
+      P.n_nodes, P.lay, P.d_adj_ptr, P.d_adj, P.d_enode, P.d_elem, ms, mad, P.d_nptr, P.d_ncol,
+      P.d_nbits, P.d_slotmap, P.d_rowptr, P.d_vals, want_K, want_R, P.d_vec, P.d_err);
+  P.launches++;
+  return cudaGetLastError();
+}
+
+template <int QD>
+cudaError_t launch_gather_q(Plan &P, bool want_K, bool want_R) {
+  const int rounds = (P.lay.s + 31) / 32;
+  switch (rounds) {
+    case 1: return launch_gather_t<QD, 1>(P, want_K, want_R);
+    case 2: return launch_gather_t<QD, 2>(P, want_K, want_R);
+    case 3: return launch_gather_t<QD, 3>(P, want_K, want_R);
+    case 4: return launch_gather_t<QD, 4>(P, want_K, want_R);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_pattern_count(Plan &P) {
+  const int cap = pattern_cap(P);
+  const size_t smem = pattern_smem(cap);
+  cudaError_t ce = cudaFuncSetAttribute(pattern_kernel<0>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (ce != cudaSuccess) return ce;
+  const unsigned blocks = unsigned((P.n_nodes + kWarpsPerBlock - 1) / kWarpsPerBlock);
+  pattern_kernel<0><<<blocks, kWarpsPerBlock * 32, smem, P.stream>>>(
+      P.n_nodes, P.lay, P.d_adj_ptr, P.d_adj, P.d_enode, P.d_elem, cap, P.d_count, P.d_ncount,
+      nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, P.d_err);
+  P.launches++;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pattern_fill(Plan &P) {
+  const int cap = pattern_cap(P);
+  const size_t smem = pattern_smem(cap);
+  cudaError_t ce = cudaFuncSetAttribute(pattern_kernel<1>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (ce != cudaSuccess) return ce;
+  const unsigned blocks = unsigned((P.n_nodes + kWarpsPerBlock - 1) / kWarpsPerBlock);
+  pattern_kernel<1><<<blocks, kWarpsPerBlock * 32, smem, P.stream>>>(
+      P.n_nodes, P.lay, P.d_adj_ptr, P.d_adj, P.d_enode, P.d_elem, cap, nullptr, nullptr,
+      P.d_rowptr, P.d_colidx, P.d_nptr, P.d_ncol, P.d_nbits, P.d_slotmap, P.d_err);
+  P.launches++;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gather(Plan &P, bool want_K, bool want_R) {
+  switch (P.qdim) {
+    case 1: return launch_gather_q<1>(P, want_K, want_R);
+    case 2: return launch_gather_q<2>(P, want_K, want_R);
+    case 3: return launch_gather_q<3>(P, want_K, want_R);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace gfgpu

@@ -1,485 +1,258 @@
-// Affine-simplex assembly kernels (sm_103a, FP64).
+// Affine-simplex element pass (sm_103a, FP64).
 //
 // GetFEM's exec loop (getfem_generic_assembly_compile_and_exec.cc:8750-8869)
 // recomputes, at every Gauss point q of every element, the geometric
 // transformation (J, B), the real base gradients grad_ref . B^T and the
-// contraction, accumulates elem += J w_q t_q and inserts elem into the sparse
-// matrix.  On an affine simplex B and J are constant, so the Gauss-point sum
-// factors through a small per-element tensor and a fixed reference tensor
-// (the idea of getfem_mat_elem.cc:433 for linear geotrans):
+// contraction, and accumulates elem += J w_q t_q.  On an affine simplex B
+// and J are constant, so the Gauss-point sum factors through a small
+// per-element tensor and a fixed reference tensor (the idea of
+// getfem_mat_elem.cc:433 for linear geotrans):
 //
-//   elem[(i,a),(j,b)] = sum_{v,w} G[i,j,v,w] T_e[a,b,v,w] + cm_e M[i,j] d_ab
-//   T_e[a,b,v,w] = |J| (c0 g_va g_wb + c1 d_ab g_v.g_w + c2 g_vb g_wa)
+//   elem[(i,a),(j,b)] = sum_{v,w} G[i,j,v,w] T[(a,v),(b,w)] + cm M[i,j] d_ab
+//   T[(a,v),(b,w)] = |J| (c0 g_va g_wb + c1 d_ab g_v.g_w + c2 g_vb g_wa)
 //
 // with g_v the real gradients of the barycentric coordinates and
 // G[i,j,v,w] = sum_q w_q c_iv(x_q) c_jw(x_q) (grad phi_i = sum_v c_iv
-// grad lambda_v), computed with the element's own quadrature rule, so the
-// result is the reference's Gauss-point sum in exact arithmetic.
+// grad lambda_v) computed with the element's own quadrature rule, so the
+// result is the reference's Gauss-point sum in exact arithmetic.  G is
+// sparse: c_iv = 0 unless vertex v carries weight in node i.
 //
-// Pass 1 (element pass): one thread per element writes T_e, cm_e, |J| and
-// the drop threshold 1e-14 max|elem| (compile_and_exec.cc:5453).
-// Pass 2 (row gather): one warp per DOF node walks the node's elements in
-// element order, expands the contributions of its rows, drops those with
-// |e| <= threshold (compile_and_exec.cc:4889) and writes the CSR row values
-// and the residual.  No atomics: every K entry is summed in element order,
-// as the reference's column merge sums it.
-// The sparsity pattern is built by the same warp-per-node walk.
-#include <cub/cub.cuh>
-
+// A block of 4 warps handles 32 elements (lane = element in every warp).
+// FP64 is the bound on this part, and an FP64 warp instruction occupies the
+// SM's FP64 pipe for many cycles whatever the number of active lanes, so
+// control flow is uniform within each warp: warp 0 computes the geometry,
+// all warps fill T (symmetric: upper triangle, in shared memory), and warp w
+// builds rows w, w+4, ... of the element matrices.  Rows of the element matrix are
+// built in registers and stored with 32-byte vector stores, so every DRAM
+// sector is written whole.  The pass also writes the element's whole
+// contribution to the assembled vector, V = K_e u_e + scale |J| M f (no
+// threshold, as the reference's vector assembly), and the drop threshold
+// 1e-14 max|elem| over all entries (compile_and_exec.cc:5453) into the
+// element scratch read by the row gather.
 #include <cmath>
-#include <cstdio>
+#include <cstring>
 
 #include "host/refelem.h"
+#include "k_common.cuh"
 #include "plan.h"
 
 namespace gfgpu {
 
 namespace {
 
-constexpr int kWarp = 32;
-constexpr int kMaxLocal = 128;  // local nodes per element held in shared memory
+constexpr int kEpWarps = 4;            // warps per block (share 32 elements)
+constexpr int kEpThreads = 32 * kEpWarps;
 
-__device__ __forceinline__ void set_err(int *err, int bit) { atomicOr(err, bit); }
-
-// --------------------------------------------------------- element pass
-
-template <int DIM, int QD>
-__global__ void __launch_bounds__(128) simplex_element_pass(
+template <int DIM, int QD, int NB, bool MASS>
+__global__ void __launch_bounds__(kEpThreads) simplex_element_pass(
     int64_t E, const double *__restrict__ pts, const int32_t *__restrict__ cv,
-    const SimplexTables *__restrict__ tab, SimplexLayout lay, gfgpu_form form,
-    SlotPtrs slots, bool psd_hint, double *__restrict__ out,
-    int *__restrict__ err) {
-  constexpr int NV = DIM + 1;
-  int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  if (e >= E) return;
-  double x[NV][DIM];
-#pragma unroll
-  for (int v = 0; v < NV; ++v) {
-    int p = __ldg(cv + e * NV + v);
-#pragma unroll
-    for (int d = 0; d < DIM; ++d) x[v][d] = __ldg(pts + int64_t(p) * DIM + d);
+    const int32_t *__restrict__ enode, const SimplexTables *__restrict__ tab, KeLayout L,
+    gfgpu_form form, SlotPtrs slots, const double *__restrict__ fsrc, double fscale,
+    const double *__restrict__ u, double *__restrict__ out, int *__restrict__ err) {
+  constexpr int NV = DIM + 1, M = QD * NV, NTP = M * (M + 1) / 2;
+  constexpr int S = NB * QD, RS = (S + 3) & ~3;
+  constexpr int NG = NV * DIM + 8;  // g, J c0, J c1, J c2, J cmass, J, flag
+  __shared__ int8_t s_nterm[NB * NB];
+  __shared__ int8_t s_vw[NB * NB * kMaxPairTerms];
+  __shared__ double s_gval[NB * NB * kMaxPairTerms];
+  __shared__ double s_mass[NB * NB];
+  __shared__ double Gs[NG][32];     // geometry of the block's 32 elements
+  __shared__ double Tp[NTP][32];    // upper triangle of T per element
+  __shared__ long long mxs[kEpWarps][32];
+  __shared__ double Us[S][32];      // u at the element's DOFs
+  for (int k = threadIdx.x; k < NB * NB; k += blockDim.x) {
+    s_nterm[k] = tab->nterm[k];
+    s_mass[k] = tab->mass[k];
   }
-  // K(d,m) = x_{m+1,d} - x_{0,d}; B = K^{-T}; g_v = B grad_ref(lambda_v)
-  double K[DIM][DIM], g[NV][DIM], det;
-#pragma unroll
-  for (int d = 0; d < DIM; ++d)
-#pragma unroll
-    for (int m = 0; m < DIM; ++m) K[d][m] = x[m + 1][d] - x[0][d];
-  if (DIM == 2) {
-    det = K[0][0] * K[1][1] - K[0][1] * K[1][0];
-    double id = 1.0 / det;
-    // B = K^{-T}: B(d,m) = inv(K)(m,d)
-    double Ki[2][2] = {{K[1][1] * id, -K[0][1] * id}, {-K[1][0] * id, K[0][0] * id}};
-#pragma unroll
-    for (int v = 1; v < NV; ++v)
-#pragma unroll
-      for (int d = 0; d < DIM; ++d) g[v][d] = Ki[v - 1][d];
-  } else {
-    double c00 = K[1][1] * K[2][2] - K[1][2] * K[2][1];
-    double c01 = K[1][2] * K[2][0] - K[1][0] * K[2][2];
-    double c02 = K[1][0] * K[2][1] - K[1][1] * K[2][0];
-    det = K[0][0] * c00 + K[0][1] * c01 + K[0][2] * c02;
-    double id = 1.0 / det;
-    // inverse(K)(m,d) = cofactor(d,m)/det
-    double Ki[3][3];
-    Ki[0][0] = c00 * id;
-    Ki[1][0] = c01 * id;
-    Ki[2][0] = c02 * id;
-    Ki[0][1] = (K[0][2] * K[2][1] - K[0][1] * K[2][2]) * id;
-    Ki[1][1] = (K[0][0] * K[2][2] - K[0][2] * K[2][0]) * id;
-    Ki[2][1] = (K[0][1] * K[2][0] - K[0][0] * K[2][1]) * id;
-    Ki[0][2] = (K[0][1] * K[1][2] - K[0][2] * K[1][1]) * id;
-    Ki[1][2] = (K[0][2] * K[1][0] - K[0][0] * K[1][2]) * id;
-    Ki[2][2] = (K[0][0] * K[1][1] - K[0][1] * K[1][0]) * id;
-#pragma unroll
-    for (int v = 1; v < NV; ++v)
-#pragma unroll
-      for (int d = 0; d < DIM; ++d) g[v][d] = Ki[v - 1][d];
+  for (int k = threadIdx.x; k < NB * NB * kMaxPairTerms; k += blockDim.x) {
+    s_vw[k] = tab->vw[k];
+    s_gval[k] = tab->gval[k];
   }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t e = blockIdx.x * int64_t(32) + lane;
+  const bool active = e < E;
+  // ---- warp 0: geometry and coefficients (lane = element)
+  if (wid == 0) {
+    double g[NV][DIM], det = 0.0;
+    double c0 = 0, c1 = 0, c2 = 0, cmass = 0;
+    if (active) {
+      double x[NV][DIM];
 #pragma unroll
-  for (int d = 0; d < DIM; ++d) {
-    double s = 0;
+      for (int v = 0; v < NV; ++v) {
+        const int p = __ldg(cv + e * NV + v);
 #pragma unroll
-    for (int v = 1; v < NV; ++v) s += g[v][d];
-    g[0][d] = -s;
-  }
-  double *o = out + e * lay.stride;
-  if (det == 0.0) {
-    set_err(err, ERR_JACOBIAN);
-    for (int k = 0; k < lay.stride; ++k) o[k] = 0.0;
-    return;
-  }
-  const double J = fabs(det);
-  // coefficients (element constants) summed over the terms of each kind
-  double c0 = 0, c1 = 0, c2 = 0, cmass = 0;
-  for (int t = 0; t < form.n_terms; ++t) {
-    const gfgpu_term &T = form.terms[t];
-    auto cval = [&](const gfgpu_coef &c) -> double {
-      if (c.kind == GFGPU_COEF_CONST) return c.value;
-      if (c.kind == GFGPU_COEF_ELEMENT) return c.value * slots.p[c.slot][e];
-      return 0.0;
-    };
-    if (T.kind == GFGPU_TERM_GRADGRAD) {
-      c0 += T.scale * cval(T.c[0]);
-      c1 += T.scale * cval(T.c[1]);
-      c2 += T.scale * cval(T.c[2]);
-    } else if (T.kind == GFGPU_TERM_MASS) {
-      cmass += T.scale * cval(T.c[0]);
-    }
-  }
-  double Tl[QD * QD * NV * NV];
+        for (int d = 0; d < DIM; ++d) x[v][d] = __ldg(pts + int64_t(p) * DIM + d);
+      }
+      // K(d,m) = x_{m+1,d} - x_{0,d}; J = |det K|; g_v = K^{-T} grad_ref(lambda_v)
+      double K[DIM][DIM];
 #pragma unroll
-  for (int a = 0; a < QD; ++a)
+      for (int d = 0; d < DIM; ++d)
 #pragma unroll
-    for (int b = 0; b < QD; ++b)
+        for (int m = 0; m < DIM; ++m) K[d][m] = x[m + 1][d] - x[0][d];
+      if (DIM == 2) {
+        det = K[0][0] * K[1][1] - K[0][1] * K[1][0];
+        const double id = 1.0 / det;
+        g[1][0] = K[1][1] * id, g[1][1] = -K[0][1] * id;
+        g[2][0] = -K[1][0] * id, g[2][1] = K[0][0] * id;
+      } else {
+        const double c00 = K[1][1] * K[2][2] - K[1][2] * K[2][1];
+        const double c01 = K[1][2] * K[2][0] - K[1][0] * K[2][2];
+        const double c02 = K[1][0] * K[2][1] - K[1][1] * K[2][0];
+        det = K[0][0] * c00 + K[0][1] * c01 + K[0][2] * c02;
+        const double id = 1.0 / det;
+        g[1][0] = c00 * id, g[2][0] = c01 * id, g[3][0] = c02 * id;
+        g[1][1] = (K[0][2] * K[2][1] - K[0][1] * K[2][2]) * id;
+        g[2][1] = (K[0][0] * K[2][2] - K[0][2] * K[2][0]) * id;
+        g[3][1] = (K[0][1] * K[2][0] - K[0][0] * K[2][1]) * id;
+        g[1][2] = (K[0][1] * K[1][2] - K[0][2] * K[1][1]) * id;
+        g[2][2] = (K[0][2] * K[1][0] - K[0][0] * K[1][2]) * id;
+        g[3][2] = (K[0][0] * K[1][1] - K[0][1] * K[1][0]) * id;
+      }
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) {
+        double s = 0;
+#pragma unroll
+        for (int v = 1; v < NV; ++v) s += g[v][d];
+        g[0][d] = -s;
+      }
+      for (int t = 0; t < form.n_terms; ++t) {
+        const gfgpu_term &T = form.terms[t];
+        auto cval = [&](const gfgpu_coef &c) -> double {
+          if (c.kind == GFGPU_COEF_CONST) return c.value;
+          if (c.kind == GFGPU_COEF_ELEMENT) return c.value * slots.p[c.slot][e];
+          return 0.0;
+        };
+        if (T.kind == GFGPU_TERM_GRADGRAD) {
+          c0 += T.scale * cval(T.c[0]);
+          c1 += T.scale * cval(T.c[1]);
+          c2 += T.scale * cval(T.c[2]);
+        } else if (T.kind == GFGPU_TERM_MASS) {
+          cmass += T.scale * cval(T.c[0]);
+        }
+      }
+    } else {
 #pragma unroll
       for (int v = 0; v < NV; ++v)
 #pragma unroll
-        for (int w = 0; w < NV; ++w) {
-          double s = 0;
-          if (a == b) {
-            double gg = 0;
+        for (int d = 0; d < DIM; ++d) g[v][d] = 0.0;
+    }
+    const bool bad = active && det == 0.0;
+    if (bad) set_err(err, ERR_JACOBIAN);
+    const double J = bad ? 0.0 : fabs(det);
 #pragma unroll
-            for (int k = 0; k < DIM; ++k) gg += g[v][k] * g[w][k];
-            s = c1 * gg;
-          }
-          if (QD > 1) s += c0 * g[v][a] * g[w][b] + c2 * g[v][b] * g[w][a];
-          double val = J * s;
-          Tl[((a * QD + b) * NV + v) * NV + w] = val;
-          o[((a * QD + b) * NV + v) * NV + w] = val;
+    for (int v = 0; v < NV; ++v)
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) Gs[v * DIM + d][lane] = bad ? 0.0 : g[v][d];
+    Gs[NV * DIM + 0][lane] = J * c0;
+    Gs[NV * DIM + 1][lane] = J * c1;
+    Gs[NV * DIM + 2][lane] = J * c2;
+    Gs[NV * DIM + 3][lane] = J * cmass;
+    Gs[NV * DIM + 4][lane] = J;
+  }
+  __syncthreads();
+  // ---- all warps: T[(a,v),(b,w)] = J (c0 g_va g_wb + c1 d_ab g_v.g_w + c2 g_vb g_wa)
+  {
+    const double Jc0 = Gs[NV * DIM + 0][lane], Jc1 = Gs[NV * DIM + 1][lane];
+    const double Jc2 = Gs[NV * DIM + 2][lane];
+    int k = 0;
+#pragma unroll
+    for (int p = 0; p < M; ++p)
+#pragma unroll
+      for (int q = p; q < M; ++q, ++k) {
+        if (k % kEpWarps != wid) continue;  // warp-uniform
+        const int a = p / NV, v = p % NV, b = q / NV, w = q % NV;
+        double val = 0.0;
+        if (a == b) {
+          double gg = 0;
+#pragma unroll
+          for (int d = 0; d < DIM; ++d) gg += Gs[v * DIM + d][lane] * Gs[w * DIM + d][lane];
+          val = Jc1 * gg;
         }
-  const double cm = J * cmass;
-  o[lay.off_cm] = cm;
-  o[lay.off_jw] = J;
-  // threshold: max |elem|.  For a positive semi-definite element matrix the
-  // largest entry is on the diagonal (|e_ij| <= sqrt(e_ii e_jj)).
-  bool psd = psd_hint && cmass >= 0;
-  if (QD > 1) psd = psd && (c1 + c2 >= 0) && (c1 - c2 >= 0) && (c1 + c2 + DIM * c0 >= 0);
-  else psd = psd && c1 >= 0;
-  const int nb = tab->nb;
-  double mx = 0;
-  for (int i = 0; i < nb; ++i) {
-    int jlo = psd ? i : 0, jhi = psd ? i + 1 : nb;
-    for (int j = jlo; j < jhi; ++j) {
-      int pij = i * nb + j;
-      int nt = tab->nterm[pij];
+        if (QD > 1)
+          val += Jc0 * Gs[v * DIM + a][lane] * Gs[w * DIM + b][lane] +
+                 Jc2 * Gs[v * DIM + b][lane] * Gs[w * DIM + a][lane];
+        Tp[k][lane] = val;
+      }
+  }
+  __syncthreads();
+  // ---- warp w: rows r = w, w + 4, ... of every element of the block.
+  // Row (i,a) is built in registers, multiplied into R_e = K_e u_e + V (no
+  // threshold, as the reference's vector assembly) and written with 32-byte
+  // stores that fill whole sectors.
+  for (int j = wid; j < NB; j += kEpWarps) {
+    const int nd = active ? __ldg(enode + e * NB + j) : 0;
 #pragma unroll
-      for (int a = 0; a < QD; ++a)
+    for (int b = 0; b < QD; ++b)
+      Us[j * QD + b][lane] = (active && u) ? __ldg(u + int64_t(nd) * QD + b) : 0.0;
+  }
+  __syncthreads();
+  const double cm = Gs[NV * DIM + 3][lane], jf = Gs[NV * DIM + 4][lane] * fscale;
+  double *o = out + e * L.stride;
+  long long mx = 0;
+  for (int r = wid; r < S; r += kEpWarps) {
+    const int i = r / QD, a = r % QD;
+    double row[RS];
+#pragma unroll
+    for (int j = 0; j < NB; ++j) {
+      const int pij = i * NB + j;
+      const int nt = s_nterm[pij];
+      const double mij = MASS ? cm * s_mass[pij] : 0.0;
+#pragma unroll
+      for (int b = 0; b < QD; ++b) row[j * QD + b] = (MASS && a == b) ? mij : 0.0;
+      for (int t = 0; t < nt; ++t) {
+        const int vw = s_vw[pij * kMaxPairTerms + t];
+        const int v = vw / NV, w = vw % NV;
+        const double gv = s_gval[pij * kMaxPairTerms + t];
 #pragma unroll
         for (int b = 0; b < QD; ++b) {
-          if (psd && a != b) continue;
-          double s = 0;
-          for (int t = 0; t < nt; ++t) {
-            int vw = tab->vw[pij * kMaxPairTerms + t];
-            s += tab->gval[pij * kMaxPairTerms + t] * Tl[(a * QD + b) * NV * NV + vw];
+          int p = a * NV + v, q = b * NV + w;
+          if (p > q) {
+            const int tmp = p;
+            p = q;
+            q = tmp;
           }
-          if (a == b) s += cm * tab->mass[pij];
-          mx = fmax(mx, fabs(s));
-        }
-    }
-  }
-  if (!isfinite(mx)) set_err(err, ERR_NAN);
-  o[lay.off_thr] = mx * 1e-14;
-}
-
-// Contribution of element e's local entry ((li,a),(lj,b)).
-struct SimplexSource {
-  const double *elem;
-  const SimplexTables *tab;
-  SimplexLayout lay;
-  int qd, nv, nb;
-  __device__ __forceinline__ double thr(int e) const { return elem[int64_t(e) * lay.stride + lay.off_thr]; }
-  __device__ __forceinline__ double value(int e, int li, int lj, int a, int b) const {
-    const double *T = elem + int64_t(e) * lay.stride;
-    const int pij = li * nb + lj;
-    const int nt = tab->nterm[pij];
-    const double *Tab = T + (a * qd + b) * nv * nv;
-    double c = 0;
-    for (int t = 0; t < nt; ++t)
-      c += tab->gval[pij * kMaxPairTerms + t] * Tab[tab->vw[pij * kMaxPairTerms + t]];
-    if (a == b) c += T[lay.off_cm] * tab->mass[pij];
-    return c;
-  }
-  __device__ __forceinline__ double jw(int e) const { return elem[int64_t(e) * lay.stride + lay.off_jw]; }
-  __device__ __forceinline__ double mass(int li, int lj) const { return tab->mass[li * nb + lj]; }
-};
-
-// ------------------------------------------------------ warp utilities
-
-// Bitonic sort of n (power of two) ints in shared memory by one warp.
-__device__ void warp_sort(int *a, int n) {
-  const int lane = threadIdx.x & 31;
-  for (int k = 2; k <= n; k <<= 1) {
-    for (int j = k >> 1; j > 0; j >>= 1) {
-      for (int i = lane; i < n; i += kWarp) {
-        int ixj = i ^ j;
-        if (ixj > i) {
-          int x = a[i], y = a[ixj];
-          bool up = (i & k) == 0;
-          if ((x > y) == up) a[i] = y, a[ixj] = x;
-        }
-      }
-      __syncwarp();
-    }
-  }
-}
-
-// In-place unique of a sorted array; returns the new length.
-__device__ int warp_unique(int *a, int n) {
-  const int lane = threadIdx.x & 31;
-  int out = 0;
-  for (int base = 0; base < n; base += kWarp) {
-    int i = base + lane;
-    int x = i < n ? a[i] : 0;
-    bool first = i < n && (i == 0 || a[i - 1] != x);
-    unsigned m = __ballot_sync(0xffffffffu, first);
-    __syncwarp();
-    if (first) a[out + __popc(m & ((1u << lane) - 1))] = x;
-    out += __popc(m);
-    __syncwarp();
-  }
-  return out;
-}
-
-__device__ __forceinline__ int bsearch_slot(const int *s, int n, int key) {
-  int lo = 0, hi = n;
-  while (lo < hi) {
-    int mid = (lo + hi) >> 1;
-    if (s[mid] < key) lo = mid + 1;
-    else hi = mid;
-  }
-  return (lo < n && s[lo] == key) ? lo : -1;
-}
-
-// --------------------------------------------------------- pattern build
-
-// Per warp: candidate list (max_cand ints, rounded to a power of two) and a
-// keep mask per candidate slot, then counts (MODE 0) or column indices
-// (MODE 1).
-template <class Src, int MODE>
-__global__ void __launch_bounds__(128) pattern_kernel(
-    int64_t n_nodes, int qd, int nb, const int32_t *__restrict__ adj_ptr,
-    const int32_t *__restrict__ adj, const int32_t *__restrict__ enode, Src src, int cap,
-    int64_t *__restrict__ rowcount, int32_t *__restrict__ ncount,
-    const int64_t *__restrict__ rowptr, int32_t *__restrict__ colidx,
-    const int64_t *__restrict__ nptr, int32_t *__restrict__ ncol, int *__restrict__ err) {
-  extern __shared__ int smem[];
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  int *cand = smem + wib * (2 * cap + kMaxLocal);
-  unsigned *bits = reinterpret_cast<unsigned *>(cand + cap);
-  int *ljs = reinterpret_cast<int *>(bits + cap);
-  int64_t node = blockIdx.x * int64_t(blockDim.x >> 5) + wib;
-  if (node >= n_nodes) return;
-  const int a0 = adj_ptr[node], a1 = adj_ptr[node + 1];
-  int n = 0;
-  for (int k = a0; k < a1; ++k) {
-    int el = adj[k] / nb;
-    if (n + nb > cap) {
-      if (lane == 0) set_err(err, ERR_CAPACITY);
-      return;
-    }
-    for (int j = lane; j < nb; j += kWarp) cand[n + j] = enode[int64_t(el) * nb + j];
-    n += nb;
-  }
-  int np = 1;
-  while (np < n) np <<= 1;
-  for (int j = n + lane; j < np; j += kWarp) cand[j] = 0x7fffffff;
-  __syncwarp();
-  warp_sort(cand, np);
-  int ns = warp_unique(cand, n);
-  for (int j = lane; j < ns; j += kWarp) bits[j] = 0u;
-  __syncwarp();
-  const int qq = qd * qd;
-  for (int k = a0; k < a1; ++k) {
-    const int el = adj[k] / nb, li = adj[k] % nb;
-    const double thr = src.thr(el);
-    for (int j = lane; j < nb; j += kWarp) ljs[j] = bsearch_slot(cand, ns, enode[int64_t(el) * nb + j]);
-    __syncwarp();
-    for (int c = lane; c < nb * qq; c += kWarp) {
-      int lj = c / qq, ab = c % qq;
-      double v = src.value(el, li, lj, ab / qd, ab % qd);
-      if (fabs(v) > thr) atomicOr(&bits[ljs[lj]], 1u << ab);
-    }
-    __syncwarp();
-  }
-  if (MODE == 0) {
-    for (int a = 0; a < qd; ++a) {
-      unsigned am = ((1u << qd) - 1u) << (a * qd);
-      int cnt = 0;
-      for (int j = lane; j < ns; j += kWarp) cnt += __popc(bits[j] & am);
-      for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-      if (lane == 0) rowcount[node * qd + a] = cnt;
-    }
-    int kept = 0;
-    for (int j = lane; j < ns; j += kWarp) kept += bits[j] != 0u;
-    for (int o = 16; o > 0; o >>= 1) kept += __shfl_xor_sync(0xffffffffu, kept, o);
-    if (lane == 0) ncount[node] = kept;
-  } else {
-    for (int a = 0; a < qd; ++a) {
-      unsigned am = ((1u << qd) - 1u) << (a * qd);
-      int64_t base = rowptr[node * qd + a];
-      const int64_t rowend = rowptr[node * qd + a + 1];
-      for (int j0 = 0; j0 < ns; j0 += kWarp) {
-        int j = j0 + lane;
-        unsigned m = j < ns ? (bits[j] & am) : 0u;
-        int c = __popc(m);
-        int incl = c;
-        for (int o = 1; o < 32; o <<= 1) {
-          int y = __shfl_up_sync(0xffffffffu, incl, o);
-          if (lane >= o) incl += y;
-        }
-        int total = __shfl_sync(0xffffffffu, incl, 31);
-        int pos = incl - c;
-        if (j < ns)
-          for (int b = 0; b < qd; ++b)
-            if (m & (1u << (a * qd + b))) {
-              // the count pass sized the row; never write past it
-              if (base + pos < rowend) colidx[base + pos] = cand[j] * qd + b;
-              else set_err(err, ERR_CAPACITY);
-              ++pos;
-            }
-        base += total;
-      }
-    }
-    int64_t nb0 = nptr[node];
-    const int64_t nend = nptr[node + 1];
-    for (int j0 = 0; j0 < ns; j0 += kWarp) {
-      int j = j0 + lane;
-      bool keep = j < ns && bits[j] != 0u;
-      unsigned m = __ballot_sync(0xffffffffu, keep);
-      int64_t at = nb0 + __popc(m & ((1u << lane) - 1u));
-      if (keep) {
-        if (at < nend) ncol[at] = cand[j];
-        else set_err(err, ERR_CAPACITY);
-      }
-      nb0 += __popc(m);
-    }
-  }
-}
-
-// ------------------------------------------------------------ row gather
-
-template <class Src>
-__global__ void __launch_bounds__(128) gather_kernel(
-    int64_t n_nodes, int qd, int nb, const int32_t *__restrict__ adj_ptr,
-    const int32_t *__restrict__ adj, const int32_t *__restrict__ enode, Src src, int ms,
-    const int64_t *__restrict__ nptr, const int32_t *__restrict__ ncol,
-    const int64_t *__restrict__ rowptr, const int32_t *__restrict__ colidx,
-    double *__restrict__ vals, bool want_K, bool want_R, const double *__restrict__ u,
-    const double *__restrict__ fsrc, double fscale, double *__restrict__ vec,
-    int *__restrict__ err) {
-  extern __shared__ double dsm[];
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const int qq = qd * qd;
-  // per warp: acc[ms*qq] doubles, then pos[ms*qq] ints, slots[ms] ints, ljs[nb]
-  const size_t per_warp = size_t(ms) * qq * 8 + size_t(ms) * qq * 4 + size_t(ms) * 4 + 4 * kMaxLocal;
-  char *base = reinterpret_cast<char *>(dsm) + wib * ((per_warp + 15) / 16 * 16);
-  double *acc = reinterpret_cast<double *>(base);
-  int *pos = reinterpret_cast<int *>(acc + size_t(ms) * qq);
-  int *slots = pos + size_t(ms) * qq;
-  int *ljs = slots + ms;
-  int64_t node = blockIdx.x * int64_t(blockDim.x >> 5) + wib;
-  if (node >= n_nodes) return;
-  const int64_t s0 = nptr[node];
-  const int ns = int(nptr[node + 1] - s0);
-  if (ns > ms) {
-    if (lane == 0) set_err(err, ERR_CAPACITY);
-    return;
-  }
-  if (want_K) {
-    for (int j = lane; j < ns; j += kWarp) slots[j] = ncol[s0 + j];
-    for (int j = lane; j < ns * qq; j += kWarp) pos[j] = -1, acc[j] = 0.0;
-    __syncwarp();
-    for (int a = 0; a < qd; ++a) {
-      const int64_t r0 = rowptr[node * qd + a], r1 = rowptr[node * qd + a + 1];
-      for (int64_t p = r0 + lane; p < r1; p += kWarp) {
-        int col = colidx[p];
-        int s = bsearch_slot(slots, ns, col / qd);
-        if (s >= 0) pos[(s * qd + a) * qd + col % qd] = int(p - r0);
-      }
-    }
-    __syncwarp();
-  }
-  double racc[3] = {0.0, 0.0, 0.0};
-  const int a0 = adj_ptr[node], a1 = adj_ptr[node + 1];
-  for (int k = a0; k < a1; ++k) {
-    const int el = adj[k] / nb, li = adj[k] % nb;
-    const int32_t *en = enode + int64_t(el) * nb;
-    if (want_K) {
-      for (int j = lane; j < nb; j += kWarp) ljs[j] = bsearch_slot(slots, ns, en[j]);
-      __syncwarp();
-    }
-    const double thr = src.thr(el);
-    for (int c = lane; c < nb * qq; c += kWarp) {
-      const int lj = c / qq, ab = c % qq, a = ab / qd, b = ab % qd;
-      const double v = src.value(el, li, lj, a, b);
-      if (want_R) {
-        double uv = u[int64_t(en[lj]) * qd + b];
-        if (a == 0) racc[0] += v * uv;
-        else if (a == 1) racc[1] += v * uv;
-        else racc[2] += v * uv;
-      }
-      if (want_K && fabs(v) > thr) {
-        int s = ljs[lj];
-        if (s >= 0) {
-          int q = (s * qd + a) * qd + b;
-          if (pos[q] >= 0) acc[q] += v;
+          row[j * QD + b] += gv * Tp[p * M - (p * (p - 1)) / 2 + (q - p)][lane];
         }
       }
     }
-    if (want_R && fsrc) {
-      const double jw = src.jw(el) * fscale;
-      for (int c = lane; c < nb * qd; c += kWarp) {
-        const int lj = c / qd, a = c % qd;
-        double v = jw * src.mass(li, lj) * fsrc[int64_t(en[lj]) * qd + a];
-        if (a == 0) racc[0] += v;
-        else if (a == 1) racc[1] += v;
-        else racc[2] += v;
+#pragma unroll
+    for (int c = S; c < RS; ++c) row[c] = 0.0;
+    // load term: scale |J| sum_j M[i,j] f[(j,a)]
+    double rv = 0.0;
+    if (fsrc && active) {
+      double s = 0.0;
+#pragma unroll
+      for (int j = 0; j < NB; ++j) {
+        const int nd = __ldg(enode + e * NB + j);
+        s += s_mass[i * NB + j] * __ldg(fsrc + int64_t(nd) * QD + a);
       }
+      rv = jf * s;
     }
-    if (want_K) __syncwarp();
-  }
-  if (want_K) {
-    __syncwarp();
-    for (int a = 0; a < qd; ++a) {
-      const int64_t r0 = rowptr[node * qd + a];
-      for (int j = lane; j < ns * qd; j += kWarp) {
-        int s = j / qd, b = j % qd;
-        int q = (s * qd + a) * qd + b;
-        int p = pos[q];
-        if (p >= 0) vals[r0 + p] = acc[q];
-      }
+#pragma unroll
+    for (int c = 0; c < S; ++c) {
+      rv += row[c] * Us[c][lane];
+      const long long bitsv = __double_as_longlong(row[c]) & 0x7fffffffffffffffLL;
+      mx = bitsv > mx ? bitsv : mx;
     }
-  }
-  if (want_R) {
-    for (int a = 0; a < qd; ++a) {
-      double r = racc[a];
-      for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
-      if (lane == 0) {
-        if (!isfinite(r)) set_err(err, ERR_NAN);
-        vec[node * qd + a] = r;
-      }
+    if (active) {
+      double4 *dst = reinterpret_cast<double4 *>(o + r * RS);
+#pragma unroll
+      for (int c = 0; c < RS; c += 4) dst[c / 4] = make_double4(row[c], row[c + 1], row[c + 2], row[c + 3]);
+      o[L.off_vec + r] = rv;
     }
   }
-}
-
-SimplexSource make_simplex_source(Plan &P) {
-  SimplexSource s;
-  s.elem = P.d_elem;
-  s.tab = P.d_stab;
-  s.lay = P.lay;
-  s.qd = P.qdim;
-  s.nv = P.dim + 1;
-  s.nb = P.nb;
-  return s;
-}
-
-constexpr int kWarpsPerBlock = 4;
-
-size_t pattern_smem(int cap) { return size_t(kWarpsPerBlock) * (2 * cap + kMaxLocal) * sizeof(int); }
-size_t gather_smem(int ms, int qd) {
-  size_t per = size_t(ms) * qd * qd * 12 + size_t(ms) * 4 + 4 * kMaxLocal;
-  return size_t(kWarpsPerBlock) * ((per + 15) / 16 * 16);
+  mxs[wid][lane] = mx;
+  __syncthreads();
+  if (wid == 0 && active) {
+    long long m = mxs[0][lane];
+#pragma unroll
+    for (int k = 1; k < kEpWarps; ++k) m = mxs[k][lane] > m ? mxs[k][lane] : m;
+    const double mxd = __longlong_as_double(m);
+    if (!isfinite(mxd)) set_err(err, ERR_NAN);
+    o[L.off_thr] = mxd * 1e-14;
+#pragma unroll
+    for (int c = S; c < RS; ++c) o[L.off_vec + c] = 0.0;
+  }
 }
 
 }  // namespace
@@ -487,7 +260,7 @@ size_t gather_smem(int ms, int qd) {
 // ---------------------------------------------------------------- host
 
 // Sparse barycentric reference tensor of FEM_PK(dim, degree) for the plan's
-// quadrature rule, and the reference mass matrix.
+// quadrature rule, the reference mass matrix, and the element scratch layout.
 int build_simplex_tables(Plan &P, std::string &errmsg) {
   const int dim = P.dim, K = P.degree;
   RefElement fe(dim, SIMPLEX, K);
@@ -523,16 +296,16 @@ int build_simplex_tables(Plan &P, std::string &errmsg) {
     for (int d = 0; d < dim; ++d) w[i * nv + d + 1] = fe.lattice[i * dim + d], s += fe.lattice[i * dim + d];
     w[i * nv] = K - s;
   }
+  std::vector<double> val(nb), grad(size_t(nb) * dim);
   for (int qq = 0; qq < q.nq; ++qq) {
     double lam[4];
     lam[0] = 1.0;
     for (int d = 0; d < dim; ++d) lam[d + 1] = q.pts[qq * dim + d], lam[0] -= lam[d + 1];
+    fe.eval(&q.pts[qq * dim], val.data(), grad.data());
     for (int i = 0; i < nb; ++i) {
       double f[4], df[4];
       for (int v = 0; v < nv; ++v) factor(w[i * nv + v], lam[v], f[v], df[v]);
-      double val = 1.0;
-      for (int v = 0; v < nv; ++v) val *= f[v];
-      phi[qq * nb + i] = val;
+      phi[qq * nb + i] = val[i];  // the reference's tabulated base values
       for (int v = 0; v < nv; ++v) {
         double c = df[v];
         for (int u = 0; u < nv; ++u)
@@ -566,91 +339,58 @@ int build_simplex_tables(Plan &P, std::string &errmsg) {
       t.mass[pij] = m;
     }
   P.nq = q.nq;
-  const int qd = P.qdim;
-  P.lay.nT = qd * qd * nv * nv;
-  P.lay.off_cm = P.lay.nT;
-  P.lay.off_jw = P.lay.nT + 1;
-  P.lay.off_thr = P.lay.nT + 2;
-  P.lay.stride = P.lay.nT + 3;
+  const int qd = P.qdim, s = nb * qd;
+  P.lay.nb = nb;
+  P.lay.qd = qd;
+  P.lay.s = s;
+  // rows padded to a multiple of 4 doubles: 32-byte aligned rows and blocks
+  P.lay.rowstride = (s + 3) & ~3;
+  P.lay.off_vec = s * P.lay.rowstride;
+  P.lay.off_thr = P.lay.off_vec + P.lay.rowstride;
+  P.lay.stride = P.lay.off_thr + 4;
+  P.lay.linear = true;
   return GFGPU_OK;
 }
 
-SlotPtrs slot_ptrs(const Plan &P) {
+cudaError_t launch_simplex_element_pass(Plan &P, bool with_u) {
+  if (P.n_elements == 0) return cudaSuccess;
+  const int threads = kEpThreads;
+  const unsigned blocks = unsigned((P.n_elements + 31) / 32);  // 32 elements per block
   SlotPtrs sp;
   for (int i = 0; i < GFGPU_MAX_SLOTS; ++i) sp.p[i] = P.slot_ptr[i];
-  return sp;
-}
-
-cudaError_t launch_simplex_element_pass(Plan &P) {
-  const int threads = 128;
-  const unsigned blocks = unsigned((P.n_elements + threads - 1) / threads);
-  if (P.n_elements == 0) return cudaSuccess;
-  SlotPtrs sp = slot_ptrs(P);
-#define GFGPU_EP(D, Q)                                                                 \
-  simplex_element_pass<D, Q><<<blocks, threads, 0, P.stream>>>(                        \
-      P.n_elements, P.d_points, P.d_cv, P.d_stab, P.lay, P.form, sp, P.psd, P.d_elem, P.d_err)
-  if (P.dim == 2 && P.qdim == 1) GFGPU_EP(2, 1);
-  else if (P.dim == 2 && P.qdim == 2) GFGPU_EP(2, 2);
-  else if (P.dim == 3 && P.qdim == 1) GFGPU_EP(3, 1);
-  else if (P.dim == 3 && P.qdim == 3) GFGPU_EP(3, 3);
-  else return cudaErrorInvalidValue;
-#undef GFGPU_EP
-  P.launches++;
-  return cudaGetLastError();
-}
-
-cudaError_t launch_pattern_count(Plan &P) {
-  const int cap = P.max_cand < 32 ? 32 : P.max_cand;
-  int np = 1;
-  while (np < cap) np <<= 1;
-  size_t smem = pattern_smem(np);
-  cudaError_t ce = cudaFuncSetAttribute(pattern_kernel<SimplexSource, 0>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-  if (ce != cudaSuccess) return ce;
-  const unsigned blocks = unsigned((P.n_nodes + kWarpsPerBlock - 1) / kWarpsPerBlock);
-  pattern_kernel<SimplexSource, 0><<<blocks, kWarpsPerBlock * 32, smem, P.stream>>>(
-      P.n_nodes, P.qdim, P.nb, P.d_adj_ptr, P.d_adj, P.d_enode, make_simplex_source(P), np,
-      P.d_count, P.d_ncount, nullptr, nullptr, nullptr, nullptr, P.d_err);
-  P.launches++;
-  return cudaGetLastError();
-}
-
-cudaError_t launch_pattern_fill(Plan &P) {
-  const int cap = P.max_cand < 32 ? 32 : P.max_cand;
-  int np = 1;
-  while (np < cap) np <<= 1;
-  size_t smem = pattern_smem(np);
-  cudaError_t ce = cudaFuncSetAttribute(pattern_kernel<SimplexSource, 1>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-  if (ce != cudaSuccess) return ce;
-  const unsigned blocks = unsigned((P.n_nodes + kWarpsPerBlock - 1) / kWarpsPerBlock);
-  pattern_kernel<SimplexSource, 1><<<blocks, kWarpsPerBlock * 32, smem, P.stream>>>(
-      P.n_nodes, P.qdim, P.nb, P.d_adj_ptr, P.d_adj, P.d_enode, make_simplex_source(P), np,
-      nullptr, nullptr, P.d_rowptr, P.d_colidx, P.d_nptr, P.d_ncol, P.d_err);
-  P.launches++;
-  return cudaGetLastError();
-}
-
-cudaError_t launch_gather(Plan &P, bool want_K, bool want_R) {
-  const int ms = P.max_slots < 1 ? 1 : P.max_slots;
-  size_t smem = gather_smem(ms, P.qdim);
-  cudaError_t ce = cudaFuncSetAttribute(gather_kernel<SimplexSource>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-  if (ce != cudaSuccess) return ce;
   const double *fsrc = nullptr;
   double fscale = 0.0;
+  bool mass = false;
   for (int t = 0; t < P.form.n_terms; ++t) {
     const gfgpu_term &T = P.form.terms[t];
     if (T.kind == GFGPU_TERM_SOURCE) {
       fsrc = P.slot_ptr[T.field_slot];
       fscale = T.scale * (T.c[0].kind == GFGPU_COEF_CONST ? T.c[0].value : 1.0);
     }
+    if (T.kind == GFGPU_TERM_MASS) mass = true;
   }
-  const unsigned blocks = unsigned((P.n_nodes + kWarpsPerBlock - 1) / kWarpsPerBlock);
-  gather_kernel<SimplexSource><<<blocks, kWarpsPerBlock * 32, smem, P.stream>>>(
-      P.n_nodes, P.qdim, P.nb, P.d_adj_ptr, P.d_adj, P.d_enode, make_simplex_source(P), ms,
-      P.d_nptr, P.d_ncol, P.d_rowptr, P.d_colidx, P.d_vals, want_K, want_R,
-      P.slot_ptr[GFGPU_SLOT_U], fsrc, fscale, P.d_vec, P.d_err);
+#define GFGPU_EP(D, Q, N)                                                                      \
+  do {                                                                                         \
+    if (mass)                                                                                  \
+      simplex_element_pass<D, Q, N, true><<<blocks, threads, 0, P.stream>>>(                   \
+          P.n_elements, P.d_points, P.d_cv, P.d_enode, P.d_stab, P.lay, P.form, sp, fsrc,      \
+          fscale, with_u ? P.slot_ptr[GFGPU_SLOT_U] : nullptr, P.d_elem, P.d_err);             \
+    else                                                                                       \
+    simplex_element_pass<D, Q, N, false><<<blocks, threads, 0, P.stream>>>(                    \
+        P.n_elements, P.d_points, P.d_cv, P.d_enode, P.d_stab, P.lay, P.form, sp, fsrc, fscale, \
+        with_u ? P.slot_ptr[GFGPU_SLOT_U] : nullptr, P.d_elem, P.d_err);                     \
+  } while (0)
+  const int d = P.dim, k = P.degree, q = P.qdim;
+  if (d == 2 && k == 1 && q == 1) GFGPU_EP(2, 1, 3);
+  else if (d == 2 && k == 2 && q == 1) GFGPU_EP(2, 1, 6);
+  else if (d == 2 && k == 1 && q == 2) GFGPU_EP(2, 2, 3);
+  else if (d == 2 && k == 2 && q == 2) GFGPU_EP(2, 2, 6);
+  else if (d == 3 && k == 1 && q == 1) GFGPU_EP(3, 1, 4);
+  else if (d == 3 && k == 2 && q == 1) GFGPU_EP(3, 1, 10);
+  else if (d == 3 && k == 1 && q == 3) GFGPU_EP(3, 3, 4);
+  else if (d == 3 && k == 2 && q == 3) GFGPU_EP(3, 3, 10);
+  else return cudaErrorInvalidValue;
+#undef GFGPU_EP
   P.launches++;
   return cudaGetLastError();
 }

@@ -35,13 +35,18 @@ struct SimplexTables {
   double mass[kMaxNb * kMaxNb];  // reference mass matrix sum_q w_q phi_i phi_j
 };
 
-// Per-element layout of the simplex element pass output (doubles):
-//   T[qd*qd*nv*nv]  (a, b, v, w)   |J| (c0 g_va g_wb + c1 d_ab g_v.g_w + c2 g_vb g_wa)
-//   cm              |J| * mass coefficient
-//   jw              |J|
-//   thr             1e-14 * max |elem|
-struct SimplexLayout {
-  int nT, off_cm, off_jw, off_thr, stride;
+// Per-element scratch written by every element kernel and read by the
+// pattern build and the row gather (doubles):
+//   K_e   s x s, row (li,a) = li*qd + a at offset row*rowstride (rowstride even)
+//   V_e   s entries at off_vec: the element's contribution to the assembled
+//         vector (K_e u_e + load for linear forms, the element residual of a
+//         nonlinear form)
+//   thr   1e-14 max|K_e| at off_thr
+// stride is even, so every element block and every row is 16-byte aligned.
+struct KeLayout {
+  int nb = 0, qd = 0, s = 0;
+  int rowstride = 0, off_vec = 0, off_thr = 0, stride = 0;
+  bool linear = true;  // R = K_full u + sum V_e (else R = sum V_e)
 };
 
 struct SlotPtrs {
@@ -80,7 +85,7 @@ struct Plan {
   // tables
   SimplexTables stab{};
   SimplexTables *d_stab = nullptr;
-  SimplexLayout lay{};
+  KeLayout lay{};
 
   // element pass scratch
   double *d_elem = nullptr;     // E x lay.stride
@@ -91,6 +96,8 @@ struct Plan {
   int64_t nnz = -1;
   int64_t *d_nptr = nullptr;    // node-level pattern: n_nodes + 1
   int32_t *d_ncol = nullptr;
+  uint16_t *d_nbits = nullptr;  // keep bits (a*qd+b) of each node-level slot
+  int16_t *d_slotmap = nullptr; // per adjacency entry and local node: slot or -1
   int32_t max_slots = 0;
   double *d_vec = nullptr;      // n_dof
   double *d_pot = nullptr;      // 1
@@ -105,11 +112,10 @@ struct Plan {
 };
 
 // kernels (k_simplex.cu)
-cudaError_t launch_simplex_element_pass(Plan &P);
+cudaError_t launch_simplex_element_pass(Plan &P, bool with_u);
 cudaError_t launch_pattern_count(Plan &P);
 cudaError_t launch_pattern_fill(Plan &P);
 cudaError_t launch_gather(Plan &P, bool want_K, bool want_R);
-cudaError_t launch_potential(Plan &P);
 int build_simplex_tables(Plan &P, std::string &err);
 
 }  // namespace gfgpu
