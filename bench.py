@@ -280,24 +280,32 @@ def main():
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     ab = algorithmic_bytes(mesh, mf, nnz)
-    gather_bytes = ab["K"] + ab["R"] + ab["u"] + ab["f"] + ab["dofmap"]
     step_bytes = sum(ab.values())
-    gather_gbs = gather_bytes / (kt[1] * 1e-3) / 1e9
+    # the dominant kernel of the step and its achieved rate on the step's
+    # algorithmic bytes (pattern cached: K values and R written, inputs read)
+    names = ["element_pass", "row_gather"]
+    dom = int(np.argmax(kt))
+    dom_gbs = step_bytes / (kt[dom] * 1e-3) / 1e9
     fp64_peak = C.c_double()
     L.check(lib.gfgpu_fp64_peak(0, C.byref(fp64_peak)))
-    # FP64 flops executed by the gather: 2 per reference-tensor term per
-    # element entry, 2 for the residual product, 2 for the load term
+    # FP64 flops the element pass executes per element (from its loop
+    # structure): element-matrix rows (2 per reference-tensor term per
+    # component pair), R_e = K_e u_e, the load term, T and the geometry
     from getfem_gb300.tables import simplex_term_count
-    nterm_sum, nb = simplex_term_count(3, 2, "IM_TETRAHEDRON(5)")
-    qd = 3
-    gflop = E * (2.0 * nterm_sum * qd * qd + 2.0 * nb * nb * qd + 2.0 * nb * nb * qd * qd
-                 + 3.0 * nb * nb * qd) / 1e9
+    nterm_sum, nb = simplex_term_count(3, 2)
+    qd, M = 3, 3 * 4
+    s_ = nb * qd
+    ep_flops = (2.0 * nterm_sum * qd * qd + 2.0 * s_ * s_ + 2.0 * s_ * nb
+                + 6.0 * M * (M + 1) / 2 + 150.0)
+    ep_tflops = E * ep_flops / (kt[0] * 1e-3) / 1e12
+    # DRAM bytes per launch of the dominant kernel: from one ncu capture of
+    # the same kernel on the 20^3 x 6 mesh, scaled by the element count
     traffic = None
-    prof = os.path.join(ROOT, "profiles", "gather_p2tet_traffic.json")
+    prof = os.path.join(ROOT, "profiles", "dram_bytes_per_element.json")
     if os.path.exists(prof):
         try:
-            traffic = _json.load(open(prof)).get("bytes_per_element") * E
-        except (ValueError, TypeError):
+            traffic = float(_json.load(open(prof))[names[dom]]) * E
+        except (ValueError, TypeError, KeyError):
             traffic = None
     cpu = None
     if not args.no_cpu:
@@ -318,13 +326,13 @@ def main():
                    "l2": "inputs larger than L2 (K values, scratch and DOF data >> 129 MB)",
                    "dofs_per_s": value * mf.nb_dof() / E},
         "kernels_ms": {"element_pass": float(kt[0]), "row_gather": float(kt[1])},
-        "roofline": {"bound": "hbm", "kernel": "row_gather", "achieved": gather_gbs,
-                     "peak": hbm_peak, "unit": "GB/s", "frac": gather_gbs / hbm_peak,
-                     "traffic": traffic, "algorithmic_bytes": gather_bytes,
+        "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": dom_gbs,
+                     "peak": hbm_peak, "unit": "GB/s", "frac": dom_gbs / hbm_peak,
+                     "traffic": traffic, "algorithmic_bytes": step_bytes,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
-        "fp64": {"achieved_tflops": gflop / (kt[1] * 1e-3) / 1e3,
-                 "peak_tflops": fp64_peak.value,
-                 "frac": gflop / (kt[1] * 1e-3) / 1e3 / fp64_peak.value,
+        "fp64": {"kernel": "element_pass", "achieved_tflops": ep_tflops,
+                 "peak_tflops": fp64_peak.value, "frac": ep_tflops / fp64_peak.value,
+                 "flops_per_element": ep_flops,
                  "peak_source": "gfgpu_fp64_peak FMA microbenchmark, this run"},
         "step_hbm_frac": step_bytes / (ms * 1e-3) / 1e9 / hbm_peak,
         "e2e": {"value": e2e, "unit": "elements/s", "h2d_bytes_per_step": 8 * mf.nb_dof(),
