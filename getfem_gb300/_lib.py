@@ -63,6 +63,16 @@ class Space(C.Structure):
                 ("dofs", C.POINTER(C.c_int64))]
 
 
+class NoallocArgs(C.Structure):
+    _fields_ = [("dim", C.c_int32), ("degree", C.c_int32), ("qdim", C.c_int32),
+                ("im", C.c_char_p), ("n_elements", C.c_int64), ("n_nodes", C.c_int64),
+                ("points", C.c_void_p), ("cvpts", C.c_void_p), ("enode", C.c_void_p),
+                ("adj_ptr", C.c_void_p), ("adj", C.c_void_p),
+                ("slots", C.c_void_p * MAX_SLOTS), ("vec", C.c_void_p)]
+
+
+NOALLOC_SCRATCH_BYTES = 128 << 20
+
 _lib = None
 
 # name -> (restype, argtypes)
@@ -95,6 +105,8 @@ _PROTOS = {
     "gfgpu_copy_result": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     "gfgpu_kernel_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int32]),
     "gfgpu_fp64_peak": (C.c_int, [C.c_int32, C.POINTER(C.c_double)]),
+    "gfgpu_assemble_vector_noalloc": (C.c_int, [C.POINTER(NoallocArgs), C.POINTER(Form),
+                                                C.c_void_p]),
 }
 
 

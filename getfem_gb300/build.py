@@ -19,7 +19,7 @@ LIB = os.path.join(HERE, "libgfgpu.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 HOST_SOURCES = ["host/refelem.cc", "gfgpu_host.cc"]
-CUDA_SOURCES = ["gfgpu_api.cu", "k_simplex.cu", "k_assemble.cu", "k_probe.cu"]
+CUDA_SOURCES = ["gfgpu_api.cu", "k_simplex.cu", "k_assemble.cu", "k_probe.cu", "k_noalloc.cu"]
 
 
 def _nvcc() -> str:

@@ -43,7 +43,7 @@ namespace {
 constexpr int kEpWarps = 4;            // warps per block (share 32 elements)
 constexpr int kEpThreads = 32 * kEpWarps;
 
-template <int DIM, int QD, int NB, bool MASS>
+template <int DIM, int QD, int NB, bool MASS, bool STORE_K>
 __global__ void __launch_bounds__(kEpThreads) simplex_element_pass(
     int64_t E, const double *__restrict__ pts, const int32_t *__restrict__ cv,
     const int32_t *__restrict__ enode, const SimplexTables *__restrict__ tab, KeLayout L,
@@ -235,9 +235,12 @@ __global__ void __launch_bounds__(kEpThreads) simplex_element_pass(
       mx = bitsv > mx ? bitsv : mx;
     }
     if (active) {
-      double4 *dst = reinterpret_cast<double4 *>(o + r * RS);
+      if (STORE_K) {
+        double4 *dst = reinterpret_cast<double4 *>(o + r * RS);
 #pragma unroll
-      for (int c = 0; c < RS; c += 4) dst[c / 4] = make_double4(row[c], row[c + 1], row[c + 2], row[c + 3]);
+        for (int c = 0; c < RS; c += 4)
+          dst[c / 4] = make_double4(row[c], row[c + 1], row[c + 2], row[c + 3]);
+      }
       o[L.off_vec + r] = rv;
     }
   }
@@ -249,7 +252,7 @@ __global__ void __launch_bounds__(kEpThreads) simplex_element_pass(
     for (int k = 1; k < kEpWarps; ++k) m = mxs[k][lane] > m ? mxs[k][lane] : m;
     const double mxd = __longlong_as_double(m);
     if (!isfinite(mxd)) set_err(err, ERR_NAN);
-    o[L.off_thr] = mxd * 1e-14;
+    if (STORE_K) o[L.off_thr] = mxd * 1e-14;
 #pragma unroll
     for (int c = S; c < RS; ++c) o[L.off_vec + c] = 0.0;
   }
@@ -259,14 +262,15 @@ __global__ void __launch_bounds__(kEpThreads) simplex_element_pass(
 
 // ---------------------------------------------------------------- host
 
-// Sparse barycentric reference tensor of FEM_PK(dim, degree) for the plan's
-// quadrature rule, the reference mass matrix, and the element scratch layout.
-int build_simplex_tables(Plan &P, std::string &errmsg) {
-  const int dim = P.dim, K = P.degree;
+// Sparse barycentric reference tensor of FEM_PK(dim, degree) for the
+// quadrature rule `im`, the reference mass matrix, and the element scratch
+// layout.
+int fill_simplex_tables(int dim, int K, int qdim, const std::string &im, SimplexTables &t,
+                        KeLayout &lay, int &nq, std::string &errmsg) {
   RefElement fe(dim, SIMPLEX, K);
   Quadrature q;
-  if (!quadrature_by_name(P.im, q) || q.dim != dim) {
-    errmsg = "unsupported integration method " + P.im;
+  if (!quadrature_by_name(im, q) || q.dim != dim) {
+    errmsg = "unsupported integration method " + im;
     return GFGPU_E_UNSUPPORTED;
   }
   if (fe.nb > kMaxNb || K > 2) {
@@ -274,7 +278,6 @@ int build_simplex_tables(Plan &P, std::string &errmsg) {
     return GFGPU_E_UNSUPPORTED;
   }
   const int nb = fe.nb, nv = dim + 1;
-  SimplexTables &t = P.stab;
   std::memset(&t, 0, sizeof(t));
   t.nb = nb;
   t.nv = nv;
@@ -338,18 +341,22 @@ int build_simplex_tables(Plan &P, std::string &errmsg) {
       for (int qq = 0; qq < q.nq; ++qq) m += q.w[qq] * phi[qq * nb + i] * phi[qq * nb + j];
       t.mass[pij] = m;
     }
-  P.nq = q.nq;
-  const int qd = P.qdim, s = nb * qd;
-  P.lay.nb = nb;
-  P.lay.qd = qd;
-  P.lay.s = s;
+  nq = q.nq;
+  const int qd = qdim, s = nb * qd;
+  lay.nb = nb;
+  lay.qd = qd;
+  lay.s = s;
   // rows padded to a multiple of 4 doubles: 32-byte aligned rows and blocks
-  P.lay.rowstride = (s + 3) & ~3;
-  P.lay.off_vec = s * P.lay.rowstride;
-  P.lay.off_thr = P.lay.off_vec + P.lay.rowstride;
-  P.lay.stride = P.lay.off_thr + 4;
-  P.lay.linear = true;
+  lay.rowstride = (s + 3) & ~3;
+  lay.off_vec = s * lay.rowstride;
+  lay.off_thr = lay.off_vec + lay.rowstride;
+  lay.stride = lay.off_thr + 4;
+  lay.linear = true;
   return GFGPU_OK;
+}
+
+int build_simplex_tables(Plan &P, std::string &errmsg) {
+  return fill_simplex_tables(P.dim, P.degree, P.qdim, P.im, P.stab, P.lay, P.nq, errmsg);
 }
 
 cudaError_t launch_simplex_element_pass(Plan &P, bool with_u) {
@@ -372,11 +379,11 @@ cudaError_t launch_simplex_element_pass(Plan &P, bool with_u) {
 #define GFGPU_EP(D, Q, N)                                                                      \
   do {                                                                                         \
     if (mass)                                                                                  \
-      simplex_element_pass<D, Q, N, true><<<blocks, threads, 0, P.stream>>>(                   \
+      simplex_element_pass<D, Q, N, true, true><<<blocks, threads, 0, P.stream>>>(             \
           P.n_elements, P.d_points, P.d_cv, P.d_enode, P.d_stab, P.lay, P.form, sp, fsrc,      \
           fscale, with_u ? P.slot_ptr[GFGPU_SLOT_U] : nullptr, P.d_elem, P.d_err);             \
     else                                                                                       \
-    simplex_element_pass<D, Q, N, false><<<blocks, threads, 0, P.stream>>>(                    \
+    simplex_element_pass<D, Q, N, false, true><<<blocks, threads, 0, P.stream>>>(              \
         P.n_elements, P.d_points, P.d_cv, P.d_enode, P.d_stab, P.lay, P.form, sp, fsrc, fscale, \
         with_u ? P.slot_ptr[GFGPU_SLOT_U] : nullptr, P.d_elem, P.d_err);                     \
   } while (0)
@@ -392,6 +399,57 @@ cudaError_t launch_simplex_element_pass(Plan &P, bool with_u) {
   else return cudaErrorInvalidValue;
 #undef GFGPU_EP
   P.launches++;
+  return cudaGetLastError();
+}
+
+// The element pass storing only the element vectors V_e = K_e u_e + load
+// (layout: V_e at offset 0, `vstride` doubles per element), for callers that
+// assemble the vector alone.
+cudaError_t launch_simplex_vector_pass(int dim, int degree, int qdim, int64_t E,
+                                       const double *pts, const int32_t *cv, const int32_t *enode,
+                                       const SimplexTables *tab, const gfgpu_form &form,
+                                       const double *const *slot, double *vout, int vstride,
+                                       int *err, cudaStream_t stream) {
+  if (E == 0) return cudaSuccess;
+  KeLayout L;
+  L.qd = qdim;
+  L.off_vec = 0;
+  L.off_thr = 0;
+  L.stride = vstride;
+  SlotPtrs sp;
+  for (int i = 0; i < GFGPU_MAX_SLOTS; ++i) sp.p[i] = slot[i];
+  const double *fsrc = nullptr;
+  double fscale = 0.0;
+  bool mass = false;
+  for (int t = 0; t < form.n_terms; ++t) {
+    const gfgpu_term &T = form.terms[t];
+    if (T.kind == GFGPU_TERM_SOURCE) {
+      fsrc = slot[T.field_slot];
+      fscale = T.scale * (T.c[0].kind == GFGPU_COEF_CONST ? T.c[0].value : 1.0);
+    }
+    if (T.kind == GFGPU_TERM_MASS) mass = true;
+  }
+  const unsigned blocks = unsigned((E + 31) / 32);
+#define GFGPU_VP(D, Q, N)                                                                       \
+  do {                                                                                          \
+    if (mass)                                                                                   \
+      simplex_element_pass<D, Q, N, true, false><<<blocks, kEpThreads, 0, stream>>>(            \
+          E, pts, cv, enode, tab, L, form, sp, fsrc, fscale, slot[GFGPU_SLOT_U], vout, err);    \
+    else                                                                                        \
+      simplex_element_pass<D, Q, N, false, false><<<blocks, kEpThreads, 0, stream>>>(           \
+          E, pts, cv, enode, tab, L, form, sp, fsrc, fscale, slot[GFGPU_SLOT_U], vout, err);    \
+  } while (0)
+  const int d = dim, k = degree, q = qdim;
+  if (d == 2 && k == 1 && q == 1) GFGPU_VP(2, 1, 3);
+  else if (d == 2 && k == 2 && q == 1) GFGPU_VP(2, 1, 6);
+  else if (d == 2 && k == 1 && q == 2) GFGPU_VP(2, 2, 3);
+  else if (d == 2 && k == 2 && q == 2) GFGPU_VP(2, 2, 6);
+  else if (d == 3 && k == 1 && q == 1) GFGPU_VP(3, 1, 4);
+  else if (d == 3 && k == 2 && q == 1) GFGPU_VP(3, 1, 10);
+  else if (d == 3 && k == 1 && q == 3) GFGPU_VP(3, 3, 4);
+  else if (d == 3 && k == 2 && q == 3) GFGPU_VP(3, 3, 10);
+  else return cudaErrorInvalidValue;
+#undef GFGPU_VP
   return cudaGetLastError();
 }
 

@@ -117,5 +117,12 @@ cudaError_t launch_pattern_count(Plan &P);
 cudaError_t launch_pattern_fill(Plan &P);
 cudaError_t launch_gather(Plan &P, bool want_K, bool want_R);
 int build_simplex_tables(Plan &P, std::string &err);
+int fill_simplex_tables(int dim, int degree, int qdim, const std::string &im, SimplexTables &t,
+                        KeLayout &lay, int &nq, std::string &err);
+cudaError_t launch_simplex_vector_pass(int dim, int degree, int qdim, int64_t E,
+                                       const double *pts, const int32_t *cv, const int32_t *enode,
+                                       const SimplexTables *tab, const gfgpu_form &form,
+                                       const double *const *slot, double *vout, int vstride,
+                                       int *err, cudaStream_t stream);
 
 }  // namespace gfgpu

@@ -235,6 +235,58 @@ int gfgpu_kernel_times(gfgpu_plan *plan, float *times, int32_t n);
    compute roofline of the FP64 kernels. */
 int gfgpu_fp64_peak(int32_t kind, double *tflops);
 
+/* ------------------------------------------------------------------ */
+/* Vector assembly that allocates no device memory.                    */
+/* This entry point has no counterpart in the reference.               */
+/* ------------------------------------------------------------------ */
+
+/* Some callers cannot allocate device memory: code that works inside a
+   memory budget owned by another allocator (a framework's caching
+   allocator, an arena sized at start-up) must not call cudaMalloc behind
+   that allocator's back, and cudaMalloc/cudaFree synchronise the device,
+   which a caller assembling in a tight loop cannot afford.  For them,
+   gfgpu_assemble_vector_noalloc assembles the vector (order 1) of an
+   affine-simplex form -- the same result as a plan's gfgpu_assemble(plan, 1)
+   -- from the caller's device arrays into the caller's device output, and
+   calls no cudaMalloc, cudaFree or other allocating routine.
+
+   Its scratch (one vector of rowstride doubles per element, rowstride = the
+   element's DOF count rounded up to 4) lives in a static device array of
+   GFGPU_NOALLOC_SCRATCH_BYTES that every GPU which loads the library holds
+   until the process exits; larger meshes are rejected with GFGPU_E_INVALID
+   (about 560 000 P2 tetrahedra with 3 components, 1.4 million with one).
+
+   - The first call on a device looks up the device addresses of the static
+     arrays (cudaGetSymbolAddress, with that device current); make that first
+     call before any stream capture.
+   - Every call shares the arrays, which keep the last call's contents: each
+     call writes every element's slot before reading it and overwrites the
+     output, so nothing has to be cleared, but calls that overlap on the GPU
+     race: issue them on one stream, one after another.
+   - The call waits for its stream before returning the status.
+
+   Inputs (device memory): points (n_points x dim), cvpts (n_elements x
+   (dim+1) vertex ids), enode (n_elements x nb: DOF node of each local node,
+   i.e. first-component DOF / qdim), the node-to-element adjacency adj_ptr
+   (n_nodes + 1) and adj (entries element*nb + local node, ascending element
+   order within each node), data slots as for a plan (slot 0 = u).  Output:
+   vec (n_nodes*qdim), overwritten. */
+#define GFGPU_NOALLOC_SCRATCH_BYTES ((size_t)128 << 20)
+typedef struct {
+  int32_t dim, degree, qdim;
+  const char *im;
+  int64_t n_elements, n_nodes;
+  const double *points;
+  const int32_t *cvpts;
+  const int32_t *enode;
+  const int32_t *adj_ptr;
+  const int32_t *adj;
+  const double *slots[GFGPU_MAX_SLOTS];
+  double *vec;
+} gfgpu_noalloc_args;
+int gfgpu_assemble_vector_noalloc(const gfgpu_noalloc_args *args, const gfgpu_form *form,
+                                  void *cuda_stream);
+
 /* Number of kernel launches issued by the plan since creation. */
 int64_t gfgpu_launch_count(gfgpu_plan *plan);
 

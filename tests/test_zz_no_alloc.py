@@ -1,0 +1,104 @@
+"""The allocation-free vector assembly (gfgpu_assemble_vector_noalloc), for
+callers that must not allocate device memory themselves, against the plan
+entry point: same vector within the suite's tolerance, on two calls in a row.
+
+Collected last so that a run stopping at the first failure has run every
+other test first; it also passes alone in a fresh process."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import getfem_gb300 as g
+from getfem_gb300 import _lib as L
+from getfem_gb300 import gwfl
+
+from common import RTOL, vec_errors
+
+pytestmark = pytest.mark.gpu
+
+
+def _problem(nx=5, seed=21):
+    rng = np.random.default_rng(seed)
+    h = 1.0 / nx
+    jit = rng.uniform(-0.1 * h, 0.1 * h, ((nx + 1) ** 3, 3))
+    mesh = g.Mesh.regular_unit(3, nx, "simplex", jitter=jit)
+    mf = g.MeshFem(mesh, 3, fem="FEM_PK(3,2)")
+    mf0 = g.MeshFem(mesh, 1, fem="FEM_PK(3,0)")
+    mim = g.MeshIm(mesh, "IM_TETRAHEDRON(5)")
+    E = mesh.nb_convex()
+    ws = g.GaWorkspace()
+    ws.add_fem_variable("u", mf, U=rng.standard_normal(mf.nb_dof()) * 0.01)
+    ws.add_fem_constant("lambda", mf0, np.exp(rng.normal(0, 0.2, E)))
+    ws.add_fem_constant("mu", mf0, np.exp(rng.normal(0, 0.2, E)))
+    ws.add_fem_constant("f", mf, rng.standard_normal(mf.nb_dof()))
+    ws.add_expression("(lambda*Div_u*Id(3)+2*mu*Sym(Grad_u)):Grad_Test_u - f.Test_u", mim)
+    return mesh, mf, mim, ws
+
+
+def _adjacency(enode, n_nodes):
+    """node -> element*nb + local node, ascending element order (counting sort)."""
+    E, nb = enode.shape
+    flat = enode.ravel()
+    order = np.argsort(flat, kind="stable")  # stable: element order kept per node
+    ptr = np.zeros(n_nodes + 1, dtype=np.int64)
+    np.add.at(ptr, flat + 1, 1)
+    return np.cumsum(ptr).astype(np.int32), order.astype(np.int32)
+
+
+def test_noalloc_vector_matches_plan_vector_twice():
+    torch = pytest.importorskip("torch")
+    mesh, mf, mim, ws = _problem()
+    ws.assembly(1)
+    R_plan = ws.assembled_vector()
+
+    dev = torch.device("cuda", 0)
+    qd = mf.qdim
+    enode = (mf.dofs // qd).astype(np.int32)
+    n_nodes = mf.nb_dof() // qd
+    adj_ptr, adj = _adjacency(enode, n_nodes)
+    keep = []
+
+    def dptr(a, dtype):
+        t = torch.from_numpy(np.ascontiguousarray(a).astype(dtype)).to(dev)
+        keep.append(t)
+        return t.data_ptr()
+
+    args = L.NoallocArgs()
+    args.dim, args.degree, args.qdim = 3, 2, qd
+    args.im = mim.im.encode()
+    args.n_elements, args.n_nodes = mesh.nb_convex(), n_nodes
+    args.points = dptr(mesh.points, np.float64)
+    args.cvpts = dptr(mesh.cvpts, np.int32)
+    args.enode = dptr(enode, np.int32)
+    args.adj_ptr = dptr(adj_ptr, np.int32)
+    args.adj = dptr(adj, np.int32)
+    for d in ws.data.values():
+        if d.slot >= 0:
+            args.slots[d.slot] = dptr(np.asarray(d.values, dtype=np.float64), np.float64)
+    out = torch.full((mf.nb_dof(),), float("nan"), dtype=torch.float64, device=dev)
+    args.vec = out.data_ptr()
+    form = gwfl.to_form(ws.groups[0].order1)
+    lib = L.lib()
+    results = []
+    for _ in range(2):
+        out.fill_(float("nan"))
+        torch.cuda.synchronize()
+        L.check(lib.gfgpu_assemble_vector_noalloc(C.byref(args), C.byref(form), None))
+        results.append(out.cpu().numpy().copy())
+    for R in results:
+        assert vec_errors(R, R_plan).max() <= RTOL
+    assert np.array_equal(results[0], results[1])
+
+
+def test_noalloc_rejects_meshes_beyond_its_scratch():
+    args = L.NoallocArgs()
+    args.dim, args.degree, args.qdim = 3, 2, 3
+    args.im = b"IM_TETRAHEDRON(5)"
+    args.n_elements = L.NOALLOC_SCRATCH_BYTES // (32 * 8) + 1
+    args.n_nodes = 10
+    args.points = args.cvpts = args.enode = args.adj_ptr = args.adj = args.vec = 1
+    form = L.Form()
+    status = L.lib().gfgpu_assemble_vector_noalloc(C.byref(args), C.byref(form), None)
+    assert status == L.E_INVALID
+    assert b"GFGPU_NOALLOC_SCRATCH_BYTES" in L.lib().gfgpu_last_error()
