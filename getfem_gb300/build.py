@@ -19,7 +19,11 @@ LIB = os.path.join(HERE, "libgfgpu.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 HOST_SOURCES = ["host/refelem.cc", "gfgpu_host.cc"]
-CUDA_SOURCES = ["gfgpu_api.cu", "k_simplex.cu", "k_assemble.cu", "k_probe.cu", "k_noalloc.cu"]
+CUDA_SOURCES = ["gfgpu_api.cu", "k_simplex.cu", "k_assemble.cu", "k_probe.cu", "k_noalloc.cu",
+                "k_hex.cu"]
+# per-file nvcc flags: the Gauss-point kernels round like the reference's
+# sequence of products and sums (no implicit contraction; explicit fma only)
+CUDA_FLAGS = {"k_hex.cu": ["-fmad=false"]}
 
 
 def _nvcc() -> str:
@@ -64,8 +68,8 @@ def build(verbose: bool = False) -> str:
         objs.append(obj)
         if _stale(obj, [src] + headers):
             jobs.append([nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                         "-Xcompiler", "-ffp-contract=off",
-                         "-Xptxas", "-v" if verbose else "-O3", "-c", src, "-o", obj])
+                         "-Xcompiler", "-ffp-contract=off"] + CUDA_FLAGS.get(s, []) +
+                        ["-Xptxas", "-v" if verbose else "-O3", "-c", src, "-o", obj])
     if jobs:
         with ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
             list(ex.map(_run, jobs))

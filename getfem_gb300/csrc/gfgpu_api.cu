@@ -93,6 +93,49 @@ bool simplex_form_supported(const gfgpu_form &f, int qdim, int dim, std::string 
   return true;
 }
 
+// The forms of the Gauss-point kernels: GRADGRAD / MASS / SOURCE terms
+// with constant, per-element or nodal coefficients (LAW_ISO), or one
+// compressible neo-Hookean term on a 3-D vector field (LAW_NH).
+bool hex_form_supported(const gfgpu_form &f, int qdim, int dim, int &law, std::string &why) {
+  if (f.n_terms < 1 || f.n_terms > GFGPU_MAX_TERMS) {
+    why = "empty form";
+    return false;
+  }
+  law = LAW_ISO;
+  for (int t = 0; t < f.n_terms; ++t) {
+    const gfgpu_term &T = f.terms[t];
+    if (T.kind == GFGPU_TERM_NEOHOOKEAN) {
+      if (f.n_terms != 1) {
+        why = "a neo-Hookean term is lowered alone";
+        return false;
+      }
+      if (qdim != 3 || dim != 3) {
+        why = "neo-Hookean law is 3-D only";
+        return false;
+      }
+      law = LAW_NH;
+    } else if (T.kind == GFGPU_TERM_GRADGRAD) {
+      if (qdim == 1 && (T.c[0].kind != GFGPU_COEF_NONE || T.c[2].kind != GFGPU_COEF_NONE)) {
+        why = "div/transpose couplings need a vector field with qdim == dim";
+        return false;
+      }
+      if (qdim > 1 && qdim != dim) {
+        why = "qdim must equal the mesh dimension";
+        return false;
+      }
+    } else if (T.kind == GFGPU_TERM_SOURCE) {
+      if (T.field_slot <= 0 || T.field_slot >= GFGPU_MAX_SLOTS) {
+        why = "bad source field slot";
+        return false;
+      }
+    } else if (T.kind != GFGPU_TERM_MASS) {
+      why = "unknown term kind";
+      return false;
+    }
+  }
+  return true;
+}
+
 int status_from_err(int e) {
   if (e & ERR_JACOBIAN) {
     set_last_error("Non invertible matrix (det of the geometric transformation is 0)");
@@ -218,20 +261,29 @@ int gfgpu_plan_create(const gfgpu_space *space, const gfgpu_form *form, void *cu
     RefElement fe(S.dim, S.kind, S.degree);
     P->nb = fe.nb;
     P->nbg = S.kind == GFGPU_SIMPLEX ? S.dim + 1 : (1 << S.dim);
-    std::string why;
-    if (S.kind != GFGPU_SIMPLEX || S.degree > 2) {
-      set_last_error("element not lowered: only GT_PK + FEM_PK(dim,1|2) in this build");
-      delete P;
-      return GFGPU_E_UNSUPPORTED;
+    std::string why, err;
+    if (S.kind == GFGPU_SIMPLEX) {
+      if (S.degree > 2) {
+        set_last_error("element not lowered: simplices take FEM_PK(dim,1|2)");
+        delete P;
+        return GFGPU_E_UNSUPPORTED;
+      }
+      if (!simplex_form_supported(P->form, S.qdim, S.dim, why)) {
+        set_last_error("form not supported: " + why);
+        delete P;
+        return GFGPU_E_UNSUPPORTED;
+      }
+      P->affine_simplex = true;
+      rc = build_simplex_tables(*P, err);
+    } else {
+      if (!hex_form_supported(P->form, S.qdim, S.dim, P->law, why)) {
+        set_last_error("form not supported: " + why);
+        delete P;
+        return GFGPU_E_UNSUPPORTED;
+      }
+      rc = build_hex_tables(*P, err);
     }
-    if (!simplex_form_supported(P->form, S.qdim, S.dim, why)) {
-      set_last_error("form not supported: " + why);
-      delete P;
-      return GFGPU_E_UNSUPPORTED;
-    }
-    P->affine_simplex = true;
-    std::string err;
-    if ((rc = build_simplex_tables(*P, err)) != GFGPU_OK) {
+    if (rc != GFGPU_OK) {
       set_last_error(err);
       delete P;
       return rc;
@@ -293,6 +345,16 @@ int gfgpu_plan_create(const gfgpu_space *space, const gfgpu_form *form, void *cu
     CHK(up(P->d_adj_ptr, aptr.data(), aptr.size() * sizeof(int32_t)));
     CHK(up(P->d_adj, adj.data(), adj.size() * sizeof(int32_t)));
     CHK(up(P->d_stab, &P->stab, sizeof(SimplexTables)));
+    if (!P->affine_simplex) {
+      CHK(dalloc(&P->d_hval, P->h_val.size()));
+      CHK(dalloc(&P->d_hgrad, P->h_grad.size()));
+      CHK(dalloc(&P->d_ggrad, P->h_ggrad.size()));
+      CHK(dalloc(&P->d_hw, P->h_w.size()));
+      CHK(up(P->d_hval, P->h_val.data(), P->h_val.size() * sizeof(double)));
+      CHK(up(P->d_hgrad, P->h_grad.data(), P->h_grad.size() * sizeof(double)));
+      CHK(up(P->d_ggrad, P->h_ggrad.data(), P->h_ggrad.size() * sizeof(double)));
+      CHK(up(P->d_hw, P->h_w.data(), P->h_w.size() * sizeof(double)));
+    }
     GF_CUDA(cudaMemset(P->d_err, 0, sizeof(int)));
     GF_CUDA(cudaMemset(P->d_vec, 0, size_t(S.n_dof) * sizeof(double)));
 #undef CHK
@@ -313,6 +375,10 @@ void gfgpu_plan_destroy(gfgpu_plan *P) {
   dfree(P->d_adj_ptr);
   dfree(P->d_adj);
   dfree(P->d_stab);
+  dfree(P->d_hval);
+  dfree(P->d_hgrad);
+  dfree(P->d_ggrad);
+  dfree(P->d_hw);
   dfree(P->d_elem);
   dfree(P->d_rowptr);
   dfree(P->d_colidx);
@@ -365,11 +431,18 @@ static int check_slots(Plan &P, bool need_u) {
   for (int t = 0; t < P.form.n_terms; ++t) {
     const gfgpu_term &T = P.form.terms[t];
     for (int k = 0; k < 3; ++k)
+    {
       if (T.c[k].kind == GFGPU_COEF_ELEMENT &&
           (!P.slot_ptr[T.c[k].slot] || P.slot_n[T.c[k].slot] != P.n_elements)) {
         set_last_error("per-element coefficient slot not set or of wrong size");
         return GFGPU_E_STATE;
       }
+      if (T.c[k].kind == GFGPU_COEF_NODAL &&
+          (!P.slot_ptr[T.c[k].slot] || P.slot_n[T.c[k].slot] != P.n_nodes)) {
+        set_last_error("nodal coefficient slot not set or of wrong size");
+        return GFGPU_E_STATE;
+      }
+    }
     if (T.kind == GFGPU_TERM_SOURCE &&
         (!P.slot_ptr[T.field_slot] || P.slot_n[T.field_slot] != P.n_dof)) {
       set_last_error("source field slot not set or of wrong size");
@@ -391,14 +464,15 @@ int gfgpu_assemble(gfgpu_plan *P, int32_t order, int32_t flags, double *potentia
   (void)potential;
   const bool want_K = order == 2;
   const bool want_R = order == 1 || (flags & 2);
-  int rc = check_slots(*P, want_R);
+  int rc = check_slots(*P, want_R || P->law == LAW_NH);
   if (rc) return rc;
   const bool prof = (flags & GFGPU_PROFILE) != 0;
   if (prof && !P->ev[0])
     for (int i = 0; i < 4; ++i) GF_CUDA(cudaEventCreate(&P->ev[i]));
   GF_CUDA(cudaMemsetAsync(P->d_err, 0, sizeof(int), P->stream));
   if (prof) GF_CUDA(cudaEventRecord(P->ev[0], P->stream));
-  GF_CUDA(launch_simplex_element_pass(*P, want_R));
+  if (P->affine_simplex) GF_CUDA(launch_simplex_element_pass(*P, want_R));
+  else GF_CUDA(launch_hex_element_pass(*P));
   if (prof) GF_CUDA(cudaEventRecord(P->ev[1], P->stream));
   if ((want_K && (P->nnz < 0 || (flags & GFGPU_REBUILD_PATTERN))) || P->nnz < 0) {
     // the pattern is built at the first order-2 assembly; an order-1

@@ -58,6 +58,12 @@ struct DeviceBuf {
   size_t bytes = 0;
 };
 
+// pointwise law of a Gauss-point element kernel
+enum : int {
+  LAW_ISO = 0,  // GRADGRAD / MASS / SOURCE terms: isotropic linear tangent
+  LAW_NH = 1    // compressible neo-Hookean PK2 term
+};
+
 struct Plan {
   // discretisation
   int dim = 0, kind = 0, degree = 0, qdim = 0, nb = 0, nbg = 0, nq = 0;
@@ -66,6 +72,7 @@ struct Plan {
   gfgpu_form form{};
   cudaStream_t stream = nullptr;
   bool affine_simplex = false;  // simplex element pass applies
+  int law = LAW_ISO;
   bool psd = true;
 
   // device arrays
@@ -86,6 +93,10 @@ struct Plan {
   SimplexTables stab{};
   SimplexTables *d_stab = nullptr;
   KeLayout lay{};
+  // Gauss-point tables (hexahedra): values nq x nb, reference gradients
+  // nq x nb x dim, geometric gradients nq x nbg x dim, weights nq
+  std::vector<double> h_val, h_grad, h_ggrad, h_w;
+  double *d_hval = nullptr, *d_hgrad = nullptr, *d_ggrad = nullptr, *d_hw = nullptr;
 
   // element pass scratch
   double *d_elem = nullptr;     // E x lay.stride
@@ -119,6 +130,10 @@ cudaError_t launch_gather(Plan &P, bool want_K, bool want_R);
 int build_simplex_tables(Plan &P, std::string &err);
 int fill_simplex_tables(int dim, int degree, int qdim, const std::string &im, SimplexTables &t,
                         KeLayout &lay, int &nq, std::string &err);
+// Gauss-point kernels (k_hex.cu)
+int build_hex_tables(Plan &P, std::string &err);
+bool hex_kernel_available(int law, int degree, int qdim, int nq);
+cudaError_t launch_hex_element_pass(Plan &P);
 cudaError_t launch_simplex_vector_pass(int dim, int degree, int qdim, int64_t E,
                                        const double *pts, const int32_t *cv, const int32_t *enode,
                                        const SimplexTables *tab, const gfgpu_form &form,

@@ -496,6 +496,12 @@ def _lower_linear(tree, var, dim, fields, has_test2):
         th = dict(theta0)
         th[nm] = th[nm] * 2.0
         if np.max(np.abs(blocks(th) - B)) > 1e-9 * max(1.0, np.max(np.abs(B))):
+            if fields[nm].qdim == 1:
+                # a scalar field on the variable's (scalar) mesh_fem that
+                # multiplies the variable is a nodal coefficient
+                f2 = dict(fields)
+                f2[nm] = FieldInfo(nm, "nodal", 1, slot=fields[nm].slot)
+                return _lower_linear(tree, var, dim, f2, has_test2)
             raise L.UnsupportedExpression(L.E_UNSUPPORTED,
                                           f"field {nm} multiplies the variable")
 

@@ -52,6 +52,14 @@ CASES = [
      NH, {"mu": "P0", "D1": "C"}, False, "modes"),
     ("q4hex_laplace", 3, "QK", 4, 1, "IM_GAUSS_PARALLELEPIPED(3,9)", 2,
      "kappa*Grad_u.Grad_Test_u", {"kappa": "P0"}, False, "normal"),
+    ("q1hex_nodal_kappa", 3, "QK", 1, 1, "IM_GAUSS_PARALLELEPIPED(3,3)", 3,
+     "kappa*Grad_u.Grad_Test_u + 3*u*Test_u - f*Test_u", {"kappa": "S", "f": "V"}, True,
+     "normal"),
+    ("q2hex_elastic_nodal", 3, "QK", 2, 3, "IM_GAUSS_PARALLELEPIPED(3,5)", 2,
+     "(lambda*Div_u*Id(3)+2*mu*Sym(Grad_u)):Grad_Test_u - f.Test_u",
+     {"lambda": "P0", "mu": "S", "f": "V"}, True, "normal"),
+    ("q2hex_neohookean_nodal", 3, "QK", 2, 3, "IM_GAUSS_PARALLELEPIPED(3,5)", 3,
+     NH, {"mu": "S", "D1": "C"}, True, "modes"),
 ]
 
 
@@ -90,6 +98,9 @@ def make_case(case, seed):
             inputs[cname] = np.exp(rng.normal(0.0, sigma, E))
         elif ck == "V":
             inputs[cname] = rng.standard_normal(ndof) if qdim > 1 else rng.uniform(-1, 1, ndof)
+        elif ck == "S":
+            sigma = 0.3 if cname == "mu" and ukind == "modes" else 0.2
+            inputs[cname] = np.exp(rng.normal(0.0, sigma, ndof // qdim))
         elif ck == "C":
             inputs[cname] = np.array([1.5])
     with tempfile.TemporaryDirectory() as td:
@@ -138,8 +149,10 @@ def make_case(case, seed):
 def main():
     if not os.path.exists(DRIVER):
         sys.exit(f"{DRIVER} missing: make -C oracle/refbuild REF=/root/reference")
+    only = set(sys.argv[1:])  # optional: names of the fixtures to (re)make
     for i, case in enumerate(CASES):
-        make_case(case, 1000 + i)
+        if not only or case[0] in only:
+            make_case(case, 1000 + i)
 
 
 if __name__ == "__main__":
