@@ -8,5 +8,7 @@ C ABI of libgfgpu.so (include/gfgpu.h), whose kernels run on sm_103a.
 from ._lib import GfgpuError, UnsupportedExpression  # noqa: F401
 from .mesh import Mesh, MeshFem, MeshIm  # noqa: F401
 from .workspace import GaWorkspace  # noqa: F401
+from .adjoint import Potential  # noqa: F401
 
-__all__ = ["GaWorkspace", "Mesh", "MeshFem", "MeshIm", "GfgpuError", "UnsupportedExpression"]
+__all__ = ["GaWorkspace", "Mesh", "MeshFem", "MeshIm", "Potential", "GfgpuError",
+           "UnsupportedExpression"]

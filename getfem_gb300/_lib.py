@@ -22,6 +22,8 @@ SLOT_U = 0
 REBUILD_PATTERN = 1
 WITH_VECTOR = 2
 PROFILE = 4
+SLOT_POINTS = -1
+RESULT_ROWPTR, RESULT_COLIDX, RESULT_VALUES, RESULT_VECTOR = 0, 1, 2, 3
 
 _STATUS_NAMES = {
     E_INVALID: "GFGPU_E_INVALID", E_UNSUPPORTED: "GFGPU_E_UNSUPPORTED", E_CUDA: "GFGPU_E_CUDA",
@@ -107,6 +109,9 @@ _PROTOS = {
     "gfgpu_fp64_peak": (C.c_int, [C.c_int32, C.POINTER(C.c_double)]),
     "gfgpu_assemble_vector_noalloc": (C.c_int, [C.POINTER(NoallocArgs), C.POINTER(Form),
                                                 C.c_void_p]),
+    "gfgpu_potential_gradient": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64,
+                                           C.c_int32]),
+    "gfgpu_set_points": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32]),
 }
 
 

@@ -96,7 +96,7 @@ bool simplex_form_supported(const gfgpu_form &f, int qdim, int dim, std::string 
 // The forms of the Gauss-point kernels: GRADGRAD / MASS / SOURCE terms
 // with constant, per-element or nodal coefficients (LAW_ISO), or one
 // compressible neo-Hookean term on a 3-D vector field (LAW_NH).
-bool hex_form_supported(const gfgpu_form &f, int qdim, int dim, int &law, std::string &why) {
+bool gauss_form_supported(const gfgpu_form &f, int qdim, int dim, int &law, std::string &why) {
   if (f.n_terms < 1 || f.n_terms > GFGPU_MAX_TERMS) {
     why = "empty form";
     return false;
@@ -262,31 +262,40 @@ int gfgpu_plan_create(const gfgpu_space *space, const gfgpu_form *form, void *cu
     P->nb = fe.nb;
     P->nbg = S.kind == GFGPU_SIMPLEX ? S.dim + 1 : (1 << S.dim);
     std::string why, err;
-    if (S.kind == GFGPU_SIMPLEX) {
-      if (S.degree > 2) {
-        set_last_error("element not lowered: simplices take FEM_PK(dim,1|2)");
-        delete P;
-        return GFGPU_E_UNSUPPORTED;
-      }
-      if (!simplex_form_supported(P->form, S.qdim, S.dim, why)) {
-        set_last_error("form not supported: " + why);
-        delete P;
-        return GFGPU_E_UNSUPPORTED;
-      }
-      P->affine_simplex = true;
-      rc = build_simplex_tables(*P, err);
-    } else {
-      if (!hex_form_supported(P->form, S.qdim, S.dim, P->law, why)) {
-        set_last_error("form not supported: " + why);
-        delete P;
-        return GFGPU_E_UNSUPPORTED;
-      }
-      rc = build_hex_tables(*P, err);
+    if ((S.kind == GFGPU_SIMPLEX && S.degree > 2) || (S.kind == GFGPU_HEX && S.dim != 3)) {
+      set_last_error("element not lowered: FEM_PK(dim,1|2) on simplices, FEM_QK(3,K) on hexahedra");
+      delete P;
+      return GFGPU_E_UNSUPPORTED;
     }
-    if (rc != GFGPU_OK) {
+    // orders 1 and 2: the affine-simplex pass for the linear forms on
+    // simplices, else the Gauss-point element kernel; order 0: the
+    // Gauss-point potential kernel
+    if (S.kind == GFGPU_SIMPLEX && simplex_form_supported(P->form, S.qdim, S.dim, why)) {
+      P->affine_simplex = true;
+      if ((rc = build_simplex_tables(*P, err)) != GFGPU_OK) {
+        set_last_error(err);
+        delete P;
+        return rc;
+      }
+    } else if (!gauss_form_supported(P->form, S.qdim, S.dim, P->law, why)) {
+      set_last_error("form not supported: " + why);
+      delete P;
+      return GFGPU_E_UNSUPPORTED;
+    }
+    if ((rc = build_gauss_tables(*P, err)) != GFGPU_OK) {
       set_last_error(err);
       delete P;
       return rc;
+    }
+    if (!P->affine_simplex) {
+      P->kmat = S.dim == 3 && gauss_element_available(S.kind, P->law, S.degree, S.qdim, P->nq);
+      gauss_element_layout(*P);
+    }
+    P->kpot = gauss_potential_available(S.dim, S.kind, S.degree, S.qdim, P->law);
+    if (!P->kmat && !P->kpot) {
+      set_last_error("no kernel for this element, integration method and form");
+      delete P;
+      return GFGPU_E_UNSUPPORTED;
     }
     const int64_t E = S.n_elements, nb = P->nb, nbg = P->nbg;
     // validate and convert indices
@@ -312,6 +321,14 @@ int gfgpu_plan_create(const gfgpu_space *space, const gfgpu_form *form, void *cu
       for (int64_t e = 0; e < E; ++e)
         for (int li = 0; li < nb; ++li) adj[fill[en[e * nb + li]]++] = int32_t(e * nb + li);
     }
+    // point -> (element, vertex) adjacency for the shape gradient
+    std::vector<int32_t> pptr(size_t(S.n_points + 1), 0), padj(size_t(E * nbg));
+    for (int64_t k = 0; k < E * nbg; ++k) pptr[cv[k] + 1]++;
+    for (int64_t i = 0; i < S.n_points; ++i) pptr[i + 1] += pptr[i];
+    {
+      std::vector<int32_t> fill(pptr.begin(), pptr.end() - 1);
+      for (int64_t k = 0; k < E * nbg; ++k) padj[fill[cv[k]]++] = int32_t(k);
+    }
     P->max_cand = int32_t(P->max_adj * nb);
     if (P->max_cand > 4096) throw std::runtime_error("node valence too large for the pattern kernel");
     if (P->nb > 128) throw std::runtime_error("more than 128 local nodes per element");
@@ -327,7 +344,7 @@ int gfgpu_plan_create(const gfgpu_space *space, const gfgpu_form *form, void *cu
     CHK(dalloc(&P->d_adj_ptr, aptr.size()));
     CHK(dalloc(&P->d_adj, adj.size()));
     CHK(dalloc(&P->d_stab, 1));
-    CHK(dalloc(&P->d_elem, size_t(E * P->lay.stride)));
+    if (P->kmat) CHK(dalloc(&P->d_elem, size_t(E * P->lay.stride)));
     CHK(dalloc(&P->d_vec, size_t(S.n_dof)));
     CHK(dalloc(&P->d_pot, 1));
     CHK(dalloc(&P->d_err, 1));
@@ -345,7 +362,11 @@ int gfgpu_plan_create(const gfgpu_space *space, const gfgpu_form *form, void *cu
     CHK(up(P->d_adj_ptr, aptr.data(), aptr.size() * sizeof(int32_t)));
     CHK(up(P->d_adj, adj.data(), adj.size() * sizeof(int32_t)));
     CHK(up(P->d_stab, &P->stab, sizeof(SimplexTables)));
-    if (!P->affine_simplex) {
+    CHK(dalloc(&P->d_padj_ptr, pptr.size()));
+    CHK(dalloc(&P->d_padj, padj.size()));
+    CHK(up(P->d_padj_ptr, pptr.data(), pptr.size() * sizeof(int32_t)));
+    CHK(up(P->d_padj, padj.data(), padj.size() * sizeof(int32_t)));
+    {
       CHK(dalloc(&P->d_hval, P->h_val.size()));
       CHK(dalloc(&P->d_hgrad, P->h_grad.size()));
       CHK(dalloc(&P->d_ggrad, P->h_ggrad.size()));
@@ -379,6 +400,11 @@ void gfgpu_plan_destroy(gfgpu_plan *P) {
   dfree(P->d_hgrad);
   dfree(P->d_ggrad);
   dfree(P->d_hw);
+  dfree(P->d_padj_ptr);
+  dfree(P->d_padj);
+  dfree(P->d_epart);
+  dfree(P->d_npart);
+  dfree(P->d_xpart);
   dfree(P->d_elem);
   dfree(P->d_rowptr);
   dfree(P->d_colidx);
@@ -458,10 +484,26 @@ int gfgpu_assemble(gfgpu_plan *P, int32_t order, int32_t flags, double *potentia
     return GFGPU_E_INVALID;
   }
   if (order == 0) {
-    set_last_error("order 0 is not lowered for this form");
+    if (!P->kpot) {
+      set_last_error("order 0 is not lowered for this element and form");
+      return GFGPU_E_UNSUPPORTED;
+    }
+    int rc = check_slots(*P, true);
+    if (rc) return rc;
+    if (!P->d_epart && (rc = dalloc(&P->d_epart, size_t(P->n_elements)))) return rc;
+    GF_CUDA(cudaMemsetAsync(P->d_err, 0, sizeof(int), P->stream));
+    GF_CUDA(launch_potential(*P, P->d_pot));
+    if (potential) {
+      GF_CUDA(cudaMemcpyAsync(potential, P->d_pot, sizeof(double), cudaMemcpyDeviceToHost,
+                              P->stream));
+      return check_err(*P);
+    }
+    return GFGPU_OK;
+  }
+  if (!P->kmat) {
+    set_last_error("orders 1 and 2 are not lowered for this element, integration method and form");
     return GFGPU_E_UNSUPPORTED;
   }
-  (void)potential;
   const bool want_K = order == 2;
   const bool want_R = order == 1 || (flags & 2);
   int rc = check_slots(*P, want_R || P->law == LAW_NH);
@@ -483,6 +525,88 @@ int gfgpu_assemble(gfgpu_plan *P, int32_t order, int32_t flags, double *potentia
   GF_CUDA(launch_gather(*P, want_K, want_R));
   if (prof) GF_CUDA(cudaEventRecord(P->ev[3], P->stream));
   P->profiled = prof;
+  return GFGPU_OK;
+}
+
+int gfgpu_potential_gradient(gfgpu_plan *P, int32_t slot, double *grad, int64_t n,
+                             int32_t on_device) {
+  if (!P || !grad || (slot != GFGPU_SLOT_POINTS && (slot < 1 || slot >= GFGPU_MAX_SLOTS))) {
+    set_last_error("gfgpu_potential_gradient: bad arguments");
+    return GFGPU_E_INVALID;
+  }
+  if (!P->kpot) {
+    set_last_error("order 0 is not lowered for this element and form");
+    return GFGPU_E_UNSUPPORTED;
+  }
+  int rc = check_slots(*P, true);
+  if (rc) return rc;
+  // what the slot holds, from the form's coefficients
+  int64_t need = 0;
+  bool nodal = false;
+  if (slot == GFGPU_SLOT_POINTS) {
+    need = P->n_points * P->dim;
+  } else {
+    bool el = false, nd = false;
+    for (int t = 0; t < P->form.n_terms; ++t)
+      for (int k = 0; k < 3; ++k)
+        if (P->form.terms[t].c[k].slot == slot) {
+          el |= P->form.terms[t].c[k].kind == GFGPU_COEF_ELEMENT;
+          nd |= P->form.terms[t].c[k].kind == GFGPU_COEF_NODAL;
+        }
+    if (el == nd) {
+      set_last_error(el ? "slot used both as element and nodal coefficient"
+                        : "slot is not a coefficient of the form");
+      return GFGPU_E_INVALID;
+    }
+    nodal = nd;
+    need = nodal ? P->n_nodes : P->n_elements;
+  }
+  if (n != need) {
+    set_last_error("gfgpu_potential_gradient: gradient has " + std::to_string(need) + " entries");
+    return GFGPU_E_INVALID;
+  }
+  if (!P->d_epart && (rc = dalloc(&P->d_epart, size_t(P->n_elements)))) return rc;
+  double *dst = grad, *tmp = nullptr;
+  if (!on_device) {
+    if ((rc = dalloc(&tmp, size_t(need)))) return rc;
+    dst = tmp;
+  }
+  GF_CUDA(cudaMemsetAsync(P->d_err, 0, sizeof(int), P->stream));
+  cudaError_t ce;
+  if (slot == GFGPU_SLOT_POINTS) {
+    if (!P->d_xpart && (rc = dalloc(&P->d_xpart, size_t(P->n_elements) * P->nbg * P->dim))) {
+      dfree(tmp);
+      return rc;
+    }
+    ce = launch_shape_gradient(*P, dst);
+  } else {
+    if (nodal && !P->d_npart && (rc = dalloc(&P->d_npart, size_t(P->n_elements) * P->nb))) {
+      dfree(tmp);
+      return rc;
+    }
+    ce = launch_coef_gradient(*P, slot, nodal, dst);
+  }
+  if (ce == cudaSuccess && tmp)
+    ce = cudaMemcpyAsync(grad, tmp, size_t(need) * sizeof(double), cudaMemcpyDeviceToHost,
+                         P->stream);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(P->stream);
+  dfree(tmp);
+  if (ce != cudaSuccess) {
+    set_last_error(std::string("gfgpu_potential_gradient: ") + cudaGetErrorString(ce));
+    return GFGPU_E_CUDA;
+  }
+  return check_err(*P);
+}
+
+int gfgpu_set_points(gfgpu_plan *P, const double *points, int64_t n, int32_t on_device) {
+  if (!P || !points || n != P->n_points * P->dim) {
+    set_last_error("gfgpu_set_points: bad arguments");
+    return GFGPU_E_INVALID;
+  }
+  GF_CUDA(cudaMemcpyAsync(P->d_points, points, size_t(n) * sizeof(double),
+                          on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                          P->stream));
+  GF_CUDA(cudaStreamSynchronize(P->stream));
   return GFGPU_OK;
 }
 

@@ -1,0 +1,513 @@
+// Potentials (order-0 assembly) and their adjoint gradients, FP64, for every
+// element the plans take (GT_PK(N,1) + FEM_PK(N,1|2) simplices, GT_QK(3,1) +
+// FEM_QK(3,1|2|4) hexahedra).
+//
+// Order 0 of the reference's exec loop (getfem_generic_assembly_compile_and_exec.cc:
+// 8750-8869 with ga_instruction_scalar_assembly :4656-4667): E += t(q) J w_q
+// over elements and Gauss points, t the scalar integrand.  Integrands:
+//   GRADGRAD  D:Grad_u with D_ak = c1 Grad_u(a,k) + c0 div_u d_ak + c2 Grad_u(k,a)
+//   MASS      c u.u        SOURCE  c f.u
+//   NEOHOOKEAN W = C1 (j1 - 3) + D1 (sqrt|i3| - 1)^2, the strain energy of
+//             getfem_nonlinear_elasticity.cc:503-527 (1e200 if det F <= 0).
+//
+// One warp per element, one lane per Gauss point (q = lane, lane + 32, ...).
+// Three modes share the pointwise code:
+//   MODE_ENERGY  per-element energy  E_e = sum_q w_q J psi(q)
+//   MODE_COEF    derivative of E in one data slot: per element (element
+//                coefficient) and per (element, local node) (nodal
+//                coefficient); the node partials are gathered afterwards
+//   MODE_SHAPE   derivative of E in the mesh vertex coordinates x_v, with the
+//                DOF values held fixed: dE/dx_v[d] = sum_q w_q J (psi G_v[d] -
+//                sum_{a,k} P[a,k] Grad_u(a,d) G_v[k]), G_v = B grad(phi_geo_v),
+//                P = dpsi/dGrad_u; per (element, vertex), gathered per point.
+// Per-element results are combined by deterministic reductions (fixed order).
+#include <cmath>
+
+#include "host/refelem.h"
+#include "k_common.cuh"
+#include "plan.h"
+
+namespace gfgpu {
+
+namespace {
+
+constexpr int kGpWarps = 4;
+
+template <int DIM>
+__device__ __forceinline__ void geo_inverse(const double *K, double *B, double &det) {
+  // B(d,m) = B[d + DIM m] = K^{-T}, as the reference's closed forms
+  if constexpr (DIM == 2) {
+    det = K[0] * K[3] - K[1] * K[2];
+    B[0] = K[3] / det, B[1] = -K[2] / det, B[2] = -K[1] / det, B[3] = K[0] / det;
+  } else {
+    const double a0 = K[4] * K[8] - K[5] * K[7];
+    const double a1 = K[5] * K[6] - K[3] * K[8];
+    const double a2 = K[3] * K[7] - K[4] * K[6];
+    det = K[0] * a0 + K[1] * a1 + K[2] * a2;
+    double c[9];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+        c[i + 3 * j] = K[i1 + 3 * j1] * K[i2 + 3 * j2] - K[i1 + 3 * j2] * K[i2 + 3 * j1];
+      }
+    // Ki(i,j) = c(j,i) / det ; B(d,m) = Ki(m,d) = c(d,m) / det
+#pragma unroll
+    for (int k = 0; k < 9; ++k) B[k] = c[k] / det;
+  }
+}
+
+__device__ __forceinline__ double coef_val(const gfgpu_coef &c, const SlotPtrs &slots, int64_t e,
+                                           const int32_t *en, const double *phi, int nb) {
+  if (c.kind == GFGPU_COEF_CONST) return c.value;
+  if (c.kind == GFGPU_COEF_ELEMENT) return c.value * slots.p[c.slot][e];
+  if (c.kind == GFGPU_COEF_NODAL) {
+    double s = 0.0;
+    for (int j = 0; j < nb; ++j) s += phi[j] * slots.p[c.slot][en[j]];
+    return c.value * s;
+  }
+  return 0.0;
+}
+
+// derivative factor of a coefficient in the data of slot ws: d c / d theta_e
+// (element) or d c / d theta_j = factor * phi_j (nodal)
+__device__ __forceinline__ void coef_dfac(const gfgpu_coef &c, int ws, double &fe, double &fn) {
+  fe = fn = 0.0;
+  if (c.slot != ws) return;
+  if (c.kind == GFGPU_COEF_ELEMENT) fe = c.value;
+  if (c.kind == GFGPU_COEF_NODAL) fn = c.value;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <int DIM, int QD, int NB, int NBG, int LAW>
+__global__ void __launch_bounds__(kGpWarps * 32) gauss_potential_kernel(
+    int64_t E, int nq, int mode, int wslot, const double *__restrict__ pts,
+    const int32_t *__restrict__ cv, const int32_t *__restrict__ enode,
+    const double *__restrict__ hval, const double *__restrict__ hgrad,
+    const double *__restrict__ ggrad, const double *__restrict__ hw, gfgpu_form form,
+    SlotPtrs slots, double *__restrict__ out_e, double *__restrict__ out_n,
+    double *__restrict__ out_x, int *__restrict__ err) {
+  constexpr int S = NB * QD;
+  __shared__ double us_all[kGpWarps][S];
+  __shared__ double xs_all[kGpWarps][NBG * DIM];
+  __shared__ int32_t en_all[kGpWarps][NB];
+  __shared__ double dn_all[kGpWarps][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t e = int64_t(blockIdx.x) * kGpWarps + w;
+  if (e >= E) return;
+  double *us = us_all[w];
+  double *xs = xs_all[w];
+  int32_t *en = en_all[w];
+  double *dn = dn_all[w];
+  for (int j = lane; j < NB; j += 32) en[j] = enode[e * NB + j];
+  for (int k = lane; k < NBG * DIM; k += 32)
+    xs[k] = pts[int64_t(cv[e * NBG + k / DIM]) * DIM + k % DIM];
+  __syncwarp();
+  const double *u = slots.p[GFGPU_SLOT_U];
+  for (int c = lane; c < S; c += 32) us[c] = u[int64_t(en[c / QD]) * QD + c % QD];
+  __syncwarp();
+  double acc = 0.0;                  // energy or element-coefficient derivative
+  double accx[NBG * DIM];            // shape derivative partials of this lane
+#pragma unroll
+  for (int k = 0; k < NBG * DIM; ++k) accx[k] = 0.0;
+  double accn[(NB + 31) / 32];       // nodal partials, node j = lane + 32 r
+#pragma unroll
+  for (int r = 0; r < (NB + 31) / 32; ++r) accn[r] = 0.0;
+  for (int q0 = 0; q0 < nq; q0 += 32) {
+    const int q = q0 + lane;
+    const bool act = q < nq;
+    const int qq = act ? q : 0;
+    double K[DIM * DIM];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d)
+#pragma unroll
+      for (int m = 0; m < DIM; ++m) {
+        double s = 0.0;
+#pragma unroll
+        for (int v = 0; v < NBG; ++v) s += xs[v * DIM + d] * ggrad[(qq * NBG + v) * DIM + m];
+        K[d + DIM * m] = s;
+      }
+    double B[DIM * DIM], det;
+    geo_inverse<DIM>(K, B, det);
+    if (act && det == 0.0) set_err(err, ERR_JACOBIAN);
+    const double wJ = (act && det != 0.0) ? fabs(det) * hw[qq] : 0.0;
+    // Grad_u(a,d) and u(x_q)
+    double Gu[QD][DIM], uq[QD];
+#pragma unroll
+    for (int a = 0; a < QD; ++a) {
+      uq[a] = 0.0;
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) Gu[a][d] = 0.0;
+    }
+    const double *phi = hval + qq * NB;
+    for (int j = 0; j < NB; ++j) {
+      const double *hg = hgrad + (qq * NB + j) * DIM;
+      double gj[DIM];
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) {
+        double s = 0.0;
+#pragma unroll
+        for (int m = 0; m < DIM; ++m) s += hg[m] * B[d + DIM * m];
+        gj[d] = s;
+      }
+#pragma unroll
+      for (int a = 0; a < QD; ++a) {
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) Gu[a][d] += us[j * QD + a] * gj[d];
+      }
+    }
+    for (int j = 0; j < NB; ++j)
+#pragma unroll
+      for (int a = 0; a < QD; ++a) uq[a] += phi[j] * us[j * QD + a];
+    // integrand psi, P = dpsi/dGrad_u, and the coefficient derivatives
+    double psi = 0.0, de = 0.0, dnq = 0.0;
+    double P[QD][DIM];
+#pragma unroll
+    for (int a = 0; a < QD; ++a)
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) P[a][d] = 0.0;
+    if constexpr (LAW == LAW_NH) {
+      const gfgpu_term &T = form.terms[0];
+      const double sc = T.scale;
+      const double C1 = coef_val(T.c[0], slots, e, en, phi, NB);
+      const double D1 = coef_val(T.c[1], slots, e, en, phi, NB);
+      double F[9], C[9];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          double s = 0.0;
+#pragma unroll
+          for (int m = 0; m < 3; ++m) s += Gu[m][i] * Gu[m][j];
+          C[i + 3 * j] = 2.0 * (0.5 * (s + Gu[i][j] + Gu[j][i])) + (i == j ? 1.0 : 0.0);
+          F[i + 3 * j] = Gu[i][j] + (i == j ? 1.0 : 0.0);
+        }
+      const double detF = F[0] * (F[4] * F[8] - F[5] * F[7]) - F[3] * (F[1] * F[8] - F[2] * F[7]) +
+                          F[6] * (F[1] * F[5] - F[2] * F[4]);
+      double Cb[9], i3;
+      geo_inverse<3>(C, Cb, i3);  // Cb(d,m) = C^{-T}(d,m) = C^{-1}(d,m) (C symmetric)
+      const double i1 = C[0] + C[4] + C[8];
+      const double p13 = pow(fabs(i3), -1.0 / 3.0);
+      const double j1 = i1 * p13;
+      const double r = sqrt(fabs(i3)) - 1.0;
+      if (detF > 0.0) {
+        psi = sc * (C1 * (j1 - 3.0) + D1 * (r * r));
+        double f1e, f1n, f2e, f2n;
+        coef_dfac(T.c[0], wslot, f1e, f1n);
+        coef_dfac(T.c[1], wslot, f2e, f2n);
+        const double dW1 = sc * (j1 - 3.0), dW2 = sc * (r * r);
+        de = dW1 * f1e + dW2 * f2e;
+        dnq = dW1 * f1n + dW2 * f2n;
+        if (mode == 2) {
+          // P = sc F S(E), S the law's second Piola-Kirchhoff stress
+          const double dd = D1 - D1 / sqrt(fabs(i3));
+          double Sm[9];
+#pragma unroll
+          for (int k = 0; k < 9; ++k) {
+            const double di3 = Cb[k] * i3;
+            const double dj1 = ((k % 4 == 0 ? 1.0 : 0.0) - i1 / (3.0 * i3) * di3) * p13;
+            Sm[k] = 2.0 * C1 * dj1 + 2.0 * dd * di3;
+          }
+#pragma unroll
+          for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+              double s = 0.0;
+#pragma unroll
+              for (int m = 0; m < 3; ++m) s += F[a + 3 * m] * Sm[m + 3 * k];
+              P[a][k] = sc * s;
+            }
+        }
+      } else {
+        psi = sc * 1e200;
+      }
+    } else {
+      double div = 0.0;
+      if constexpr (QD > 1) {
+#pragma unroll
+        for (int a = 0; a < QD; ++a) div += Gu[a][a < DIM ? a : 0];
+      }
+      for (int t = 0; t < form.n_terms; ++t) {
+        const gfgpu_term &T = form.terms[t];
+        const double sc = T.scale;
+        if (T.kind == GFGPU_TERM_GRADGRAD) {
+          const double c0 = coef_val(T.c[0], slots, e, en, phi, NB) * sc;
+          const double c1 = coef_val(T.c[1], slots, e, en, phi, NB) * sc;
+          const double c2 = coef_val(T.c[2], slots, e, en, phi, NB) * sc;
+          double v = 0.0, gg = 0.0, gt = 0.0;
+#pragma unroll
+          for (int a = 0; a < QD; ++a)
+#pragma unroll
+            for (int k = 0; k < DIM; ++k) {
+              double Dk = c1 * Gu[a][k];
+              if constexpr (QD > 1) Dk += (k == a ? c0 * div : 0.0) + c2 * Gu[k < QD ? k : 0][a];
+              v += Dk * Gu[a][k];
+              gg += Gu[a][k] * Gu[a][k];
+              if constexpr (QD > 1) gt += Gu[k < QD ? k : 0][a] * Gu[a][k];
+              P[a][k] += 2.0 * Dk;
+            }
+          psi += v;
+          double fe, fn;
+          coef_dfac(T.c[0], wslot, fe, fn);
+          de += sc * div * div * fe, dnq += sc * div * div * fn;
+          coef_dfac(T.c[1], wslot, fe, fn);
+          de += sc * gg * fe, dnq += sc * gg * fn;
+          coef_dfac(T.c[2], wslot, fe, fn);
+          de += sc * gt * fe, dnq += sc * gt * fn;
+        } else if (T.kind == GFGPU_TERM_MASS) {
+          const double c0 = coef_val(T.c[0], slots, e, en, phi, NB) * sc;
+          double uu = 0.0;
+#pragma unroll
+          for (int a = 0; a < QD; ++a) {
+            psi += c0 * uq[a] * uq[a];
+            uu += uq[a] * uq[a];
+          }
+          double fe, fn;
+          coef_dfac(T.c[0], wslot, fe, fn);
+          de += sc * uu * fe, dnq += sc * uu * fn;
+        } else if (T.kind == GFGPU_TERM_SOURCE) {
+          const bool none = T.c[0].kind == GFGPU_COEF_NONE;
+          const double c0 = (none ? 1.0 : coef_val(T.c[0], slots, e, en, phi, NB)) * sc;
+          const double *f = slots.p[T.field_slot];
+          double fq[QD];
+#pragma unroll
+          for (int a = 0; a < QD; ++a) fq[a] = 0.0;
+          for (int j = 0; j < NB; ++j)
+#pragma unroll
+            for (int a = 0; a < QD; ++a) fq[a] += phi[j] * f[int64_t(en[j]) * QD + a];
+          double fu = 0.0;
+          for (int j = 0; j < NB; ++j)
+#pragma unroll
+            for (int a = 0; a < QD; ++a) {
+              psi += c0 * fq[a] * phi[j] * us[j * QD + a];
+              fu += fq[a] * phi[j] * us[j * QD + a];
+            }
+          if (!none) {
+            double fe, fn;
+            coef_dfac(T.c[0], wslot, fe, fn);
+            de += sc * fu * fe, dnq += sc * fu * fn;
+          }
+        }
+      }
+    }
+    if (!act) psi = de = dnq = 0.0;
+    if (mode == 0) {
+      acc += psi * wJ;
+    } else if (mode == 1) {
+      acc += de * wJ;
+      dn[lane] = dnq * wJ;
+      __syncwarp();
+      const int nlast = nq - q0 < 32 ? nq - q0 : 32;
+#pragma unroll
+      for (int r = 0; r < (NB + 31) / 32; ++r) {
+        const int j = lane + 32 * r;
+        if (j < NB) {
+          double s = 0.0;
+          for (int l = 0; l < nlast; ++l) s += dn[l] * hval[(q0 + l) * NB + j];
+          accn[r] += s;
+        }
+      }
+      __syncwarp();
+    } else {
+      // H(d,k) = psi d_dk - sum_a P(a,k) Grad_u(a,d); dE/dx_v[d] += wJ H(d,:).G_v
+      double H[DIM][DIM];
+#pragma unroll
+      for (int d = 0; d < DIM; ++d)
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) {
+          double s = d == k ? psi : 0.0;
+#pragma unroll
+          for (int a = 0; a < QD; ++a) s -= P[a][k] * Gu[a][d];
+          H[d][k] = act ? wJ * s : 0.0;
+        }
+#pragma unroll
+      for (int v = 0; v < NBG; ++v) {
+        const double *gg = ggrad + (qq * NBG + v) * DIM;
+        double Gv[DIM];
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) {
+          double s = 0.0;
+#pragma unroll
+          for (int m = 0; m < DIM; ++m) s += gg[m] * B[k + DIM * m];
+          Gv[k] = s;
+        }
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+          double s = 0.0;
+#pragma unroll
+          for (int k = 0; k < DIM; ++k) s += H[d][k] * Gv[k];
+          accx[v * DIM + d] += s;
+        }
+      }
+    }
+  }
+  if (mode == 0 || mode == 1) {
+    const double tot = warp_sum(acc);
+    if (lane == 0) {
+      if (!isfinite(tot) && mode == 1) set_err(err, ERR_NAN);
+      out_e[e] = tot;
+    }
+    if (mode == 1 && out_n) {
+#pragma unroll
+      for (int r = 0; r < (NB + 31) / 32; ++r) {
+        const int j = lane + 32 * r;
+        if (j < NB) out_n[e * NB + j] = accn[r];
+      }
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < NBG * DIM; ++k) {
+      const double tot = warp_sum(accx[k]);
+      if (lane == 0) out_x[e * NBG * DIM + k] = tot;
+    }
+  }
+}
+
+// Sum of n values in a fixed order (one block): deterministic.
+__global__ void __launch_bounds__(1024) ordered_sum(const double *__restrict__ v, int64_t n,
+                                                    double *__restrict__ out) {
+  __shared__ double s[1024];
+  const int t = threadIdx.x;
+  const int64_t per = (n + 1023) / 1024;
+  double a = 0.0;
+  for (int64_t i = t * per; i < (t + 1) * per && i < n; ++i) a += v[i];
+  s[t] = a;
+  __syncthreads();
+  for (int o = 512; o > 0; o >>= 1) {
+    if (t < o) s[t] += s[t + o];
+    __syncthreads();
+  }
+  if (t == 0) *out = s[0];
+}
+
+// out[n] = sum over the adjacency codes of node n of part[code]
+__global__ void adjacency_gather(int64_t n, int width, const int32_t *__restrict__ ptr,
+                                 const int32_t *__restrict__ adj, int nper,
+                                 const double *__restrict__ part, double *__restrict__ out) {
+  const int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (t >= n * width) return;
+  const int64_t node = t / width;
+  const int d = int(t % width);
+  double s = 0.0;
+  for (int k = ptr[node]; k < ptr[node + 1]; ++k) s += part[int64_t(adj[k]) * width + d];
+  (void)nper;
+  out[t] = s;
+}
+
+template <int DIM, int QD, int NB, int NBG, int LAW>
+cudaError_t launch_gp(Plan &P, int mode, int wslot, const SlotPtrs &sp, double *oe, double *on,
+                      double *ox) {
+  const unsigned blocks = unsigned((P.n_elements + kGpWarps - 1) / kGpWarps);
+  gauss_potential_kernel<DIM, QD, NB, NBG, LAW><<<blocks, kGpWarps * 32, 0, P.stream>>>(
+      P.n_elements, P.nq, mode, wslot, P.d_points, P.d_cv, P.d_enode, P.d_hval, P.d_hgrad,
+      P.d_ggrad, P.d_hw, P.form, sp, oe, on, ox, P.d_err);
+  return cudaGetLastError();
+}
+
+cudaError_t dispatch_gp(Plan &P, int mode, int wslot, double *oe, double *on, double *ox) {
+  SlotPtrs sp;
+  for (int i = 0; i < GFGPU_MAX_SLOTS; ++i) sp.p[i] = P.slot_ptr[i];
+  const int k = P.degree, q = P.qdim;
+  if (P.law == LAW_NH) {
+    if (P.kind == HEX && k == 2) return launch_gp<3, 3, 27, 8, LAW_NH>(P, mode, wslot, sp, oe, on, ox);
+    if (P.kind == HEX && k == 1) return launch_gp<3, 3, 8, 8, LAW_NH>(P, mode, wslot, sp, oe, on, ox);
+    if (P.kind == SIMPLEX && k == 2) return launch_gp<3, 3, 10, 4, LAW_NH>(P, mode, wslot, sp, oe, on, ox);
+    if (P.kind == SIMPLEX && k == 1) return launch_gp<3, 3, 4, 4, LAW_NH>(P, mode, wslot, sp, oe, on, ox);
+    return cudaErrorInvalidValue;
+  }
+#define GP(D, Q, NB, NBG) return launch_gp<D, Q, NB, NBG, LAW_ISO>(P, mode, wslot, sp, oe, on, ox)
+  if (P.kind == SIMPLEX && P.dim == 2) {
+    if (k == 1 && q == 1) GP(2, 1, 3, 3);
+    if (k == 2 && q == 1) GP(2, 1, 6, 3);
+    if (k == 1 && q == 2) GP(2, 2, 3, 3);
+    if (k == 2 && q == 2) GP(2, 2, 6, 3);
+  } else if (P.kind == SIMPLEX && P.dim == 3) {
+    if (k == 1 && q == 1) GP(3, 1, 4, 4);
+    if (k == 2 && q == 1) GP(3, 1, 10, 4);
+    if (k == 1 && q == 3) GP(3, 3, 4, 4);
+    if (k == 2 && q == 3) GP(3, 3, 10, 4);
+  } else if (P.kind == HEX) {
+    if (k == 1 && q == 1) GP(3, 1, 8, 8);
+    if (k == 2 && q == 1) GP(3, 1, 27, 8);
+    if (k == 4 && q == 1) GP(3, 1, 125, 8);
+    if (k == 1 && q == 3) GP(3, 3, 8, 8);
+    if (k == 2 && q == 3) GP(3, 3, 27, 8);
+  }
+#undef GP
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+bool gauss_potential_available(int dim, int kind, int degree, int qdim, int law) {
+  if (law == LAW_NH) return dim == 3 && qdim == 3 && degree <= 2;
+  if (kind == SIMPLEX) return degree <= 2 && (qdim == 1 || qdim == dim);
+  return dim == 3 && ((degree <= 2 && (qdim == 1 || qdim == 3)) || (degree == 4 && qdim == 1));
+}
+
+// Gauss tables of any element (values, reference gradients, geometric
+// gradients, weights) into the plan's host vectors.
+int build_gauss_tables(Plan &P, std::string &errmsg) {
+  RefElement fe(P.dim, P.kind, P.degree), gt(P.dim, P.kind, 1);
+  Quadrature q;
+  if (!quadrature_by_name(P.im, q) || q.dim != P.dim) {
+    errmsg = "unsupported integration method " + P.im;
+    return GFGPU_E_UNSUPPORTED;
+  }
+  P.nq = q.nq;
+  const int D = P.dim;
+  P.h_val.assign(size_t(q.nq) * fe.nb, 0.0);
+  P.h_grad.assign(size_t(q.nq) * fe.nb * D, 0.0);
+  P.h_ggrad.assign(size_t(q.nq) * gt.nb * D, 0.0);
+  std::vector<double> gv(gt.nb);
+  for (int k = 0; k < q.nq; ++k) {
+    fe.eval(&q.pts[size_t(k) * D], &P.h_val[size_t(k) * fe.nb], &P.h_grad[size_t(k) * fe.nb * D]);
+    gt.eval(&q.pts[size_t(k) * D], gv.data(), &P.h_ggrad[size_t(k) * gt.nb * D]);
+  }
+  P.h_w = q.w;
+  return GFGPU_OK;
+}
+
+cudaError_t launch_potential(Plan &P, double *d_out) {
+  if (P.n_elements == 0) return cudaMemsetAsync(d_out, 0, sizeof(double), P.stream);
+  cudaError_t ce = dispatch_gp(P, 0, -1, P.d_epart, nullptr, nullptr);
+  if (ce != cudaSuccess) return ce;
+  ordered_sum<<<1, 1024, 0, P.stream>>>(P.d_epart, P.n_elements, d_out);
+  P.launches += 2;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_coef_gradient(Plan &P, int slot, bool nodal, double *d_out) {
+  if (P.n_elements == 0) return cudaSuccess;
+  cudaError_t ce = dispatch_gp(P, 1, slot, nodal ? P.d_epart : d_out, nodal ? P.d_npart : nullptr,
+                               nullptr);
+  if (ce != cudaSuccess) return ce;
+  P.launches++;
+  if (nodal) {
+    const int64_t n = P.n_nodes;
+    adjacency_gather<<<unsigned((n + 255) / 256), 256, 0, P.stream>>>(
+        n, 1, P.d_adj_ptr, P.d_adj, P.nb, P.d_npart, d_out);
+    P.launches++;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_shape_gradient(Plan &P, double *d_out) {
+  if (P.n_elements == 0) return cudaMemsetAsync(d_out, 0, sizeof(double) * P.n_points * P.dim,
+                                                P.stream);
+  cudaError_t ce = dispatch_gp(P, 2, -1, nullptr, nullptr, P.d_xpart);
+  if (ce != cudaSuccess) return ce;
+  const int64_t n = P.n_points;
+  adjacency_gather<<<unsigned((n * P.dim + 255) / 256), 256, 0, P.stream>>>(
+      n, P.dim, P.d_padj_ptr, P.d_padj, P.nbg, P.d_xpart, d_out);
+  P.launches += 2;
+  return cudaGetLastError();
+}
+
+}  // namespace gfgpu

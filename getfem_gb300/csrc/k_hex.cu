@@ -1,4 +1,5 @@
-// Gauss-point element kernel for hexahedra (GT_QK(3,1) + FEM_QK(3,K)), FP64.
+// Gauss-point element kernel for 3-D elements (GT_QK(3,1) + FEM_QK(3,K)
+// hexahedra, GT_PK(3,1) + FEM_PK(3,K) tetrahedra), FP64.
 //
 // The reference's exec loop (getfem_generic_assembly_compile_and_exec.cc:
 // 8750-8869) for one element per CTA, with the Gauss points processed in
@@ -36,7 +37,6 @@ namespace gfgpu {
 namespace {
 
 constexpr int kHexThreads = 256;
-constexpr int NBG = 8;    // GT_QK(3,1) vertices
 constexpr int kLaw = 40;  // per-q neo-Hookean state for the tangent (doubles)
 constexpr int kRes = 36;  // per-q residual state (doubles)
 
@@ -100,7 +100,7 @@ __device__ __forceinline__ double nh_dsde(const double *st, int i, int j, int k,
   return 4.0 * C1 * ddj1 + 4.0 * dd * ddi3 + 4.0 * A22 * dij * dkl;
 }
 
-template <int QD, int NB, int NQ, int LAW>
+template <int QD, int NB, int NBG, int NQ, int LAW>
 struct HexSmem {
   static constexpr int S = NB * QD, NA = 3 * QD;
   static constexpr int n_g = NQ * NB * 3, n_A = NQ * NA * NA, n_c = NQ, n_m = NQ,
@@ -119,14 +119,14 @@ struct HexSmem {
   static_assert(QD * S * RG <= kHexThreads, "element too large for one CTA");
 };
 
-template <int QD, int NB, int NQ, int LAW>
+template <int QD, int NB, int NBG, int NQ, int LAW>
 __global__ void __launch_bounds__(kHexThreads) hex_element_kernel(
     int64_t E, const double *__restrict__ pts, const int32_t *__restrict__ cv,
     const int32_t *__restrict__ enode, const double *__restrict__ hval,
     const double *__restrict__ hgrad, const double *__restrict__ ggrad,
     const double *__restrict__ hw, KeLayout L, gfgpu_form form, SlotPtrs slots,
     double *__restrict__ out, int *__restrict__ err) {
-  using M = HexSmem<QD, NB, NQ, LAW>;
+  using M = HexSmem<QD, NB, NBG, NQ, LAW>;
   constexpr int S = M::S, NA = M::NA;
   extern __shared__ __align__(16) double sm[];
   double *gq = sm + M::o_g;   // [q][j][d] real gradients
@@ -433,10 +433,10 @@ __global__ void __launch_bounds__(kHexThreads) hex_element_kernel(
   }
 }
 
-template <int QD, int NB, int NQ, int LAW>
+template <int QD, int NB, int NBG, int NQ, int LAW>
 cudaError_t launch_hex_t(Plan &P, const SlotPtrs &sp) {
-  using M = HexSmem<QD, NB, NQ, LAW>;
-  auto kern = hex_element_kernel<QD, NB, NQ, LAW>;
+  using M = HexSmem<QD, NB, NBG, NQ, LAW>;
+  auto kern = hex_element_kernel<QD, NB, NBG, NQ, LAW>;
   cudaError_t ce = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         int(M::bytes));
   if (ce != cudaSuccess) return ce;
@@ -448,37 +448,21 @@ cudaError_t launch_hex_t(Plan &P, const SlotPtrs &sp) {
 
 }  // namespace
 
-// Tables of the hexahedral element at the plan's quadrature points (values,
-// reference gradients, geometric-transformation gradients, weights), kept on
-// the host in the plan for upload, and the element scratch layout.
-int build_hex_tables(Plan &P, std::string &errmsg) {
-  if (P.dim != 3) {
-    errmsg = "hexahedral kernels are 3-D";
-    return GFGPU_E_UNSUPPORTED;
+bool gauss_element_available(int kind, int law, int degree, int qdim, int nq) {
+  if (kind == HEX) {
+    const bool nq_ok = (degree == 1 && (nq == 8 || nq == 27)) || (degree == 2 && nq == 27);
+    if (law == LAW_NH) return qdim == 3 && nq_ok;
+    return (qdim == 1 || qdim == 3) && nq_ok;
   }
-  RefElement fe(3, HEX, P.degree), gt(3, HEX, 1);
-  Quadrature q;
-  if (!quadrature_by_name(P.im, q) || q.dim != 3) {
-    errmsg = "unsupported integration method " + P.im;
-    return GFGPU_E_UNSUPPORTED;
-  }
-  if (!hex_kernel_available(P.law, P.degree, P.qdim, q.nq)) {
-    errmsg = "no hexahedral kernel for FEM_QK(3," + std::to_string(P.degree) + "), qdim " +
-             std::to_string(P.qdim) + ", " + std::to_string(q.nq) + " Gauss points";
-    return GFGPU_E_UNSUPPORTED;
-  }
-  P.nq = q.nq;
-  P.h_val.assign(size_t(q.nq) * fe.nb, 0.0);
-  P.h_grad.assign(size_t(q.nq) * fe.nb * 3, 0.0);
-  P.h_ggrad.assign(size_t(q.nq) * gt.nb * 3, 0.0);
-  std::vector<double> gv(gt.nb);
-  for (int k = 0; k < q.nq; ++k) {
-    fe.eval(&q.pts[size_t(k) * 3], &P.h_val[size_t(k) * fe.nb], &P.h_grad[size_t(k) * fe.nb * 3]);
-    gt.eval(&q.pts[size_t(k) * 3], gv.data(), &P.h_ggrad[size_t(k) * gt.nb * 3]);
-  }
-  P.h_w = q.w;
-  const int s = fe.nb * P.qdim;
-  P.lay.nb = fe.nb;
+  // tetrahedra: the neo-Hookean law (the linear forms take the simplex pass)
+  return law == LAW_NH && qdim == 3 &&
+         ((degree == 2 && nq == 15) || (degree == 1 && (nq == 4 || nq == 15)));
+}
+
+// Element scratch layout of the Gauss-point kernel.
+void gauss_element_layout(Plan &P) {
+  const int s = P.nb * P.qdim;
+  P.lay.nb = P.nb;
   P.lay.qd = P.qdim;
   P.lay.s = s;
   P.lay.rowstride = (s + 3) & ~3;
@@ -486,13 +470,6 @@ int build_hex_tables(Plan &P, std::string &errmsg) {
   P.lay.off_thr = P.lay.off_vec + P.lay.rowstride;
   P.lay.stride = P.lay.off_thr + 4;
   P.lay.linear = P.law != LAW_NH;
-  return GFGPU_OK;
-}
-
-bool hex_kernel_available(int law, int degree, int qdim, int nq) {
-  const bool nq_ok = (degree == 1 && (nq == 8 || nq == 27)) || (degree == 2 && nq == 27);
-  if (law == LAW_NH) return qdim == 3 && nq_ok;
-  return (qdim == 1 || qdim == 3) && nq_ok;
 }
 
 cudaError_t launch_hex_element_pass(Plan &P) {
@@ -504,18 +481,22 @@ cudaError_t launch_hex_element_pass(Plan &P) {
   if (P.slot_n[GFGPU_SLOT_U] != P.n_dof) sp.p[GFGPU_SLOT_U] = nullptr;
   const int k = P.degree, q = P.qdim, nq = P.nq;
   cudaError_t ce = cudaErrorInvalidValue;
-  if (P.law == LAW_NH) {
-    if (k == 2 && nq == 27) ce = launch_hex_t<3, 27, 27, LAW_NH>(P, sp);
-    else if (k == 1 && nq == 8) ce = launch_hex_t<3, 8, 8, LAW_NH>(P, sp);
-    else if (k == 1 && nq == 27) ce = launch_hex_t<3, 8, 27, LAW_NH>(P, sp);
+  if (P.kind != HEX) {
+    if (P.law == LAW_NH && k == 2 && nq == 15) ce = launch_hex_t<3, 10, 4, 15, LAW_NH>(P, sp);
+    else if (P.law == LAW_NH && k == 1 && nq == 4) ce = launch_hex_t<3, 4, 4, 4, LAW_NH>(P, sp);
+    else if (P.law == LAW_NH && k == 1 && nq == 15) ce = launch_hex_t<3, 4, 4, 15, LAW_NH>(P, sp);
+  } else if (P.law == LAW_NH) {
+    if (k == 2 && nq == 27) ce = launch_hex_t<3, 27, 8, 27, LAW_NH>(P, sp);
+    else if (k == 1 && nq == 8) ce = launch_hex_t<3, 8, 8, 8, LAW_NH>(P, sp);
+    else if (k == 1 && nq == 27) ce = launch_hex_t<3, 8, 8, 27, LAW_NH>(P, sp);
   } else if (q == 1) {
-    if (k == 1 && nq == 8) ce = launch_hex_t<1, 8, 8, LAW_ISO>(P, sp);
-    else if (k == 1 && nq == 27) ce = launch_hex_t<1, 8, 27, LAW_ISO>(P, sp);
-    else if (k == 2 && nq == 27) ce = launch_hex_t<1, 27, 27, LAW_ISO>(P, sp);
+    if (k == 1 && nq == 8) ce = launch_hex_t<1, 8, 8, 8, LAW_ISO>(P, sp);
+    else if (k == 1 && nq == 27) ce = launch_hex_t<1, 8, 8, 27, LAW_ISO>(P, sp);
+    else if (k == 2 && nq == 27) ce = launch_hex_t<1, 27, 8, 27, LAW_ISO>(P, sp);
   } else if (q == 3) {
-    if (k == 1 && nq == 8) ce = launch_hex_t<3, 8, 8, LAW_ISO>(P, sp);
-    else if (k == 1 && nq == 27) ce = launch_hex_t<3, 8, 27, LAW_ISO>(P, sp);
-    else if (k == 2 && nq == 27) ce = launch_hex_t<3, 27, 27, LAW_ISO>(P, sp);
+    if (k == 1 && nq == 8) ce = launch_hex_t<3, 8, 8, 8, LAW_ISO>(P, sp);
+    else if (k == 1 && nq == 27) ce = launch_hex_t<3, 8, 8, 27, LAW_ISO>(P, sp);
+    else if (k == 2 && nq == 27) ce = launch_hex_t<3, 27, 8, 27, LAW_ISO>(P, sp);
   }
   if (ce == cudaSuccess) P.launches++;
   return ce;

@@ -97,6 +97,12 @@ struct Plan {
   // nq x nb x dim, geometric gradients nq x nbg x dim, weights nq
   std::vector<double> h_val, h_grad, h_ggrad, h_w;
   double *d_hval = nullptr, *d_hgrad = nullptr, *d_ggrad = nullptr, *d_hw = nullptr;
+  bool kmat = true;        // an element-matrix kernel exists (orders 1 and 2)
+  bool kpot = false;       // the Gauss-point potential kernel exists (order 0)
+  // point -> (element, vertex) adjacency, codes e * nbg + v sorted by e
+  int32_t *d_padj_ptr = nullptr, *d_padj = nullptr;
+  // per-element partials of potentials and gradients (allocated on use)
+  double *d_epart = nullptr, *d_npart = nullptr, *d_xpart = nullptr;
 
   // element pass scratch
   double *d_elem = nullptr;     // E x lay.stride
@@ -130,9 +136,15 @@ cudaError_t launch_gather(Plan &P, bool want_K, bool want_R);
 int build_simplex_tables(Plan &P, std::string &err);
 int fill_simplex_tables(int dim, int degree, int qdim, const std::string &im, SimplexTables &t,
                         KeLayout &lay, int &nq, std::string &err);
-// Gauss-point kernels (k_hex.cu)
-int build_hex_tables(Plan &P, std::string &err);
-bool hex_kernel_available(int law, int degree, int qdim, int nq);
+// potentials and adjoint gradients (k_gauss.cu)
+bool gauss_potential_available(int dim, int kind, int degree, int qdim, int law);
+int build_gauss_tables(Plan &P, std::string &err);
+cudaError_t launch_potential(Plan &P, double *d_out);
+cudaError_t launch_coef_gradient(Plan &P, int slot, bool nodal, double *d_out);
+cudaError_t launch_shape_gradient(Plan &P, double *d_out);
+// Gauss-point element kernels (k_hex.cu)
+bool gauss_element_available(int kind, int law, int degree, int qdim, int nq);
+void gauss_element_layout(Plan &P);
 cudaError_t launch_hex_element_pass(Plan &P);
 cudaError_t launch_simplex_vector_pass(int dim, int degree, int qdim, int64_t E,
                                        const double *pts, const int32_t *cv, const int32_t *enode,

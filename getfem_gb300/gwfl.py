@@ -449,10 +449,10 @@ def _coef_terms(c_const, c_fields, fields):
     return out
 
 
-def _lower_linear(tree, var, dim, fields, has_test2):
+def _lower_linear(tree, var, dim, fields, has_test2, probe=None):
     """Lower a weak form affine in u (or bilinear in Test/Test2)."""
     Q, N = var.qdim, dim
-    P = _Probe(tree, var, dim, fields)
+    P = probe(fields) if probe is not None else _Probe(tree, var, dim, fields)
     vals, grads = _basis(Q, N)
     zQ, zG = np.zeros(Q), np.zeros((Q, N))
     scal_fields = [nm for nm, f in fields.items() if f.kind in ("element", "nodal")]
@@ -501,7 +501,7 @@ def _lower_linear(tree, var, dim, fields, has_test2):
                 # multiplies the variable is a nodal coefficient
                 f2 = dict(fields)
                 f2[nm] = FieldInfo(nm, "nodal", 1, slot=fields[nm].slot)
-                return _lower_linear(tree, var, dim, f2, has_test2)
+                return _lower_linear(tree, var, dim, f2, has_test2, probe)
             raise L.UnsupportedExpression(L.E_UNSUPPORTED,
                                           f"field {nm} multiplies the variable")
 
@@ -637,6 +637,71 @@ def _match_neohookean(tree, var):
     return a1.args[0][0], a1.args[1][0]
 
 
+def _match_neohookean_potential(tree, var):
+    """Compressible_Neo_Hookean_potential(Grad_u,[p1;p2])"""
+    S = tree
+    if not (S.kind == "call" and S.value == "Compressible_Neo_Hookean_potential"
+            and len(S.args) == 2):
+        return None
+    a0, a1 = S.args
+    if not (a0.kind == "name" and a0.value == "Grad_" + var.name):
+        return None
+    if a1.kind != "matrix" or len(a1.args) != 2 or any(len(r) != 1 for r in a1.args):
+        return None
+    return a1.args[0][0], a1.args[1][0]
+
+
+class _PolarProbe(_Probe):
+    """Probe of a potential P(u) quadratic in (u, Grad_u): evaluates the
+    polarisation (P(U + V) - P(U - V)) / 4 = B(U, V) + L(V) / 2, where
+    P(u) = B(u, u) + L(u), as the affine weak form the linear lowering reads."""
+
+    def eval(self, V=None, GV=None, theta=None, U=None, GU=None, V2=None, GV2=None):
+        plus = float(evaluate(self.tree, self.env(U=U + V, GU=GU + GV, V=None, GV=None,
+                                                  theta=theta)))
+        minus = float(evaluate(self.tree, self.env(U=U - V, GU=GU - GV, V=None, GV=None,
+                                                   theta=theta)))
+        return (plus - minus) / 4.0
+
+
+def _lower_potential(tree, var, dim, fields) -> "Lowered":
+    """A potential quadratic in u: order 0 assembles P(u) = B(u,u) + L(u),
+    order 1 its derivative 2 B(u, .) + L, order 2 the bilinear form 2 B (the
+    derivatives GWFL's Diff gives for such a potential)."""
+    Q, N = var.qdim, dim
+    base = _Probe(tree, var, dim, fields)
+    zQ, zG = np.zeros(Q), np.zeros((Q, N))
+    th = {nm: 1.0 for nm, f in fields.items() if f.kind in ("element", "nodal")}
+    for nm, f in fields.items():
+        if f.kind == "vfield":
+            th[nm] = np.ones(f.qdim)
+    if abs(base.eval(U=zQ, GU=zG, V=None, GV=None, theta=th)) > 0:
+        raise L.UnsupportedExpression(L.E_UNSUPPORTED,
+                                      "potential terms independent of the variable")
+    terms2, terms1 = _lower_linear(tree, var, dim, fields, False,
+                                   probe=lambda f: _PolarProbe(tree, var, dim, f))
+    # quadratic check: P(2u) = 4 B(u,u) + 2 L(u)
+    rng = np.random.default_rng(99)
+    Ur, GUr = rng.uniform(-1, 1, Q), rng.uniform(-1, 1, (Q, N))
+    p1 = base.eval(U=Ur, GU=GUr, V=None, GV=None, theta=th)
+    p2 = base.eval(U=2 * Ur, GU=2 * GUr, V=None, GV=None, theta=th)
+    pm = base.eval(U=-Ur, GU=-GUr, V=None, GV=None, theta=th)
+    quad, lin = (p1 + pm) / 2.0, (p1 - pm) / 2.0
+    if abs(p2 - (4 * quad + 2 * lin)) > 1e-9 * max(1.0, abs(p2)):
+        raise L.UnsupportedExpression(L.E_UNSUPPORTED, "potential is not quadratic in u")
+    src = []
+    for t in terms1:
+        t2 = dict(t)
+        t2["scale"] = 2.0 * t["scale"]   # the probe saw L / 2
+        src.append(t2)
+    dbl = []
+    for t in terms2:
+        t2 = dict(t)
+        t2["scale"] = 2.0 * t["scale"]
+        dbl.append(t2)
+    return Lowered(order2=dbl, order1=dbl + src, order0=terms2 + src, max_order=0)
+
+
 def lower(expr: str, var: FieldInfo, dim: int, fields: dict, add_derivative_order=2) -> Lowered:
     """Lower a GWFL expression over one fem variable to descriptor terms."""
     tree = parse(expr)
@@ -660,11 +725,14 @@ def lower(expr: str, var: FieldInfo, dim: int, fields: dict, add_derivative_orde
         if base != name and s != base:
             raise L.UnsupportedExpression(L.E_UNSUPPORTED,
                                           f"derivatives of data fields ({s}) are not lowered")
-    if not has_test:
-        raise L.UnsupportedExpression(L.E_UNSUPPORTED,
-                                      "potential (order 0) expressions are not lowered")
+    if has_test2 and not has_test:
+        raise L.UnsupportedExpression(L.E_UNSUPPORTED, "Test2 without Test")
     nh = _match_neohookean(tree, var)
-    if nh is not None:
+    nh_pot = None if has_test else _match_neohookean_potential(tree, var)
+    if not has_test and nh_pot is None:
+        return _lower_potential(tree, var, dim, fields)
+    if nh is not None or nh_pot is not None:
+        nh = nh if nh is not None else nh_pot
         if dim != 3 or var.qdim != 3:
             raise L.UnsupportedExpression(L.E_UNSUPPORTED, "neo-Hookean law is 3-D only")
         coefs = []
@@ -685,6 +753,10 @@ def lower(expr: str, var: FieldInfo, dim: int, fields: dict, add_derivative_orde
                                               "a law parameter must be one field times a constant")
             coefs.append(entries[0] if entries else _coef(L.COEF_CONST, 0, 0.0))
         t = _term(L.TERM_NEOHOOKEAN, 1.0, [coefs[0], coefs[1], None])
+        if nh_pot is not None:
+            # the potential, and its first and second derivatives in u (the
+            # PK2 residual and tangent)
+            return Lowered(order2=[t], order1=[t], order0=[t], max_order=0)
         return Lowered(order2=[t], order1=[t], order0=[], max_order=2)
     terms2, terms1 = _lower_linear(tree, var, dim, fields, has_test2)
     if has_test2:

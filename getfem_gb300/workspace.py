@@ -46,6 +46,7 @@ class _Group:
         self.mim = mim
         self.order2 = []
         self.order1 = []
+        self.order0 = []
         self.plans = {}   # key: tuple(form terms) -> plan handle
 
 
@@ -63,6 +64,7 @@ class GaWorkspace:
         self.groups = []
         self._K = None
         self._V = None
+        self._E = None
         self._ext_K = None
         self._ext_V = None
         self._slots = 1  # slot 0 is the variable
@@ -139,6 +141,7 @@ class GaWorkspace:
             self.groups.append(g)
         g.order2 += low.order2
         g.order1 += low.order1
+        g.order0 += low.order0
         return low.max_order
 
     def clear_expressions(self):
@@ -202,22 +205,29 @@ class GaWorkspace:
     def assembly(self, order: int):
         if order not in (0, 1, 2):
             raise ValueError("order must be 0, 1 or 2")
-        if order == 0:
-            raise L.UnsupportedExpression(L.E_UNSUPPORTED, "potential assembly is not lowered")
         lib = L.lib()
         n = None
         results = []
+        pot = 0.0
         for g in self.groups:
-            terms = g.order2 if order == 2 else g.order1
+            terms = (g.order0, g.order1, g.order2)[order]
             if not terms:
                 continue
             h = self._plan(g, terms)
-            self._upload(h, terms, need_u=(order == 1))
+            self._upload(h, terms, need_u=(order <= 1))
+            if order == 0:
+                e = C.c_double()
+                L.check(lib.gfgpu_assemble(h, 0, 0, C.byref(e)))
+                pot += e.value
+                continue
             L.check(lib.gfgpu_assemble(h, order, 0, None))
             L.check(lib.gfgpu_sync(h))
             n = g.var.mf.nb_dof()
             results.append(h)
-        if order == 2:
+        if order == 0:
+            # accumulated like the reference's assembled_potential
+            self._E = pot
+        elif order == 2:
             self._K = self._collect_matrix(results, n)
             if self._ext_K is not None and self._K is not None:
                 self._ext_K += self._K
@@ -256,6 +266,9 @@ class GaWorkspace:
 
     def assembled_vector(self):
         return self._V
+
+    def assembled_potential(self):
+        return self._E
 
     def plans(self):
         """Raw plan handles (for device-side access through the C ABI)."""

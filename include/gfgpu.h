@@ -98,6 +98,8 @@ typedef struct {
 /* Data slots.  Slot 0 is the variable u (n_dof values). */
 #define GFGPU_SLOT_U 0
 #define GFGPU_MAX_SLOTS 8
+/* Pseudo-slot naming the mesh vertex coordinates (gfgpu_potential_gradient). */
+#define GFGPU_SLOT_POINTS (-1)
 
 /* The discretisation: mesh, mesh_fem DOF map and mesh_im.  All arrays are
    host memory and are copied at plan creation. */
@@ -220,6 +222,26 @@ int gfgpu_assemble_host(gfgpu_plan *plan, const double *u, double *vals, double 
 #define GFGPU_RESULT_VALUES 2
 #define GFGPU_RESULT_VECTOR 3
 int gfgpu_copy_result(gfgpu_plan *plan, int32_t which, void *dst);
+
+/* Adjoint of the potential (order-0 assembly of the plan's form, with u and
+   the data fixed) with respect to
+     slot >= 1            a coefficient slot of the form: per-element data
+                          (n = n_elements) or nodal data (n = n_dof / qdim);
+     GFGPU_SLOT_POINTS    the mesh vertex coordinates (n = n_points * dim),
+                          the DOF values held fixed (shape derivative).
+   grad is device memory if on_device, else host memory; waits for the
+   result.  In the reference the coefficient gradient is the order-1
+   assembly of the potential with that datum declared as a variable
+   (ga_workspace::add_fem_variable + assembly(1), GWFL Diff,
+   getfem_generic_assembly_workspace.cc:791); the shape derivative has no
+   counterpart there. */
+int gfgpu_potential_gradient(gfgpu_plan *plan, int32_t slot, double *grad, int64_t n,
+                             int32_t on_device);
+
+/* Replaces the mesh vertex coordinates (n = n_points * dim doubles, device
+   memory if on_device); the DOF map and the CSR pattern are kept.  Waits for
+   the copy. */
+int gfgpu_set_points(gfgpu_plan *plan, const double *points, int64_t n, int32_t on_device);
 
 /* Waits for the plan's stream and reports the device error word
    (GFGPU_E_JACOBIAN / GFGPU_E_NAN) of the last assembly. */

@@ -311,6 +311,23 @@ void neohookean_law(const double *E, double C1, double D1, double det_trans, dou
         }
 }
 
+// Strain energy of the compressible neo-Hookean law
+// (getfem_nonlinear_elasticity.cc:503-527 with compressible = neohookean =
+// true): W = C1 (j1 - 3) + D1 (sqrt|i3| - 1)^2 with C = I + 2E, i1 = tr C,
+// i3 = det C, j1 = i1 |i3|^(-1/3); 1e200 when det(I + Grad_u) <= 0.
+double neohookean_energy(const double *E, double C1, double D1, double det_trans) {
+  if (det_trans <= 0) return 1e200;
+  double C[9];
+  for (int k = 0; k < 9; ++k) C[k] = 2 * E[k];
+  for (int i = 0; i < 3; ++i) C[i * 4] += 1.0;
+  double Ci[9], i3;
+  inv3(C, Ci, i3);
+  const double i1 = C[0] + C[4] + C[8];
+  const double j1 = i1 * std::pow(std::fabs(i3), -1.0 / 3.0);
+  const double r = std::sqrt(std::fabs(i3)) - 1.0;
+  return C1 * (j1 - 3.0) + D1 * (r * r);
+}
+
 // ------------------------------------------------------------ assembly core
 struct Problem {
   gfref_problem p;
@@ -503,6 +520,10 @@ void exec_range(Problem &P, int order, int64_t e0, int64_t e1, Outputs &out) {
           double detF = F[0] * (F[4] * F[8] - F[5] * F[7]) - F[3] * (F[1] * F[8] - F[2] * F[7]) +
                         F[6] * (F[1] * F[5] - F[2] * F[4]);
           double S[9], gs[81];
+          if (order == 0) {
+            t[0] += sc * neohookean_energy(E, C1, D1, detF);
+            continue;
+          }
           neohookean_law(E, C1, D1, detF, S, order == 2 ? gs : nullptr);
           if (order == 1) {
             // (F S)(a,k) Grad_Test_u(a,k)

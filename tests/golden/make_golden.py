@@ -25,6 +25,7 @@ OUT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 NH = "((Id(meshdim)+Grad_u)*(Compressible_Neo_Hookean_PK2(Grad_u,[0.5*mu;D1]))):Grad_Test_u"
+NH_POT = "Compressible_Neo_Hookean_potential(Grad_u,[0.5*mu;D1])"
 
 # name, dim, gt, degree, qdim, im, nx, expr, consts{name: kind}, jitter, u kind
 CASES = [
@@ -60,7 +61,19 @@ CASES = [
      {"lambda": "P0", "mu": "S", "f": "V"}, True, "normal"),
     ("q2hex_neohookean_nodal", 3, "QK", 2, 3, "IM_GAUSS_PARALLELEPIPED(3,5)", 3,
      NH, {"mu": "S", "D1": "C"}, True, "modes"),
+    # potentials: order 0 is the energy, orders 1 and 2 the reference's
+    # symbolic derivatives of it (GWFL Diff)
+    ("q2hex_nh_potential", 3, "QK", 2, 3, "IM_GAUSS_PARALLELEPIPED(3,5)", 3,
+     NH_POT, {"mu": "P0", "D1": "C"}, True, "modes"),
+    ("p2tet_nh_potential", 3, "PK", 2, 3, "IM_TETRAHEDRON(5)", 2,
+     NH_POT, {"mu": "P0", "D1": "C"}, True, "modes"),
+    ("q2hex_kappa_potential", 3, "QK", 2, 1, "IM_GAUSS_PARALLELEPIPED(3,5)", 3,
+     "kappa*Grad_u.Grad_u", {"kappa": "P0"}, False, "normal"),
+    ("p2tri_energy_potential", 2, "PK", 2, 1, "IM_TRIANGLE(4)", 5,
+     "kappa*Grad_u.Grad_u + 2*u*u - f*u", {"kappa": "P0", "f": "V"}, True, "normal"),
 ]
+ORDERS = {"q2hex_nh_potential": "0,1,2", "p2tet_nh_potential": "0,1,2",
+          "q2hex_kappa_potential": "0,1,2", "p2tri_energy_potential": "0,1,2"}
 
 
 def sinusoid_modes(xyz: np.ndarray, qdim: int, rng) -> np.ndarray:
@@ -114,7 +127,8 @@ def make_case(case, seed):
             jit.astype(np.float64).tofile(os.path.join(ind, "jitter.bin"))
         cs = ",".join(f"{k}:{v}" for k, v in consts.items())
         cmd = [DRIVER, f"dim={dim}", f"nx={nx}", f"gt={gt}", f"fem={deg}", f"qdim={qdim}",
-               f"im={im}", f"in={ind}", f"out={outd}", f"expr={expr}", "orders=2,1",
+               f"im={im}", f"in={ind}", f"out={outd}", f"expr={expr}",
+               f"orders={ORDERS.get(name, '2,1')}",
                f"jitter={1 if jit is not None else 0}", f"consts={cs}"]
         subprocess.run(cmd, check=True)
         info = json.load(open(os.path.join(outd, "info.json")))
@@ -135,6 +149,8 @@ def make_case(case, seed):
             K_vals=rd("K_vals.bin"),
             R=rd("R.bin"),
         )
+        if os.path.exists(os.path.join(outd, "E.bin")):
+            rec["E"] = rd("E.bin")
     for k, v in inputs.items():
         rec["in_" + k] = np.asarray(v, dtype=np.float64)
     if jit is not None:

@@ -1,6 +1,7 @@
 """Pins the oracle (oracle/gfref.cc, a CPU restatement of the reference's
 exec loop) against the reference's own assembly of the same expressions:
-sparsity pattern bit-exact, K and R within 1e-12 relative."""
+sparsity pattern bit-exact, K and R within 1e-12 relative, potentials
+(order 0) within 1e-12 relative."""
 import numpy as np
 import pytest
 
@@ -20,6 +21,9 @@ def test_oracle_matches_reference(name):
     assert value_errors(K, Kref).max() <= RTOL
     R = oracle_problem(mesh, mf, mim, grp.order1, slots).vector(nthreads=1)
     assert vec_errors(R, rec["R"]).max() <= RTOL
+    if "E" in rec:
+        E = oracle_problem(mesh, mf, mim, grp.order0, slots).potential(nthreads=1)
+        assert abs(E - float(rec["E"][0])) <= RTOL * abs(float(rec["E"][0]))
 
 
 def test_oracle_threads_agree():
