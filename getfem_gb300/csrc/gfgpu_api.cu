@@ -288,8 +288,17 @@ int gfgpu_plan_create(const gfgpu_space *space, const gfgpu_form *form, void *cu
       return rc;
     }
     if (!P->affine_simplex) {
-      P->kmat = S.dim == 3 && gauss_element_available(S.kind, P->law, S.degree, S.qdim, P->nq);
-      gauss_element_layout(*P);
+      // parallelepiped hexahedra with a scalar isotropic form take the
+      // reference-tensor kernel; the rest the Gauss-point kernel
+      if (S.kind == GFGPU_HEX && P->law == LAW_ISO && affine_hex_form_ok(P->form, S.qdim) &&
+          affine_hex_available(S.degree) && mesh_is_parallelepiped(S.points, S.cvpts, S.n_elements)) {
+        P->affine_hex = true;
+        P->kmat = true;
+        build_affine_hex_tables(*P);
+      } else {
+        P->kmat = S.dim == 3 && gauss_element_available(S.kind, P->law, S.degree, S.qdim, P->nq);
+        gauss_element_layout(*P);
+      }
     }
     P->kpot = gauss_potential_available(S.dim, S.kind, S.degree, S.qdim, P->law);
     if (!P->kmat && !P->kpot) {
@@ -362,6 +371,14 @@ int gfgpu_plan_create(const gfgpu_space *space, const gfgpu_form *form, void *cu
     CHK(up(P->d_adj_ptr, aptr.data(), aptr.size() * sizeof(int32_t)));
     CHK(up(P->d_adj, adj.data(), adj.size() * sizeof(int32_t)));
     CHK(up(P->d_stab, &P->stab, sizeof(SimplexTables)));
+    if (!P->h_aff.empty()) {
+      CHK(dalloc(&P->d_aff, P->h_aff.size()));
+      CHK(up(P->d_aff, P->h_aff.data(), P->h_aff.size() * sizeof(double)));
+    }
+    if (!P->h_tri.empty()) {
+      CHK(dalloc(&P->d_tri, P->h_tri.size()));
+      CHK(up(P->d_tri, P->h_tri.data(), P->h_tri.size() * sizeof(int32_t)));
+    }
     CHK(dalloc(&P->d_padj_ptr, pptr.size()));
     CHK(dalloc(&P->d_padj, padj.size()));
     CHK(up(P->d_padj_ptr, pptr.data(), pptr.size() * sizeof(int32_t)));
@@ -400,6 +417,8 @@ void gfgpu_plan_destroy(gfgpu_plan *P) {
   dfree(P->d_hgrad);
   dfree(P->d_ggrad);
   dfree(P->d_hw);
+  dfree(P->d_tri);
+  dfree(P->d_aff);
   dfree(P->d_padj_ptr);
   dfree(P->d_padj);
   dfree(P->d_epart);
@@ -514,7 +533,10 @@ int gfgpu_assemble(gfgpu_plan *P, int32_t order, int32_t flags, double *potentia
   GF_CUDA(cudaMemsetAsync(P->d_err, 0, sizeof(int), P->stream));
   if (prof) GF_CUDA(cudaEventRecord(P->ev[0], P->stream));
   if (P->affine_simplex) GF_CUDA(launch_simplex_element_pass(*P, want_R));
-  else GF_CUDA(launch_hex_element_pass(*P));
+  // the Gauss kernel skips the tangent and K_e when only the vector is
+  // wanted and the pattern (which reads the K_e thresholds) exists
+  else if (P->affine_hex) GF_CUDA(launch_affine_hex_pass(*P, want_K || P->nnz < 0));
+  else GF_CUDA(launch_hex_element_pass(*P, want_K || P->nnz < 0));
   if (prof) GF_CUDA(cudaEventRecord(P->ev[1], P->stream));
   if ((want_K && (P->nnz < 0 || (flags & GFGPU_REBUILD_PATTERN))) || P->nnz < 0) {
     // the pattern is built at the first order-2 assembly; an order-1

@@ -1,0 +1,277 @@
+// Element kernel for scalar FEM_QK(3,K) on parallelepiped hexahedra (GT_QK(3,1)
+// with constant Jacobian), FP64: the high-order case (FEM_QK(3,4),
+// IM_GAUSS_PARALLELEPIPED(3,9): 125 basis functions, 125 Gauss points).
+//
+// When K = sum_v x_v grad(phi_geo_v) is the same at every Gauss point, the
+// reference's per-point contraction (getfem_generic_assembly_compile_and_exec.cc:
+// 8750-8869; t(i,j) += c J w_q grad phi_i . grad phi_j with the real gradients
+// B grad_ref phi, getfem_fem.cc:160-200) factors into reference tensors:
+//   K_e[i,j] = c |J| sum_{m<=n} M'_mn G_mn[i,j],   M = B^T B,
+//   G_mm[i,j] = sum_q w_q dm phi_i dm phi_j,
+//   G_mn[i,j] = sum_q w_q (dm phi_i dn phi_j + dn phi_i dm phi_j)  (m < n),
+// plus c_m |J| Mhat[i,j] (Mhat = sum_q w_q phi_i phi_j) for a mass term and
+// c_f |J| Mhat f_e for a load.  The tables are summed on the host in long
+// double from the reference-tabulated gradients at the Gauss points (the same
+// values the reference's fem_precomp holds), so every element costs 6 FMAs per
+// entry instead of 3 x 125.
+//
+// One CTA per element.  K_e is symmetric: each thread owns upper-triangle
+// entries (tables read coalesced from L2) and writes both (r,c) and (c,r).
+// V_e = K_e u_e + load is then formed by one warp per row from the rows just
+// written (or, for a vector-only pass, from the tables directly).
+#include <cmath>
+
+#include "host/refelem.h"
+#include "k_common.cuh"
+#include "plan.h"
+
+namespace gfgpu {
+
+namespace {
+
+constexpr int kAffThreads = 256;
+constexpr int kAffTables = 7;  // G_00, G_11, G_22, G_01, G_02, G_12, Mhat
+
+template <int NB, bool WANT_K>
+__global__ void __launch_bounds__(kAffThreads) affine_hex_kernel(
+    int64_t E, const double *__restrict__ pts, const int32_t *__restrict__ cv,
+    const int32_t *__restrict__ enode, const double *__restrict__ tabs,
+    const int32_t *__restrict__ tri, const double *__restrict__ ggrad0, KeLayout L,
+    gfgpu_form form, SlotPtrs slots, double *__restrict__ out, int *__restrict__ err) {
+  constexpr int NT = NB * (NB + 1) / 2;
+  constexpr int NN = NB * NB;
+  __shared__ double cp[kAffTables];  // coefficients of the tables
+  __shared__ double cf;              // load factor c_f |J|
+  __shared__ double us[NB], fs[NB];
+  __shared__ unsigned long long smax;
+  const int64_t e = blockIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const double *u = slots.p[GFGPU_SLOT_U];
+  int src_slot = -1;
+  for (int t = 0; t < form.n_terms; ++t)
+    if (form.terms[t].kind == GFGPU_TERM_SOURCE) src_slot = form.terms[t].field_slot;
+  for (int j = tid; j < NB; j += kAffThreads) {
+    const int32_t n = enode[e * NB + j];
+    us[j] = u ? u[n] : 0.0;
+    fs[j] = src_slot >= 0 ? slots.p[src_slot][n] : 0.0;
+  }
+  if (tid == 0) {
+    smax = 0ull;
+    // K(d,m) = sum_v x_v[d] dphi_v/dxi_m (constant on a parallelepiped)
+    double K[9];
+    for (int d = 0; d < 3; ++d)
+      for (int m = 0; m < 3; ++m) {
+        double s = 0.0;
+        for (int v = 0; v < 8; ++v) s += pts[int64_t(cv[e * 8 + v]) * 3 + d] * ggrad0[v * 3 + m];
+        K[d + 3 * m] = s;
+      }
+    const double a0 = K[4] * K[8] - K[5] * K[7];
+    const double a1 = K[5] * K[6] - K[3] * K[8];
+    const double a2 = K[3] * K[7] - K[4] * K[6];
+    const double det = K[0] * a0 + K[1] * a1 + K[2] * a2;
+    if (det == 0.0) set_err(err, ERR_JACOBIAN);
+    double B[9];  // B(d,m) = cofactor(d,m) / det = K^{-T}(d,m)
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+        B[i + 3 * j] = (K[i1 + 3 * j1] * K[i2 + 3 * j2] - K[i1 + 3 * j2] * K[i2 + 3 * j1]) / det;
+      }
+    const double J = det == 0.0 ? 0.0 : fabs(det);
+    double M[9];  // M = B^T B
+    for (int m = 0; m < 3; ++m)
+      for (int n = 0; n < 3; ++n) {
+        double s = 0.0;
+        for (int d = 0; d < 3; ++d) s += B[d + 3 * m] * B[d + 3 * n];
+        M[m + 3 * n] = s;
+      }
+    double c1 = 0.0, cm = 0.0, csrc = 0.0;
+    for (int t = 0; t < form.n_terms; ++t) {
+      const gfgpu_term &T = form.terms[t];
+      auto val = [&](const gfgpu_coef &c) {
+        if (c.kind == GFGPU_COEF_CONST) return c.value;
+        if (c.kind == GFGPU_COEF_ELEMENT) return c.value * slots.p[c.slot][e];
+        return 0.0;
+      };
+      if (T.kind == GFGPU_TERM_GRADGRAD) c1 += T.scale * val(T.c[1]);
+      else if (T.kind == GFGPU_TERM_MASS) cm += T.scale * val(T.c[0]);
+      else if (T.kind == GFGPU_TERM_SOURCE)
+        csrc += T.scale * (T.c[0].kind == GFGPU_COEF_NONE ? 1.0 : val(T.c[0]));
+    }
+    const double cJ = c1 * J;
+    cp[0] = cJ * M[0], cp[1] = cJ * M[4], cp[2] = cJ * M[8];
+    cp[3] = cJ * M[3], cp[4] = cJ * M[6], cp[5] = cJ * M[7];
+    cp[6] = cm * J;
+    cf = csrc * J;
+  }
+  __syncthreads();
+  double c[kAffTables];
+#pragma unroll
+  for (int p = 0; p < kAffTables; ++p) c[p] = cp[p];
+  double *o = out + e * L.stride;
+  if constexpr (WANT_K) {
+    unsigned long long mx = 0ull;
+    for (int ent = tid; ent < NT; ent += kAffThreads) {
+      const int rc = tri[ent];
+      const int r = rc >> 16, col = rc & 0xffff;
+      const int idx = r * NB + col;
+      double v = c[0] * tabs[idx];
+#pragma unroll
+      for (int p = 1; p < kAffTables; ++p) v = fma(c[p], tabs[p * NN + idx], v);
+      o[r * L.rowstride + col] = v;
+      if (r != col) o[col * L.rowstride + r] = v;
+      const unsigned long long bits =
+          static_cast<unsigned long long>(__double_as_longlong(v)) & 0x7fffffffffffffffull;
+      mx = bits > mx ? bits : mx;
+    }
+    atomicMax(&smax, mx);
+    __syncthreads();  // the rows of K_e are visible to the block
+  }
+  // V_e[r] = sum_c K_e[r,c] u_c + c_f sum_c Mhat[r,c] f_c, one warp per row
+  for (int r = wid; r < NB; r += kAffThreads / 32) {
+    double s = 0.0, sf = 0.0;
+    for (int col = lane; col < NB; col += 32) {
+      double k;
+      if constexpr (WANT_K) {
+        k = o[r * L.rowstride + col];
+      } else {
+        const int idx = r * NB + col;
+        k = c[0] * tabs[idx];
+#pragma unroll
+        for (int p = 1; p < kAffTables; ++p) k = fma(c[p], tabs[p * NN + idx], k);
+      }
+      s = fma(k, us[col], s);
+      sf = fma(tabs[6 * NN + r * NB + col], fs[col], sf);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      s += __shfl_xor_sync(0xffffffffu, s, off);
+      sf += __shfl_xor_sync(0xffffffffu, sf, off);
+    }
+    if (lane == 0) {
+      const double v = fma(cf, sf, s);
+      if (!isfinite(v)) set_err(err, ERR_NAN);
+      o[L.off_vec + r] = v;
+    }
+  }
+  if constexpr (WANT_K) {
+    if (tid == 0) {
+      const double m = __longlong_as_double(static_cast<long long>(smax));
+      if (!isfinite(m)) set_err(err, ERR_NAN);
+      o[L.off_thr] = m * 1e-14;
+    }
+  }
+}
+
+}  // namespace
+
+// The forms of this kernel: scalar GRADGRAD (c1), MASS and SOURCE terms with
+// constant or per-element coefficients.
+bool affine_hex_form_ok(const gfgpu_form &f, int qdim) {
+  if (qdim != 1) return false;
+  for (int t = 0; t < f.n_terms; ++t) {
+    const gfgpu_term &T = f.terms[t];
+    if (T.kind != GFGPU_TERM_GRADGRAD && T.kind != GFGPU_TERM_MASS && T.kind != GFGPU_TERM_SOURCE)
+      return false;
+    for (int k = 0; k < 3; ++k)
+      if (T.c[k].kind == GFGPU_COEF_NODAL) return false;
+  }
+  return true;
+}
+
+// True when every element of the mesh is a parallelepiped: x_v = x_0 +
+// sum_d l_d(v) (x_{e_d} - x_0) for the GT_QK(3,1) vertex lattice l(v).
+bool mesh_is_parallelepiped(const double *pts, const int64_t *cv, int64_t E) {
+  for (int64_t e = 0; e < E; ++e) {
+    const int64_t *c = cv + e * 8;
+    const double *x0 = pts + c[0] * 3;
+    double ed[3][3], scale = 0.0;
+    for (int d = 0; d < 3; ++d)
+      for (int k = 0; k < 3; ++k) {
+        ed[d][k] = pts[c[1 << d] * 3 + k] - x0[k];
+        scale = std::max(scale, std::fabs(ed[d][k]));
+      }
+    for (int v = 0; v < 8; ++v)
+      for (int k = 0; k < 3; ++k) {
+        double x = x0[k];
+        for (int d = 0; d < 3; ++d)
+          if (v & (1 << d)) x += ed[d][k];
+        if (std::fabs(x - pts[c[v] * 3 + k]) > 1e-13 * scale) return false;
+      }
+  }
+  return true;
+}
+
+// Reference tensors (long double sums over the Gauss points of the
+// reference-tabulated values) and the upper-triangle entry list.
+void build_affine_hex_tables(Plan &P) {
+  const int nb = P.nb, nq = P.nq;
+  const int pm[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+  P.h_aff.assign(size_t(kAffTables) * nb * nb, 0.0);
+  std::vector<long double> acc(size_t(nb) * nb);
+  for (int p = 0; p < kAffTables; ++p) {
+    std::fill(acc.begin(), acc.end(), 0.0L);
+    for (int q = 0; q < nq; ++q) {
+      const long double w = P.h_w[q];
+      const double *g = &P.h_grad[size_t(q) * nb * 3];
+      const double *v = &P.h_val[size_t(q) * nb];
+      for (int i = 0; i < nb; ++i)
+        for (int j = 0; j < nb; ++j) {
+          long double t;
+          if (p == 6) {
+            t = (long double)v[i] * v[j];
+          } else {
+            const int m = pm[p][0], n = pm[p][1];
+            t = (long double)g[i * 3 + m] * g[j * 3 + n];
+            if (m != n) t += (long double)g[i * 3 + n] * g[j * 3 + m];
+          }
+          acc[size_t(i) * nb + j] += w * t;
+        }
+    }
+    for (size_t k = 0; k < acc.size(); ++k) P.h_aff[size_t(p) * nb * nb + k] = double(acc[k]);
+  }
+  P.h_tri.clear();
+  for (int r = 0; r < nb; ++r)
+    for (int c = r; c < nb; ++c) P.h_tri.push_back((r << 16) | c);
+  const int s = nb;
+  P.lay.nb = nb;
+  P.lay.qd = 1;
+  P.lay.s = s;
+  P.lay.rowstride = (s + 3) & ~3;
+  P.lay.off_vec = s * P.lay.rowstride;
+  P.lay.off_thr = P.lay.off_vec + P.lay.rowstride;
+  P.lay.stride = P.lay.off_thr + 4;
+  P.lay.linear = true;
+}
+
+bool affine_hex_available(int degree) { return degree == 1 || degree == 2 || degree == 3 || degree == 4; }
+
+cudaError_t launch_affine_hex_pass(Plan &P, bool want_K) {
+  if (P.n_elements == 0) return cudaSuccess;
+  SlotPtrs sp;
+  for (int i = 0; i < GFGPU_MAX_SLOTS; ++i) sp.p[i] = P.slot_ptr[i];
+  if (P.slot_n[GFGPU_SLOT_U] != P.n_dof) sp.p[GFGPU_SLOT_U] = nullptr;
+  const unsigned grid = unsigned(P.n_elements);
+#define AFF(NB)                                                                                \
+  do {                                                                                         \
+    if (want_K)                                                                                \
+      affine_hex_kernel<NB, true><<<grid, kAffThreads, 0, P.stream>>>(                          \
+          P.n_elements, P.d_points, P.d_cv, P.d_enode, P.d_aff, P.d_tri, P.d_ggrad, P.lay,     \
+          P.form, sp, P.d_elem, P.d_err);                                                      \
+    else                                                                                       \
+      affine_hex_kernel<NB, false><<<grid, kAffThreads, 0, P.stream>>>(                         \
+          P.n_elements, P.d_points, P.d_cv, P.d_enode, P.d_aff, P.d_tri, P.d_ggrad, P.lay,     \
+          P.form, sp, P.d_elem, P.d_err);                                                      \
+  } while (0)
+  switch (P.nb) {
+    case 8: AFF(8); break;
+    case 27: AFF(27); break;
+    case 64: AFF(64); break;
+    case 125: AFF(125); break;
+    default: return cudaErrorInvalidValue;
+  }
+#undef AFF
+  P.launches++;
+  return cudaGetLastError();
+}
+
+}  // namespace gfgpu

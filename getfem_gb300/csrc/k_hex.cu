@@ -112,20 +112,18 @@ struct HexSmem {
                        o_r = o_m + n_m, o_u = o_r + n_r, o_x = o_u + n_u, o_law = o_x + n_x,
                        o_W = o_law + n_law, total = o_W + n_W;
   static constexpr size_t bytes = size_t(total) * 8;
-  // element-matrix ownership in phase B: RG row groups of QD * S threads
-  static constexpr int RG0 = kHexThreads / (QD * S);
-  static constexpr int RG = RG0 < 1 ? 1 : (RG0 > NB ? NB : RG0);
-  static constexpr int NI = (NB + RG - 1) / RG;
-  static_assert(QD * S * RG <= kHexThreads, "element too large for one CTA");
+  // phase B: the upper triangle of K_e (r <= c), entries dealt round-robin
+  static constexpr int NT = S * (S + 1) / 2;
+  static constexpr int NE = (NT + kHexThreads - 1) / kHexThreads;
 };
 
-template <int QD, int NB, int NBG, int NQ, int LAW>
+template <int QD, int NB, int NBG, int NQ, int LAW, bool WANT_K>
 __global__ void __launch_bounds__(kHexThreads) hex_element_kernel(
     int64_t E, const double *__restrict__ pts, const int32_t *__restrict__ cv,
     const int32_t *__restrict__ enode, const double *__restrict__ hval,
     const double *__restrict__ hgrad, const double *__restrict__ ggrad,
-    const double *__restrict__ hw, KeLayout L, gfgpu_form form, SlotPtrs slots,
-    double *__restrict__ out, int *__restrict__ err) {
+    const double *__restrict__ hw, const int32_t *__restrict__ tri, KeLayout L,
+    gfgpu_form form, SlotPtrs slots, double *__restrict__ out, int *__restrict__ err) {
   using M = HexSmem<QD, NB, NBG, NQ, LAW>;
   constexpr int S = M::S, NA = M::NA;
   extern __shared__ __align__(16) double sm[];
@@ -307,7 +305,7 @@ __global__ void __launch_bounds__(kHexThreads) hex_element_kernel(
     }
   }
   __syncthreads();
-  if constexpr (LAW == LAW_NH) {
+  if constexpr (LAW == LAW_NH && WANT_K) {
     // ---------------------------------------------------------------- A2
     for (int z = tid; z < NQ * 81; z += kHexThreads) {
       const int q = z / 81, r = z % 81;
@@ -332,59 +330,77 @@ __global__ void __launch_bounds__(kHexThreads) hex_element_kernel(
     }
     __syncthreads();
   }
-  // ---------------------------------------------------------------- B
-  // thread -> (row group rg, component a, column c); it owns the entries
-  // (i*QD + a, c) for i = rg, rg + RG, ...
-  constexpr int NI = M::NI, RG = M::RG;
-  const bool active = tid < QD * S * RG;
-  const int c = tid % S, a = (tid / S) % QD, rg = tid / (QD * S);
-  const bool diag = c % QD == a;
-  double acc[NI];
+  double *o = out + e * L.stride;
+  if constexpr (WANT_K) {
+    // -------------------------------------------------------------- B
+    // K_e is symmetric (isotropic tangent; hyperelastic tangent): each thread
+    // owns upper-triangle entries (r, c), r = i*QD + a <= c = j*QD + b, and
+    // accumulates sum_k g_ik Z[(a,k), c] with Z = A g_j per Gauss point.
+    constexpr int NE = M::NE;
+    int goff[NE], zoff[NE];
+    bool own[NE], dg[NE];
 #pragma unroll
-  for (int k = 0; k < NI; ++k) acc[k] = 0.0;
-  for (int q = 0; q < NQ; ++q) {
-    for (int z = tid; z < NA * S; z += kHexThreads) {
-      const int ak = z / S, cz = z % S, j = cz / QD, b = cz % QD;
-      const double *A = Aq + (q * NA + ak) * NA + b * 3;
-      const double *g = gq + (q * NB + j) * 3;
-      W[z] = fma(A[0], g[0], fma(A[1], g[1], A[2] * g[2]));
+    for (int k = 0; k < NE; ++k) {
+      const int ent = tid + kHexThreads * k;
+      own[k] = ent < M::NT;
+      const int rc = own[k] ? tri[ent] : 0;
+      const int r = rc >> 16, c = rc & 0xffff;
+      goff[k] = (r / QD) * 3;
+      zoff[k] = (r % QD) * 3 * S + c;
+      dg[k] = (c % QD) == (r % QD);  // mass couples equal components
     }
-    __syncthreads();
-    if (active) {
-      const double *Zc = W + a * 3 * S + c;
-      const double z0 = Zc[0], z1 = Zc[S], z2 = Zc[2 * S];
-      const double mj = diag ? mq[q] * hval[q * NB + c / QD] : 0.0;
-      const double *gi = gq + q * NB * 3;
-      const double *phi = hval + q * NB;
+    double acc[NE];
 #pragma unroll
-      for (int k = 0; k < NI; ++k) {
-        const int i = rg + RG * k;
-        if (NI * RG == NB || i < NB) {
-          double t = fma(gi[3 * i], z0, acc[k]);
-          t = fma(gi[3 * i + 1], z1, t);
-          t = fma(gi[3 * i + 2], z2, t);
-          acc[k] = fma(mj, phi[i], t);
+    for (int k = 0; k < NE; ++k) acc[k] = 0.0;
+    for (int q = 0; q < NQ; ++q) {
+      for (int z = tid; z < NA * S; z += kHexThreads) {
+        const int ak = z / S, cz = z % S, j = cz / QD, b = cz % QD;
+        const double *A = Aq + (q * NA + ak) * NA + b * 3;
+        const double *gz = gq + (q * NB + j) * 3;
+        W[z] = fma(A[0], gz[0], fma(A[1], gz[1], A[2] * gz[2]));
+      }
+      __syncthreads();
+      const double *gi = gq + q * NB * 3;
+      const double mqq = mq[q];
+#pragma unroll
+      for (int k = 0; k < NE; ++k) {
+        if (own[k]) {
+          const double *g = gi + goff[k];
+          const double *Z = W + zoff[k];
+          double t = fma(g[0], Z[0], acc[k]);
+          t = fma(g[1], Z[S], t);
+          acc[k] = fma(g[2], Z[2 * S], t);
         }
       }
-    }
-    __syncthreads();
-  }
-  // ---------------------------------------------------------------- outputs
-  double *o = out + e * L.stride;
-  unsigned long long mx = 0ull;
-  if (active) {
+      if (mqq != 0.0) {
+        const double *phi = hval + q * NB;
 #pragma unroll
-    for (int k = 0; k < NI; ++k) {
-      const int i = rg + RG * k;
-      if (NI * RG == NB || i < NB) {
-        o[(i * QD + a) * L.rowstride + c] = acc[k];
+        for (int k = 0; k < NE; ++k) {
+          if (own[k] && dg[k]) {
+            const int ent = tid + kHexThreads * k;
+            const int rc = tri[ent];
+            acc[k] = fma(mqq * phi[(rc >> 16) / QD], phi[(rc & 0xffff) / QD], acc[k]);
+          }
+        }
+      }
+      __syncthreads();
+    }
+    // ------------------------------------------------------------ outputs
+    unsigned long long mx = 0ull;
+#pragma unroll
+    for (int k = 0; k < NE; ++k) {
+      if (own[k]) {
+        const int rc = tri[tid + kHexThreads * k];
+        const int r = rc >> 16, c = rc & 0xffff;
+        o[r * L.rowstride + c] = acc[k];
+        if (r != c) o[c * L.rowstride + r] = acc[k];
         const unsigned long long bits =
             static_cast<unsigned long long>(__double_as_longlong(acc[k])) & 0x7fffffffffffffffull;
         mx = bits > mx ? bits : mx;
       }
     }
+    atomicMax(&smax, mx);
   }
-  atomicMax(&smax, mx);
   // ---------------------------------------------------------------- C
   // R_e(i,a) = sum_q wJ_q t_q(i,a), t_q as the reference's exec loop forms
   // it (term by term, products and sums in its order)
@@ -425,24 +441,27 @@ __global__ void __launch_bounds__(kHexThreads) hex_element_kernel(
     if (!isfinite(s)) set_err(err, ERR_NAN);
     o[L.off_vec + r] = s;
   }
-  __syncthreads();
-  if (tid == 0) {
-    const double m = __longlong_as_double(static_cast<long long>(smax));
-    if (!isfinite(m)) set_err(err, ERR_NAN);
-    o[L.off_thr] = m * 1e-14;
+  if constexpr (WANT_K) {
+    __syncthreads();
+    if (tid == 0) {
+      const double m = __longlong_as_double(static_cast<long long>(smax));
+      if (!isfinite(m)) set_err(err, ERR_NAN);
+      o[L.off_thr] = m * 1e-14;
+    }
   }
 }
 
 template <int QD, int NB, int NBG, int NQ, int LAW>
-cudaError_t launch_hex_t(Plan &P, const SlotPtrs &sp) {
+cudaError_t launch_hex_t(Plan &P, const SlotPtrs &sp, bool want_K) {
   using M = HexSmem<QD, NB, NBG, NQ, LAW>;
-  auto kern = hex_element_kernel<QD, NB, NBG, NQ, LAW>;
+  auto kern = want_K ? hex_element_kernel<QD, NB, NBG, NQ, LAW, true>
+                     : hex_element_kernel<QD, NB, NBG, NQ, LAW, false>;
   cudaError_t ce = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         int(M::bytes));
   if (ce != cudaSuccess) return ce;
   kern<<<unsigned(P.n_elements), kHexThreads, M::bytes, P.stream>>>(
-      P.n_elements, P.d_points, P.d_cv, P.d_enode, P.d_hval, P.d_hgrad, P.d_ggrad, P.d_hw, P.lay,
-      P.form, sp, P.d_elem, P.d_err);
+      P.n_elements, P.d_points, P.d_cv, P.d_enode, P.d_hval, P.d_hgrad, P.d_ggrad, P.d_hw,
+      P.d_tri, P.lay, P.form, sp, P.d_elem, P.d_err);
   return cudaGetLastError();
 }
 
@@ -470,9 +489,13 @@ void gauss_element_layout(Plan &P) {
   P.lay.off_thr = P.lay.off_vec + P.lay.rowstride;
   P.lay.stride = P.lay.off_thr + 4;
   P.lay.linear = P.law != LAW_NH;
+  // upper-triangle entries (r << 16 | c), row-major
+  P.h_tri.clear();
+  for (int r = 0; r < s; ++r)
+    for (int c = r; c < s; ++c) P.h_tri.push_back((r << 16) | c);
 }
 
-cudaError_t launch_hex_element_pass(Plan &P) {
+cudaError_t launch_hex_element_pass(Plan &P, bool want_K) {
   if (P.n_elements == 0) return cudaSuccess;
   SlotPtrs sp;
   for (int i = 0; i < GFGPU_MAX_SLOTS; ++i) sp.p[i] = P.slot_ptr[i];
@@ -482,21 +505,21 @@ cudaError_t launch_hex_element_pass(Plan &P) {
   const int k = P.degree, q = P.qdim, nq = P.nq;
   cudaError_t ce = cudaErrorInvalidValue;
   if (P.kind != HEX) {
-    if (P.law == LAW_NH && k == 2 && nq == 15) ce = launch_hex_t<3, 10, 4, 15, LAW_NH>(P, sp);
-    else if (P.law == LAW_NH && k == 1 && nq == 4) ce = launch_hex_t<3, 4, 4, 4, LAW_NH>(P, sp);
-    else if (P.law == LAW_NH && k == 1 && nq == 15) ce = launch_hex_t<3, 4, 4, 15, LAW_NH>(P, sp);
+    if (P.law == LAW_NH && k == 2 && nq == 15) ce = launch_hex_t<3, 10, 4, 15, LAW_NH>(P, sp, want_K);
+    else if (P.law == LAW_NH && k == 1 && nq == 4) ce = launch_hex_t<3, 4, 4, 4, LAW_NH>(P, sp, want_K);
+    else if (P.law == LAW_NH && k == 1 && nq == 15) ce = launch_hex_t<3, 4, 4, 15, LAW_NH>(P, sp, want_K);
   } else if (P.law == LAW_NH) {
-    if (k == 2 && nq == 27) ce = launch_hex_t<3, 27, 8, 27, LAW_NH>(P, sp);
-    else if (k == 1 && nq == 8) ce = launch_hex_t<3, 8, 8, 8, LAW_NH>(P, sp);
-    else if (k == 1 && nq == 27) ce = launch_hex_t<3, 8, 8, 27, LAW_NH>(P, sp);
+    if (k == 2 && nq == 27) ce = launch_hex_t<3, 27, 8, 27, LAW_NH>(P, sp, want_K);
+    else if (k == 1 && nq == 8) ce = launch_hex_t<3, 8, 8, 8, LAW_NH>(P, sp, want_K);
+    else if (k == 1 && nq == 27) ce = launch_hex_t<3, 8, 8, 27, LAW_NH>(P, sp, want_K);
   } else if (q == 1) {
-    if (k == 1 && nq == 8) ce = launch_hex_t<1, 8, 8, 8, LAW_ISO>(P, sp);
-    else if (k == 1 && nq == 27) ce = launch_hex_t<1, 8, 8, 27, LAW_ISO>(P, sp);
-    else if (k == 2 && nq == 27) ce = launch_hex_t<1, 27, 8, 27, LAW_ISO>(P, sp);
+    if (k == 1 && nq == 8) ce = launch_hex_t<1, 8, 8, 8, LAW_ISO>(P, sp, want_K);
+    else if (k == 1 && nq == 27) ce = launch_hex_t<1, 8, 8, 27, LAW_ISO>(P, sp, want_K);
+    else if (k == 2 && nq == 27) ce = launch_hex_t<1, 27, 8, 27, LAW_ISO>(P, sp, want_K);
   } else if (q == 3) {
-    if (k == 1 && nq == 8) ce = launch_hex_t<3, 8, 8, 8, LAW_ISO>(P, sp);
-    else if (k == 1 && nq == 27) ce = launch_hex_t<3, 8, 8, 27, LAW_ISO>(P, sp);
-    else if (k == 2 && nq == 27) ce = launch_hex_t<3, 27, 8, 27, LAW_ISO>(P, sp);
+    if (k == 1 && nq == 8) ce = launch_hex_t<3, 8, 8, 8, LAW_ISO>(P, sp, want_K);
+    else if (k == 1 && nq == 27) ce = launch_hex_t<3, 8, 8, 27, LAW_ISO>(P, sp, want_K);
+    else if (k == 2 && nq == 27) ce = launch_hex_t<3, 27, 8, 27, LAW_ISO>(P, sp, want_K);
   }
   if (ce == cudaSuccess) P.launches++;
   return ce;

@@ -97,6 +97,12 @@ struct Plan {
   // nq x nb x dim, geometric gradients nq x nbg x dim, weights nq
   std::vector<double> h_val, h_grad, h_ggrad, h_w;
   double *d_hval = nullptr, *d_hgrad = nullptr, *d_ggrad = nullptr, *d_hw = nullptr;
+  std::vector<int32_t> h_tri;  // upper-triangle entries of K_e (Gauss kernel)
+  int32_t *d_tri = nullptr;
+  // parallelepiped hexahedra: reference tensors (7 x nb x nb)
+  bool affine_hex = false;
+  std::vector<double> h_aff;
+  double *d_aff = nullptr;
   bool kmat = true;        // an element-matrix kernel exists (orders 1 and 2)
   bool kpot = false;       // the Gauss-point potential kernel exists (order 0)
   // point -> (element, vertex) adjacency, codes e * nbg + v sorted by e
@@ -142,10 +148,16 @@ int build_gauss_tables(Plan &P, std::string &err);
 cudaError_t launch_potential(Plan &P, double *d_out);
 cudaError_t launch_coef_gradient(Plan &P, int slot, bool nodal, double *d_out);
 cudaError_t launch_shape_gradient(Plan &P, double *d_out);
+// parallelepiped hexahedra (k_affine_hex.cu)
+bool affine_hex_form_ok(const gfgpu_form &f, int qdim);
+bool mesh_is_parallelepiped(const double *pts, const int64_t *cv, int64_t E);
+bool affine_hex_available(int degree);
+void build_affine_hex_tables(Plan &P);
+cudaError_t launch_affine_hex_pass(Plan &P, bool want_K);
 // Gauss-point element kernels (k_hex.cu)
 bool gauss_element_available(int kind, int law, int degree, int qdim, int nq);
 void gauss_element_layout(Plan &P);
-cudaError_t launch_hex_element_pass(Plan &P);
+cudaError_t launch_hex_element_pass(Plan &P, bool want_K);
 cudaError_t launch_simplex_vector_pass(int dim, int degree, int qdim, int64_t E,
                                        const double *pts, const int32_t *cv, const int32_t *enode,
                                        const SimplexTables *tab, const gfgpu_form &form,

@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 NH = "((Id(meshdim)+Grad_u)*(Compressible_Neo_Hookean_PK2(Grad_u,[0.5*mu;D1]))):Grad_Test_u"
 
 
-HEX_CASES = ["q2hex_neohookean", "q2hex_neohookean_nodal", "q1hex_nodal_kappa",
+HEX_CASES = ["q2hex_neohookean", "q2hex_neohookean_nodal", "q1hex_nodal_kappa", "q4hex_laplace",
              "q2hex_elastic_nodal"]
 
 
