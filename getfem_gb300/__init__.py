@@ -9,6 +9,7 @@ from ._lib import GfgpuError, UnsupportedExpression  # noqa: F401
 from .mesh import Mesh, MeshFem, MeshIm  # noqa: F401
 from .workspace import GaWorkspace  # noqa: F401
 from .adjoint import Potential  # noqa: F401
+from . import solvers  # noqa: F401
 
 __all__ = ["GaWorkspace", "Mesh", "MeshFem", "MeshIm", "Potential", "GfgpuError",
            "UnsupportedExpression"]

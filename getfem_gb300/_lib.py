@@ -112,6 +112,17 @@ _PROTOS = {
     "gfgpu_potential_gradient": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64,
                                            C.c_int32]),
     "gfgpu_set_points": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32]),
+    "gfgpu_dirichlet_eliminate": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
+                                            C.c_void_p]),
+    "gfgpu_batch_create": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p)]),
+    "gfgpu_batch_assemble": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "gfgpu_batch_tune": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int32),
+                                   C.POINTER(C.c_int32)]),
+    "gfgpu_batch_sync": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "gfgpu_batch_elements": (C.c_int64, [C.c_void_p]),
+    "gfgpu_batch_destroy": (None, [C.c_void_p]),
+    "gfgpu_cg": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int64, C.c_int32,
+                           C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
 }
 
 

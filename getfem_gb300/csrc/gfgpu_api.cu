@@ -20,6 +20,29 @@ using namespace gfgpu;
 
 struct gfgpu_plan_s : public Plan {};
 
+namespace gfgpu {
+cudaError_t batch_element_pass_attr(size_t smem);
+cudaError_t batch_gather_attr(size_t smem);
+}
+
+// A batch of affine-simplex plans launched together.
+struct gfgpu_batch_s {
+  std::vector<gfgpu_plan *> plans;
+  BatchItem *d_items = nullptr;     // element pass: all items
+  int64_t *d_tile0 = nullptr;       // tile offsets (nitems + 1)
+  int nitems = 0;
+  int64_t ntiles = 0, elements = 0;
+  size_t ep_smem = 0;
+  // gather: items grouped by component count
+  BatchItem *d_gitems[4] = {};
+  int64_t *d_node0[4] = {};
+  int gn[4] = {};
+  int64_t gnodes[4] = {};
+  size_t gwarp[4] = {};
+  int grid_ep = 0, grid_ga = 0;
+  int *d_err = nullptr;
+};
+
 namespace {
 
 #define GF_CUDA(call)                                                          \
@@ -630,6 +653,190 @@ int gfgpu_set_points(gfgpu_plan *P, const double *points, int64_t n, int32_t on_
                           P->stream));
   GF_CUDA(cudaStreamSynchronize(P->stream));
   return GFGPU_OK;
+}
+
+int gfgpu_batch_create(gfgpu_plan *const *plans, int32_t n, gfgpu_batch **out) {
+  if (!plans || n < 1 || !out) {
+    set_last_error("gfgpu_batch_create: bad arguments");
+    return GFGPU_E_INVALID;
+  }
+  *out = nullptr;
+  gfgpu_batch *B = new (std::nothrow) gfgpu_batch();
+  if (!B) return GFGPU_E_NOMEM;
+  auto fail = [&](int rc, const std::string &msg) {
+    if (!msg.empty()) set_last_error(msg);
+    gfgpu_batch_destroy(B);
+    return rc;
+  };
+  std::vector<BatchItem> items;
+  std::vector<int64_t> tile0(1, 0);
+  std::vector<BatchItem> gitems[4];
+  std::vector<int64_t> node0[4];
+  for (int q = 0; q < 4; ++q) node0[q].push_back(0);
+  int rc;
+  if ((rc = dalloc(&B->d_err, 1))) return fail(rc, "");
+  for (int i = 0; i < n; ++i) {
+    Plan &P = *plans[i];
+    if (!P.affine_simplex)
+      return fail(GFGPU_E_UNSUPPORTED, "gfgpu_batch_create: batches take affine-simplex plans");
+    if (P.nnz < 0)
+      return fail(GFGPU_E_STATE, "gfgpu_batch_create: assemble each plan (order 2) first");
+    if (!P.slot_ptr[GFGPU_SLOT_U] || P.slot_n[GFGPU_SLOT_U] != P.n_dof)
+      return fail(GFGPU_E_STATE, "gfgpu_batch_create: variable u (slot 0) not set");
+    if ((rc = check_slots(P, true))) return fail(rc, "");
+    BatchItem it;
+    bool mass;
+    simplex_source_of(P, it.fsrc, it.fscale, mass);
+    it.etype = simplex_batch_type(P.dim, P.degree, P.qdim, mass);
+    it.qd = P.qdim;
+    it.E = P.n_elements;
+    it.n_nodes = P.n_nodes;
+    it.pts = P.d_points;
+    it.cv = P.d_cv;
+    it.enode = P.d_enode;
+    it.tab = P.d_stab;
+    it.L = P.lay;
+    it.form = P.form;
+    for (int k = 0; k < GFGPU_MAX_SLOTS; ++k) it.slots.p[k] = P.slot_ptr[k];
+    it.u = P.slot_ptr[GFGPU_SLOT_U];
+    it.elem = P.d_elem;
+    it.err = B->d_err;
+    it.adj_ptr = P.d_adj_ptr;
+    it.adj = P.d_adj;
+    it.ms = P.max_slots < 1 ? 1 : P.max_slots;
+    it.mad = P.max_adj < 1 ? 1 : P.max_adj;
+    it.nptr = P.d_nptr;
+    it.ncol = P.d_ncol;
+    it.nbits = P.d_nbits;
+    it.slotmap = P.d_slotmap;
+    it.rowptr = P.d_rowptr;
+    it.vals = P.d_vals;
+    it.vec = P.d_vec;
+    if (it.etype < 0 || P.lay.s > 32)
+      return fail(GFGPU_E_UNSUPPORTED, "gfgpu_batch_create: element not batched");
+    items.push_back(it);
+    tile0.push_back(tile0.back() + (P.n_elements + 31) / 32);
+    B->elements += P.n_elements;
+    B->ep_smem = std::max(B->ep_smem, simplex_batch_smem(it.etype));
+    gitems[it.qd].push_back(it);
+    node0[it.qd].push_back(node0[it.qd].back() + P.n_nodes);
+    B->gwarp[it.qd] = std::max(B->gwarp[it.qd], batch_gather_warp_bytes(it));
+    B->plans.push_back(plans[i]);
+  }
+  B->nitems = n;
+  B->ntiles = tile0.back();
+  auto upload = [&](void *dst, const void *src, size_t bytes) -> int {
+    GF_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
+    return GFGPU_OK;
+  };
+  if ((rc = dalloc(&B->d_items, items.size()))) return fail(rc, "");
+  if ((rc = dalloc(&B->d_tile0, tile0.size()))) return fail(rc, "");
+  if ((rc = upload(B->d_items, items.data(), items.size() * sizeof(BatchItem)))) return fail(rc, "");
+  if ((rc = upload(B->d_tile0, tile0.data(), tile0.size() * sizeof(int64_t)))) return fail(rc, "");
+  for (int q = 1; q <= 3; ++q) {
+    B->gn[q] = int(gitems[q].size());
+    B->gnodes[q] = node0[q].back();
+    if (!B->gn[q]) continue;
+    if ((rc = dalloc(&B->d_gitems[q], gitems[q].size()))) return fail(rc, "");
+    if ((rc = dalloc(&B->d_node0[q], node0[q].size()))) return fail(rc, "");
+    if ((rc = upload(B->d_gitems[q], gitems[q].data(), gitems[q].size() * sizeof(BatchItem))))
+      return fail(rc, "");
+    if ((rc = upload(B->d_node0[q], node0[q].data(), node0[q].size() * sizeof(int64_t))))
+      return fail(rc, "");
+  }
+  size_t gmax = 0;
+  for (int q = 1; q <= 3; ++q) gmax = std::max(gmax, B->gwarp[q]);
+  cudaError_t ce = batch_element_pass_attr(B->ep_smem);
+  if (ce == cudaSuccess) ce = batch_gather_attr(4 * gmax);
+  if (ce != cudaSuccess)
+    return fail(GFGPU_E_CUDA, std::string("gfgpu_batch_create: ") + cudaGetErrorString(ce));
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  B->grid_ep = 8 * std::max(sms, 1);
+  B->grid_ga = 8 * std::max(sms, 1);
+  *out = B;
+  return GFGPU_OK;
+}
+
+static int batch_launch(gfgpu_batch *B, cudaStream_t st, int grid_ep, int grid_ga) {
+  GF_CUDA(launch_batch_element_pass(B->d_items, B->d_tile0, B->nitems, B->ntiles, grid_ep,
+                                    B->ep_smem, st));
+  for (int q = 1; q <= 3; ++q)
+    if (B->gn[q])
+      GF_CUDA(launch_batch_gather(B->d_gitems[q], B->d_node0[q], B->gn[q], B->gnodes[q], q,
+                                  grid_ga, B->gwarp[q], st));
+  return GFGPU_OK;
+}
+
+int gfgpu_batch_assemble(gfgpu_batch *B, void *stream) {
+  if (!B) return GFGPU_E_INVALID;
+  return batch_launch(B, static_cast<cudaStream_t>(stream), B->grid_ep, B->grid_ga);
+}
+
+int gfgpu_batch_tune(gfgpu_batch *B, void *stream, int32_t *grid_ep, int32_t *grid_ga) {
+  if (!B) return GFGPU_E_INVALID;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaEvent_t e0, e1;
+  GF_CUDA(cudaEventCreate(&e0));
+  GF_CUDA(cudaEventCreate(&e1));
+  const int mult[] = {1, 2, 4, 8, 16, 32};
+  float best_ep = 1e30f, best_ga = 1e30f;
+  for (int m : mult) {
+    const int g = m * std::max(sms, 1);
+    float t_ep = 0, t_ga = 0;
+    for (int rep = 0; rep < 3; ++rep) {
+      GF_CUDA(cudaEventRecord(e0, st));
+      GF_CUDA(launch_batch_element_pass(B->d_items, B->d_tile0, B->nitems, B->ntiles, g,
+                                        B->ep_smem, st));
+      GF_CUDA(cudaEventRecord(e1, st));
+      GF_CUDA(cudaEventSynchronize(e1));
+      float t;
+      GF_CUDA(cudaEventElapsedTime(&t, e0, e1));
+      t_ep = rep == 0 ? t : std::min(t_ep, t);
+      GF_CUDA(cudaEventRecord(e0, st));
+      for (int q = 1; q <= 3; ++q)
+        if (B->gn[q])
+          GF_CUDA(launch_batch_gather(B->d_gitems[q], B->d_node0[q], B->gn[q], B->gnodes[q], q, g,
+                                      B->gwarp[q], st));
+      GF_CUDA(cudaEventRecord(e1, st));
+      GF_CUDA(cudaEventSynchronize(e1));
+      GF_CUDA(cudaEventElapsedTime(&t, e0, e1));
+      t_ga = rep == 0 ? t : std::min(t_ga, t);
+    }
+    if (t_ep < best_ep) best_ep = t_ep, B->grid_ep = g;
+    if (t_ga < best_ga) best_ga = t_ga, B->grid_ga = g;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (grid_ep) *grid_ep = B->grid_ep;
+  if (grid_ga) *grid_ga = B->grid_ga;
+  return GFGPU_OK;
+}
+
+int gfgpu_batch_sync(gfgpu_batch *B, void *stream) {
+  if (!B) return GFGPU_E_INVALID;
+  int herr = 0;
+  GF_CUDA(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
+  GF_CUDA(cudaMemcpy(&herr, B->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  return status_from_err(herr);
+}
+
+int64_t gfgpu_batch_elements(gfgpu_batch *B) { return B ? B->elements : -1; }
+
+void gfgpu_batch_destroy(gfgpu_batch *B) {
+  if (!B) return;
+  dfree(B->d_items);
+  dfree(B->d_tile0);
+  for (int q = 0; q < 4; ++q) {
+    dfree(B->d_gitems[q]);
+    dfree(B->d_node0[q]);
+  }
+  dfree(B->d_err);
+  delete B;
 }
 
 int gfgpu_sync(gfgpu_plan *P) {

@@ -168,27 +168,24 @@ __host__ __device__ __forceinline__ size_t gather_warp_bytes(int ms, int qd, int
   return (b + 15) / 16 * 16;
 }
 
-// QD components, R = ceil(nb*qd/32) lane rounds over the columns of a row.
+// The row gather of one DOF node by one warp (QD components, R =
+// ceil(nb*qd/32) lane rounds over the columns of a row); `base` is the
+// warp's shared-memory area of gather_warp_bytes(ms, QD, rowstride, mad).
 template <int QD, int R>
-__global__ void __launch_bounds__(128) gather_kernel(
-    int64_t n_nodes, KeLayout L, const int32_t *__restrict__ adj_ptr,
-    const int32_t *__restrict__ adj, const int32_t *__restrict__ enode,
-    const double *__restrict__ elem, int ms, int mad, const int64_t *__restrict__ nptr,
-    const int32_t *__restrict__ ncol, const uint16_t *__restrict__ nbits,
+__device__ __forceinline__ void gather_node(
+    char *base, int64_t node, const KeLayout &L, const int32_t *__restrict__ adj_ptr,
+    const int32_t *__restrict__ adj, const double *__restrict__ elem, int ms, int mad,
+    const int64_t *__restrict__ nptr, const uint16_t *__restrict__ nbits,
     const int16_t *__restrict__ slotmap, const int64_t *__restrict__ rowptr,
     double *__restrict__ vals, bool want_K, bool want_R, double *__restrict__ vec,
     int *__restrict__ err) {
   constexpr int QQ = QD * QD;
-  extern __shared__ __align__(16) double dsm[];
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
   const int nb = L.nb, S = L.s, rs = L.rowstride, blk = QD * rs;
-  char *base = reinterpret_cast<char *>(dsm) + wib * gather_warp_bytes(ms, QD, rs, mad);
   double *Kbuf = reinterpret_cast<double *>(base);                // 2 x blk
   double *acc = Kbuf + 2 * blk;                                    // ms * QQ
   int *adjs = reinterpret_cast<int *>(acc + size_t(ms) * QQ);     // mad
   uint16_t *bits = reinterpret_cast<uint16_t *>(adjs + mad);      // ms
-  const int64_t node = blockIdx.x * int64_t(blockDim.x >> 5) + wib;
-  if (node >= n_nodes) return;
   const int64_t s0 = nptr[node];
   const int ns = int(nptr[node + 1] - s0);
   const int a0 = adj_ptr[node], nadj = adj_ptr[node + 1] - a0;
@@ -302,6 +299,49 @@ __global__ void __launch_bounds__(128) gather_kernel(
   }
 }
 
+template <int QD, int R>
+__global__ void __launch_bounds__(128) gather_kernel(
+    int64_t n_nodes, KeLayout L, const int32_t *__restrict__ adj_ptr,
+    const int32_t *__restrict__ adj, const double *__restrict__ elem, int ms, int mad,
+    const int64_t *__restrict__ nptr, const uint16_t *__restrict__ nbits,
+    const int16_t *__restrict__ slotmap, const int64_t *__restrict__ rowptr,
+    double *__restrict__ vals, bool want_K, bool want_R, double *__restrict__ vec,
+    int *__restrict__ err) {
+  extern __shared__ __align__(16) double dsm[];
+  const int wib = threadIdx.x >> 5;
+  char *base = reinterpret_cast<char *>(dsm) + wib * gather_warp_bytes(ms, QD, L.rowstride, mad);
+  const int64_t node = blockIdx.x * int64_t(blockDim.x >> 5) + wib;
+  if (node >= n_nodes) return;
+  gather_node<QD, R>(base, node, L, adj_ptr, adj, elem, ms, mad, nptr, nbits, slotmap, rowptr,
+                     vals, want_K, want_R, vec, err);
+}
+
+// Persistent row gather over the DOF nodes of every mesh of a batch (R = 1:
+// rows of at most 32 columns); warp w of the grid takes nodes w, w + warps, ...
+template <int QD>
+__global__ void __launch_bounds__(128) batch_gather_kernel(
+    const BatchItem *__restrict__ items, const int64_t *__restrict__ node0, int nitems,
+    int64_t nnodes, size_t warp_bytes) {
+  extern __shared__ __align__(16) double dsm[];
+  const int wib = threadIdx.x >> 5;
+  char *base = reinterpret_cast<char *>(dsm) + wib * warp_bytes;
+  const int64_t nw = int64_t(gridDim.x) * (blockDim.x >> 5);
+  for (int64_t g = blockIdx.x * int64_t(blockDim.x >> 5) + wib; g < nnodes; g += nw) {
+    int lo = 0, hi = nitems - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (node0[mid] <= g) lo = mid;
+      else hi = mid - 1;
+    }
+    const BatchItem &it = items[lo];
+    if (it.qd != QD) continue;
+    __syncwarp();
+    gather_node<QD, 1>(base, g - node0[lo], it.L, it.adj_ptr, it.adj, it.elem, it.ms, it.mad,
+                       it.nptr, it.nbits, it.slotmap, it.rowptr, it.vals, true, true, it.vec,
+                       it.err);
+  }
+}
+
 size_t pattern_smem(int cap) { return size_t(kWarpsPerBlock) * (3 * cap + kMaxLocal) * sizeof(int); }
 
 int pattern_cap(const Plan &P) {
@@ -321,8 +361,8 @@ cudaError_t launch_gather_t(Plan &P, bool want_K, bool want_R) {
   if (ce != cudaSuccess) return ce;
   const unsigned blocks = unsigned((P.n_nodes + kWarpsPerBlock - 1) / kWarpsPerBlock);
   gather_kernel<QD, R><<<blocks, kWarpsPerBlock * 32, smem, P.stream>>>(
-      P.n_nodes, P.lay, P.d_adj_ptr, P.d_adj, P.d_enode, P.d_elem, ms, mad, P.d_nptr, P.d_ncol,
-      P.d_nbits, P.d_slotmap, P.d_rowptr, P.d_vals, want_K, want_R, P.d_vec, P.d_err);
+      P.n_nodes, P.lay, P.d_adj_ptr, P.d_adj, P.d_elem, ms, mad, P.d_nptr, P.d_nbits,
+      P.d_slotmap, P.d_rowptr, P.d_vals, want_K, want_R, P.d_vec, P.d_err);
   P.launches++;
   return cudaGetLastError();
 }
@@ -367,6 +407,45 @@ cudaError_t launch_pattern_fill(Plan &P) {
       P.d_rowptr, P.d_colidx, P.d_nptr, P.d_ncol, P.d_nbits, P.d_slotmap, P.d_err);
   P.launches++;
   return cudaGetLastError();
+}
+
+size_t batch_gather_warp_bytes(const BatchItem &it) {
+  return gather_warp_bytes(it.ms, it.qd, it.L.rowstride, it.mad);
+}
+
+cudaError_t launch_batch_gather(const BatchItem *items, const int64_t *node0, int nitems,
+                               int64_t nnodes, int qd, int grid, size_t warp_bytes,
+                               cudaStream_t st) {
+  if (nnodes == 0) return cudaSuccess;
+  const size_t smem = size_t(kWarpsPerBlock) * warp_bytes;
+  switch (qd) {
+    case 1:
+      batch_gather_kernel<1><<<grid, kWarpsPerBlock * 32, smem, st>>>(items, node0, nitems, nnodes,
+                                                                       warp_bytes);
+      break;
+    case 2:
+      batch_gather_kernel<2><<<grid, kWarpsPerBlock * 32, smem, st>>>(items, node0, nitems, nnodes,
+                                                                       warp_bytes);
+      break;
+    case 3:
+      batch_gather_kernel<3><<<grid, kWarpsPerBlock * 32, smem, st>>>(items, node0, nitems, nnodes,
+                                                                       warp_bytes);
+      break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t batch_gather_attr(size_t smem) {
+  cudaError_t ce;
+  if ((ce = cudaFuncSetAttribute(batch_gather_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 int(smem))) != cudaSuccess)
+    return ce;
+  if ((ce = cudaFuncSetAttribute(batch_gather_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 int(smem))) != cudaSuccess)
+    return ce;
+  return cudaFuncSetAttribute(batch_gather_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              int(smem));
 }
 
 cudaError_t launch_gather(Plan &P, bool want_K, bool want_R) {

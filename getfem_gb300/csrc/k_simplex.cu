@@ -43,23 +43,44 @@ namespace {
 constexpr int kEpWarps = 4;            // warps per block (share 32 elements)
 constexpr int kEpThreads = 32 * kEpWarps;
 
+}  // namespace
+
+// Shared memory of one 32-element tile of the simplex element pass.
+template <int DIM, int QD, int NB>
+struct EpShared {
+  static constexpr int NV = DIM + 1, M = QD * NV, NTP = M * (M + 1) / 2;
+  static constexpr int S = NB * QD;
+  static constexpr int NG = NV * DIM + 8;  // g, J c0, J c1, J c2, J cmass, J, flag
+  double s_gval[NB * NB * kMaxPairTerms];
+  double s_mass[NB * NB];
+  double Gs[NG][32];     // geometry of the tile's 32 elements
+  double Tp[NTP][32];    // upper triangle of T per element
+  double Us[S][32];      // u at the element's DOFs
+  long long mxs[kEpWarps][32];
+  int8_t s_nterm[NB * NB];
+  int8_t s_vw[NB * NB * kMaxPairTerms];
+};
+
+// One tile (32 elements, 4 warps) of the element pass; every thread of the
+// block calls it (it synchronises the block).
 template <int DIM, int QD, int NB, bool MASS, bool STORE_K>
-__global__ void __launch_bounds__(kEpThreads) simplex_element_pass(
-    int64_t E, const double *__restrict__ pts, const int32_t *__restrict__ cv,
-    const int32_t *__restrict__ enode, const SimplexTables *__restrict__ tab, KeLayout L,
-    gfgpu_form form, SlotPtrs slots, const double *__restrict__ fsrc, double fscale,
+__device__ __forceinline__ void simplex_element_tile(
+    EpShared<DIM, QD, NB> &sh, int64_t tile, int64_t E, const double *__restrict__ pts,
+    const int32_t *__restrict__ cv, const int32_t *__restrict__ enode,
+    const SimplexTables *__restrict__ tab, const KeLayout &L, const gfgpu_form &form,
+    const SlotPtrs &slots, const double *__restrict__ fsrc, double fscale,
     const double *__restrict__ u, double *__restrict__ out, int *__restrict__ err) {
-  constexpr int NV = DIM + 1, M = QD * NV, NTP = M * (M + 1) / 2;
-  constexpr int S = NB * QD, RS = (S + 3) & ~3;
-  constexpr int NG = NV * DIM + 8;  // g, J c0, J c1, J c2, J cmass, J, flag
-  __shared__ int8_t s_nterm[NB * NB];
-  __shared__ int8_t s_vw[NB * NB * kMaxPairTerms];
-  __shared__ double s_gval[NB * NB * kMaxPairTerms];
-  __shared__ double s_mass[NB * NB];
-  __shared__ double Gs[NG][32];     // geometry of the block's 32 elements
-  __shared__ double Tp[NTP][32];    // upper triangle of T per element
-  __shared__ long long mxs[kEpWarps][32];
-  __shared__ double Us[S][32];      // u at the element's DOFs
+  using SH = EpShared<DIM, QD, NB>;
+  constexpr int NV = SH::NV, M = SH::M;
+  constexpr int S = SH::S, RS = (S + 3) & ~3;
+  auto &s_nterm = sh.s_nterm;
+  auto &s_vw = sh.s_vw;
+  auto &s_gval = sh.s_gval;
+  auto &s_mass = sh.s_mass;
+  auto &Gs = sh.Gs;
+  auto &Tp = sh.Tp;
+  auto &mxs = sh.mxs;
+  auto &Us = sh.Us;
   for (int k = threadIdx.x; k < NB * NB; k += blockDim.x) {
     s_nterm[k] = tab->nterm[k];
     s_mass[k] = tab->mass[k];
@@ -69,7 +90,7 @@ __global__ void __launch_bounds__(kEpThreads) simplex_element_pass(
     s_gval[k] = tab->gval[k];
   }
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int64_t e = blockIdx.x * int64_t(32) + lane;
+  const int64_t e = tile * int64_t(32) + lane;
   const bool active = e < E;
   // ---- warp 0: geometry and coefficients (lane = element)
   if (wid == 0) {
@@ -258,6 +279,19 @@ __global__ void __launch_bounds__(kEpThreads) simplex_element_pass(
   }
 }
 
+namespace {
+
+template <int DIM, int QD, int NB, bool MASS, bool STORE_K>
+__global__ void __launch_bounds__(kEpThreads) simplex_element_pass(
+    int64_t E, const double *__restrict__ pts, const int32_t *__restrict__ cv,
+    const int32_t *__restrict__ enode, const SimplexTables *__restrict__ tab, KeLayout L,
+    gfgpu_form form, SlotPtrs slots, const double *__restrict__ fsrc, double fscale,
+    const double *__restrict__ u, double *__restrict__ out, int *__restrict__ err) {
+  __shared__ EpShared<DIM, QD, NB> sh;
+  simplex_element_tile<DIM, QD, NB, MASS, STORE_K>(sh, blockIdx.x, E, pts, cv, enode, tab, L,
+                                                   form, slots, fsrc, fscale, u, out, err);
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------- host
@@ -353,6 +387,118 @@ int fill_simplex_tables(int dim, int K, int qdim, const std::string &im, Simplex
   lay.stride = lay.off_thr + 4;
   lay.linear = true;
   return GFGPU_OK;
+}
+
+// ---------------------------------------------------------------- batched
+
+namespace {
+
+// the element-pass instances of the batched launch, (dim, degree, qdim, mass)
+constexpr int kBatchTypes = 16;
+
+template <int T>
+struct BatchType;
+#define GFGPU_BT(T, D, Q, N, MS)                        \
+  template <>                                           \
+  struct BatchType<T> {                                 \
+    static constexpr int DIM = D, QD = Q, NB = N;       \
+    static constexpr bool MASS = MS;                    \
+  };
+GFGPU_BT(0, 2, 1, 3, false) GFGPU_BT(1, 2, 1, 6, false) GFGPU_BT(2, 2, 2, 3, false)
+GFGPU_BT(3, 2, 2, 6, false) GFGPU_BT(4, 3, 1, 4, false) GFGPU_BT(5, 3, 1, 10, false)
+GFGPU_BT(6, 3, 3, 4, false) GFGPU_BT(7, 3, 3, 10, false) GFGPU_BT(8, 2, 1, 3, true)
+GFGPU_BT(9, 2, 1, 6, true) GFGPU_BT(10, 2, 2, 3, true) GFGPU_BT(11, 2, 2, 6, true)
+GFGPU_BT(12, 3, 1, 4, true) GFGPU_BT(13, 3, 1, 10, true) GFGPU_BT(14, 3, 3, 4, true)
+GFGPU_BT(15, 3, 3, 10, true)
+#undef GFGPU_BT
+
+template <int T>
+__device__ __forceinline__ void run_batch_tile(unsigned char *dsm, const BatchItem &it,
+                                               int64_t tile) {
+  using B = BatchType<T>;
+  using SH = EpShared<B::DIM, B::QD, B::NB>;
+  simplex_element_tile<B::DIM, B::QD, B::NB, B::MASS, true>(
+      *reinterpret_cast<SH *>(dsm), tile, it.E, it.pts, it.cv, it.enode, it.tab, it.L, it.form,
+      it.slots, it.fsrc, it.fscale, it.u, it.elem, it.err);
+}
+
+// Persistent element pass over the tiles of every mesh of the batch: block b
+// takes tiles b, b + grid, ...; the mesh of a tile is found by binary search
+// in the tile offsets.
+__global__ void __launch_bounds__(kEpThreads) batch_element_pass(
+    const BatchItem *__restrict__ items, const int64_t *__restrict__ tile0, int nitems,
+    int64_t ntiles) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    int lo = 0, hi = nitems - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (tile0[mid] <= t) lo = mid;
+      else hi = mid - 1;
+    }
+    const BatchItem &it = items[lo];
+    const int64_t tile = t - tile0[lo];
+    __syncthreads();  // the previous tile is done with the shared memory
+    switch (it.etype) {
+#define GFGPU_RT(T) \
+  case T: run_batch_tile<T>(dsm, it, tile); break;
+      GFGPU_RT(0) GFGPU_RT(1) GFGPU_RT(2) GFGPU_RT(3) GFGPU_RT(4) GFGPU_RT(5) GFGPU_RT(6)
+      GFGPU_RT(7) GFGPU_RT(8) GFGPU_RT(9) GFGPU_RT(10) GFGPU_RT(11) GFGPU_RT(12) GFGPU_RT(13)
+      GFGPU_RT(14) GFGPU_RT(15)
+#undef GFGPU_RT
+      default: break;
+    }
+  }
+}
+
+template <int T>
+size_t smem_of() {
+  using B = BatchType<T>;
+  return sizeof(EpShared<B::DIM, B::QD, B::NB>);
+}
+
+}  // namespace
+
+int simplex_batch_type(int dim, int degree, int qdim, bool mass) {
+  int base;
+  if (dim == 2) base = (qdim == 1 ? 0 : 2) + (degree == 1 ? 0 : 1);
+  else base = 4 + (qdim == 1 ? 0 : 2) + (degree == 1 ? 0 : 1);
+  if (degree < 1 || degree > 2 || (qdim != 1 && qdim != dim)) return -1;
+  return base + (mass ? 8 : 0);
+}
+
+size_t simplex_batch_smem(int etype) {
+  static const size_t sz[kBatchTypes] = {
+      smem_of<0>(),  smem_of<1>(),  smem_of<2>(),  smem_of<3>(),  smem_of<4>(),  smem_of<5>(),
+      smem_of<6>(),  smem_of<7>(),  smem_of<8>(),  smem_of<9>(),  smem_of<10>(), smem_of<11>(),
+      smem_of<12>(), smem_of<13>(), smem_of<14>(), smem_of<15>()};
+  return etype >= 0 && etype < kBatchTypes ? sz[etype] : 0;
+}
+
+void simplex_source_of(const Plan &P, const double *&fsrc, double &fscale, bool &mass) {
+  fsrc = nullptr;
+  fscale = 0.0;
+  mass = false;
+  for (int t = 0; t < P.form.n_terms; ++t) {
+    const gfgpu_term &T = P.form.terms[t];
+    if (T.kind == GFGPU_TERM_SOURCE) {
+      fsrc = P.slot_ptr[T.field_slot];
+      fscale = T.scale * (T.c[0].kind == GFGPU_COEF_CONST ? T.c[0].value : 1.0);
+    }
+    if (T.kind == GFGPU_TERM_MASS) mass = true;
+  }
+}
+
+cudaError_t launch_batch_element_pass(const BatchItem *items, const int64_t *tile0, int nitems,
+                                     int64_t ntiles, int grid, size_t smem, cudaStream_t st) {
+  if (ntiles == 0) return cudaSuccess;
+  batch_element_pass<<<grid, kEpThreads, smem, st>>>(items, tile0, nitems, ntiles);
+  return cudaGetLastError();
+}
+
+cudaError_t batch_element_pass_attr(size_t smem) {
+  return cudaFuncSetAttribute(batch_element_pass, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              int(smem));
 }
 
 int build_simplex_tables(Plan &P, std::string &errmsg) {

@@ -134,6 +134,44 @@ struct Plan {
   bool profiled = false;
 };
 
+// One mesh of a batched launch: everything the element pass and the row
+// gather of an affine-simplex plan read (device pointers).
+struct BatchItem {
+  int32_t etype = 0;   // element-pass instance (simplex_batch_type)
+  int32_t qd = 1;      // gather: components
+  int64_t E = 0, n_nodes = 0;
+  const double *pts = nullptr;
+  const int32_t *cv = nullptr, *enode = nullptr;
+  const SimplexTables *tab = nullptr;
+  KeLayout L{};
+  gfgpu_form form{};
+  SlotPtrs slots{};
+  const double *fsrc = nullptr;
+  double fscale = 0.0;
+  const double *u = nullptr;
+  double *elem = nullptr;
+  int *err = nullptr;
+  const int32_t *adj_ptr = nullptr, *adj = nullptr;
+  int32_t ms = 1, mad = 1;
+  const int64_t *nptr = nullptr;
+  const int32_t *ncol = nullptr;
+  const uint16_t *nbits = nullptr;
+  const int16_t *slotmap = nullptr;
+  const int64_t *rowptr = nullptr;
+  double *vals = nullptr, *vec = nullptr;
+};
+
+// batched launches (k_simplex.cu, k_assemble.cu)
+int simplex_batch_type(int dim, int degree, int qdim, bool mass);
+size_t simplex_batch_smem(int etype);
+void simplex_source_of(const Plan &P, const double *&fsrc, double &fscale, bool &mass);
+cudaError_t launch_batch_element_pass(const BatchItem *items, const int64_t *tile0, int nitems,
+                                     int64_t ntiles, int grid, size_t smem, cudaStream_t st);
+size_t batch_gather_warp_bytes(const BatchItem &it);
+cudaError_t launch_batch_gather(const BatchItem *items, const int64_t *node0, int nitems,
+                               int64_t nnodes, int qd, int grid, size_t warp_bytes,
+                               cudaStream_t st);
+
 // kernels (k_simplex.cu)
 cudaError_t launch_simplex_element_pass(Plan &P, bool with_u);
 cudaError_t launch_pattern_count(Plan &P);

@@ -243,6 +243,51 @@ int gfgpu_potential_gradient(gfgpu_plan *plan, int32_t slot, double *grad, int64
    the copy. */
 int gfgpu_set_points(gfgpu_plan *plan, const double *points, int64_t n, int32_t on_device);
 
+/* Dirichlet conditions by elimination on the plan's assembled K (after an
+   order-2 assembly), as the reference model's dof constraints on a linear
+   symmetric problem (getfem_models.cc:2806-2870): for the n constrained
+   DOFs dofs[k] with values g_k (values may be NULL for zeros),
+   rhs -= K(:, D) g on the other rows, rhs(D) = g, rows and columns D of K
+   cleared and K(d,d) = 1.  rhs is a device vector of n_dof entries (or NULL
+   to change K only).  The CSR pattern is kept.  Waits for the result. */
+int gfgpu_dirichlet_eliminate(gfgpu_plan *plan, const int64_t *dofs, int64_t n,
+                              const double *values, double *rhs);
+
+/* Conjugate gradients on the plan's K: gmm::cg (gmm/gmm_solver_cg.h:84-157)
+   with precond 0 = identity, 1 = diagonal (Jacobi), and gmm::iteration's
+   stop rule (gmm/gmm_iter.h:113-150): stops when ||r||_2 <= ||b||_2 resmax
+   or after maxiter iterations; x = 0 when b = 0.  b and x are device
+   vectors of n_dof entries; x holds the initial guess and receives the
+   solution.  *iterations and *residual (= ||r|| / ||b||) are optional. */
+int gfgpu_cg(gfgpu_plan *plan, const double *b, double *x, double resmax, int64_t maxiter,
+             int32_t precond, int64_t *iterations, double *residual);
+
+/* ------------------------------------------------------------------ */
+/* Batched assembly of many meshes (independent plans) in one launch.  */
+/* The reference assembles one mesh per ga_workspace::assembly call;   */
+/* a batch replaces a loop of such calls over independent workspaces.  */
+typedef struct gfgpu_batch_s gfgpu_batch;
+
+/* Groups n affine-simplex plans (each assembled once at order 2, so that
+   its CSR pattern exists, and with u and its data set) into one batch.
+   The plans' device buffers are referenced, not copied: data changed in
+   place (coefficients, u) is seen by the next batched assembly; a plan
+   whose data pointers change must be re-batched. */
+int gfgpu_batch_create(gfgpu_plan *const *plans, int32_t n, gfgpu_batch **out);
+/* K values and order-1 vectors of every plan of the batch: one persistent
+   element-pass launch over the elements of all meshes and one persistent
+   row-gather launch per component count, on `stream`.  Only kernel launches
+   are issued, so the call can be captured in a CUDA graph and replayed. */
+int gfgpu_batch_assemble(gfgpu_batch *batch, void *cuda_stream);
+/* Times the two launches over grid sizes of 1, 2, 4, ..., 32 blocks per SM
+   and keeps the fastest of each (optional outputs: the chosen grids). */
+int gfgpu_batch_tune(gfgpu_batch *batch, void *cuda_stream, int32_t *grid_elem,
+                     int32_t *grid_gather);
+/* Waits for `stream` and reports the batch's device error word. */
+int gfgpu_batch_sync(gfgpu_batch *batch, void *cuda_stream);
+int64_t gfgpu_batch_elements(gfgpu_batch *batch);
+void gfgpu_batch_destroy(gfgpu_batch *batch);
+
 /* Waits for the plan's stream and reports the device error word
    (GFGPU_E_JACOBIAN / GFGPU_E_NAN) of the last assembly. */
 int gfgpu_sync(gfgpu_plan *plan);

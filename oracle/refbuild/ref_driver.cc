@@ -10,6 +10,11 @@
 // usage: ref_driver key=value ...
 //   dim=2|3 nx=N gt=PK|QK fem=K qdim=Q im=IM_NAME in=DIR out=DIR
 //   expr=GWFL  orders=2,1,0  reps=R  jitter=0|1
+//   solve=cg resmax=R maxiter=N   (after the orders: solve K x = -R with
+//       homogeneous Dirichlet conditions on the boundary DOFs eliminated as
+//       the model's dof constraints do, getfem_models.cc:2806-2870, by
+//       gmm::cg with the identity preconditioner; writes x.bin and the
+//       iteration count)
 //   consts=name:KIND,...   KIND = P0 (one value per element),
 //                                 S  (scalar field on the same FEM),
 //                                 V  (field on the variable's FEM, qdim Q),
@@ -21,6 +26,7 @@
 #include "getfem/getfem_regular_meshes.h"
 #include "getfem/getfem_mesh_fem.h"
 #include "getfem/getfem_mesh_im.h"
+#include "gmm/gmm_solver_cg.h"
 #include <chrono>
 #include <cstdio>
 #include <fstream>
@@ -234,6 +240,43 @@ int main(int argc, char **argv) {
       std::vector<double> e(1, ws.assembled_potential());
       write_file(out + "/E.bin", e);
     }
+  }
+  if (arg("solve", "") == "cg") {
+    // boundary DOFs (outer faces of the mesh)
+    getfem::mesh_region border;
+    getfem::outer_faces_of_mesh(m, border);
+    m.region(1).clear();
+    for (getfem::mr_visitor i(border); !i.finished(); ++i) m.region(1).add(i.cv(), i.f());
+    dal::bit_vector bd = mf.dof_on_region(m.region(1));
+    ws.assembly(2);
+    ws.assembled_vector().clear();
+    ws.assembly(1);
+    size_type n = ndof;
+    gmm::col_matrix<gmm::wsvector<double>> A(n, n);
+    gmm::copy(ws.assembled_matrix(), A);
+    std::vector<double> b(n), x(n, 0.0);
+    gmm::copy(gmm::scaled(ws.assembled_vector(), -1.0), b);
+    std::vector<bool> isd(n, false);
+    for (dal::bv_visitor i(bd); !i.finished(); ++i) isd[i] = true;
+    for (size_type j = 0; j < n; ++j) {
+      if (isd[j]) { A.col(j).clear(); continue; }
+      std::vector<size_type> rm;
+      for (const auto &e : A.col(j)) if (isd[e.first]) rm.push_back(e.first);
+      for (size_type i : rm) A(i, j) = 0.0;
+    }
+    for (size_type i = 0; i < n; ++i) if (isd[i]) { A(i, i) = 1.0; b[i] = 0.0; }
+    gmm::csr_matrix<double> Acsr;
+    gmm::copy(A, Acsr);
+    gmm::iteration iter(std::stod(arg("resmax", "1e-12")), 0, size_t(std::stoll(arg("maxiter", "100000"))));
+    auto t0 = std::chrono::steady_clock::now();
+    gmm::cg(Acsr, x, b, gmm::identity_matrix(), iter);
+    auto t1 = std::chrono::steady_clock::now();
+    write_file(out + "/x.bin", x);
+    std::vector<int64_t> bdl;
+    for (dal::bv_visitor i(bd); !i.finished(); ++i) bdl.push_back(int64_t(i));
+    write_file(out + "/dirichlet.bin", bdl);
+    fprintf(info, ", \"cg_iterations\": %zu, \"t_cg\": %.6e", size_t(iter.get_iteration()),
+            std::chrono::duration<double>(t1 - t0).count());
   }
   fprintf(info, "}\n");
   fclose(info);

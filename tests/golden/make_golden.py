@@ -72,6 +72,11 @@ CASES = [
     ("p2tri_energy_potential", 2, "PK", 2, 1, "IM_TRIANGLE(4)", 5,
      "kappa*Grad_u.Grad_u + 2*u*u - f*u", {"kappa": "P0", "f": "V"}, True, "normal"),
 ]
+# Poisson on the 64 x 64 P1 triangle mesh, homogeneous Dirichlet conditions
+# on the boundary, solved by gmm::cg (the 2-D Poisson configuration)
+CASES.append(("p1tri_poisson_cg", 2, "PK", 1, 1, "IM_TRIANGLE(2)", 64,
+              "Grad_u.Grad_Test_u - f*Test_u", {"f": "V"}, False, "zero"))
+EXTRA = {"p1tri_poisson_cg": ["solve=cg", "resmax=1e-12", "maxiter=100000"]}
 ORDERS = {"q2hex_nh_potential": "0,1,2", "p2tet_nh_potential": "0,1,2",
           "q2hex_kappa_potential": "0,1,2", "p2tri_energy_potential": "0,1,2"}
 
@@ -103,6 +108,8 @@ def make_case(case, seed):
     inputs = {}
     if ukind == "modes":
         inputs["u"] = sinusoid_modes(mf.basic_dof_nodes(), qdim, rng)
+    elif ukind == "zero":
+        inputs["u"] = np.zeros(ndof)
     else:
         inputs["u"] = rng.standard_normal(ndof) * 0.1
     for cname, ck in consts.items():
@@ -128,7 +135,7 @@ def make_case(case, seed):
         cs = ",".join(f"{k}:{v}" for k, v in consts.items())
         cmd = [DRIVER, f"dim={dim}", f"nx={nx}", f"gt={gt}", f"fem={deg}", f"qdim={qdim}",
                f"im={im}", f"in={ind}", f"out={outd}", f"expr={expr}",
-               f"orders={ORDERS.get(name, '2,1')}",
+               f"orders={ORDERS.get(name, '2,1')}"] + EXTRA.get(name, []) + [
                f"jitter={1 if jit is not None else 0}", f"consts={cs}"]
         subprocess.run(cmd, check=True)
         info = json.load(open(os.path.join(outd, "info.json")))
@@ -151,6 +158,10 @@ def make_case(case, seed):
         )
         if os.path.exists(os.path.join(outd, "E.bin")):
             rec["E"] = rd("E.bin")
+        if os.path.exists(os.path.join(outd, "x.bin")):
+            rec["x"] = rd("x.bin")
+            rec["dirichlet"] = rd("dirichlet.bin", np.int64)
+            rec["cg_iterations"] = np.array([info["cg_iterations"]])
     for k, v in inputs.items():
         rec["in_" + k] = np.asarray(v, dtype=np.float64)
     if jit is not None:
