@@ -174,6 +174,273 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------- secondary workloads
+# Each is measured after the headline line's timed region, on rank 0 of a
+# one-GPU run, with CUDA events on the plans' stream (the default stream).
+
+def _events_ms(fn, reps):
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def bench_neohookean(steps):
+    """Q2 hexahedra 32^3 (32768 elements), compressible neo-Hookean, u = 8
+    sinusoid modes of amplitude 0.05, per-element mu lognormal(0, 0.3): K + R
+    (one pass) and the adjoint of the strain energy in mu and in the vertex
+    coordinates (dE/du is R)."""
+    import torch
+    import getfem_gb300 as g
+    from getfem_gb300 import _lib as L
+    lib = L.lib()
+    rng = np.random.default_rng(3)
+    mesh = g.Mesh.regular_unit(3, 32, "hex")
+    mf = g.MeshFem(mesh, 3, degree=2)
+    mim = g.MeshIm(mesh, "IM_GAUSS_PARALLELEPIPED(3,5)")
+    xyz = mf.basic_dof_nodes()
+    u = np.zeros((xyz.shape[0], 3))
+    for a in range(3):
+        for _ in range(8):
+            k = rng.uniform(-np.pi, np.pi, 3)
+            u[:, a] += 0.05 * np.sin(xyz @ k + rng.uniform(0, 2 * np.pi))
+    E = mesh.nb_convex()
+    dev = "cuda"
+    mu = torch.tensor(np.exp(rng.normal(0, 0.3, E)), device=dev)
+    ws = g.GaWorkspace()
+    ws.add_fem_variable("u", mf, U=torch.tensor(u.ravel(), device=dev))
+    ws.add_fem_constant("mu", g.MeshFem(mesh, 1, degree=0), mu)
+    ws.add_fixed_size_constant("D1", np.array([1.5]))
+    ws.add_expression("Compressible_Neo_Hookean_potential(Grad_u,[0.5*mu;D1])", mim)
+    grp = ws.groups[0]
+    h1 = ws._plan(grp, grp.order1)
+    ws._upload(h1, grp.order1, need_u=True)
+    h0 = ws._plan(grp, grp.order0)
+    ws._upload(h0, grp.order0, need_u=True)
+    L.check(lib.gfgpu_assemble(h1, 2, L.WITH_VECTOR, None))
+    gmu = torch.empty_like(mu)
+    gX = torch.empty(mesh.points.size, dtype=torch.float64, device=dev)
+    slot = ws.data["mu"].slot
+
+    def kr():
+        L.check(lib.gfgpu_assemble(h1, 2, L.WITH_VECTOR, None))
+
+    def adj():
+        L.check(lib.gfgpu_assemble(h0, 0, 0, None))
+        L.check(lib.gfgpu_potential_gradient(h0, slot, C.c_void_p(gmu.data_ptr()), E, 1))
+        L.check(lib.gfgpu_potential_gradient(h0, L.SLOT_POINTS, C.c_void_p(gX.data_ptr()),
+                                             gX.numel(), 1))
+    for _ in range(2):
+        kr()
+        adj()
+    t_kr = _events_ms(kr, steps)
+    t_adj = _events_ms(adj, steps)
+    out = {"workload": "Q2 hex 32^3 compressible neo-Hookean, IM_GAUSS_PARALLELEPIPED(3,5): "
+                       "K + R, then energy + dE/dmu + dE/dX (dE/du = R)",
+           "elements": E, "n_dof": mf.nb_dof(),
+           "ms_K_R": t_kr, "ms_adjoint": t_adj,
+           "elements_per_s_K_R": E / (t_kr * 1e-3),
+           "elements_per_s_K_R_adjoint": E / ((t_kr + t_adj) * 1e-3)}
+    del ws
+    return out
+
+
+def _batch_meshes(rng, n, lo, hi):
+    """n (type, nx) pairs: element counts log-uniform in [lo, hi], types
+    P1/P2 triangles (Poisson) and P1/P2 tetrahedra (elasticity)."""
+    out = []
+    for _ in range(n):
+        target = float(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+        kind = int(rng.integers(4))
+        if kind < 2:
+            nx = max(2, int(round(np.sqrt(target / 2.0))))
+        else:
+            nx = max(2, int(round((target / 6.0) ** (1.0 / 3.0))))
+        out.append((kind, nx))
+    return out
+
+
+def bench_batched(steps, n_meshes=512, lo=1e3, hi=2e5):
+    """512 independent meshes, element counts log-uniform in [1e3, 2e5], a
+    random mix of P1/P2 triangle Poisson and P1/P2 tetrahedron elasticity,
+    coefficients lognormal(0, 0.2): K + R of every mesh, plain (one
+    gfgpu_assemble per mesh) against batched (one persistent launch per
+    kernel) and its CUDA graph replayed with coefficients perturbed in place.
+    The same with many small meshes shows the launch-bound regime."""
+    import gc
+    import torch
+    import getfem_gb300 as g
+    from getfem_gb300 import _lib as L
+    from getfem_gb300.batch import Batch
+    lib = L.lib()
+    rng = np.random.default_rng(4)
+    dev = "cuda"
+    t0 = time.perf_counter()
+    wss, coefs = [], []
+    for kind, nx in _batch_meshes(rng, n_meshes, lo, hi):
+        deg = 1 + kind % 2
+        dim = 2 if kind < 2 else 3
+        mesh = g.Mesh.regular_unit(dim, nx, "simplex")
+        q = 1 if dim == 2 else 3
+        mf = g.MeshFem(mesh, q, degree=deg)
+        mf0 = g.MeshFem(mesh, 1, degree=0)
+        E = mesh.nb_convex()
+        ws = g.GaWorkspace()
+        ws.add_fem_variable("u", mf, U=torch.tensor(rng.standard_normal(mf.nb_dof()) * 1e-2,
+                                                    device=dev))
+        if dim == 2:
+            c = torch.tensor(np.exp(rng.normal(0, 0.2, E)), device=dev)
+            ws.add_fem_constant("kappa", mf0, c)
+            coefs.append(c)
+            ws.add_fem_constant("f", mf, torch.tensor(rng.uniform(-1, 1, mf.nb_dof()), device=dev))
+            ws.add_expression("kappa*Grad_u.Grad_Test_u - f*Test_u",
+                              g.MeshIm(mesh, "IM_TRIANGLE(2)" if deg == 1 else "IM_TRIANGLE(4)"))
+        else:
+            for nm in ("lambda", "mu"):
+                c = torch.tensor(np.exp(rng.normal(0, 0.2, E)), device=dev)
+                ws.add_fem_constant(nm, mf0, c)
+                coefs.append(c)
+            ws.add_fem_constant("f", mf, torch.tensor(rng.standard_normal(mf.nb_dof()), device=dev))
+            ws.add_expression(EXPR, g.MeshIm(mesh, "IM_TETRAHEDRON(2)" if deg == 1
+                                             else "IM_TETRAHEDRON(5)"))
+        wss.append(ws)
+    b = Batch(wss)
+    setup_s = time.perf_counter() - t0
+    E_total = b.elements()
+    grids = b.tune()
+    plans = b.plans
+
+    def plain():
+        for h in plans:
+            L.check(lib.gfgpu_assemble(h, 2, L.WITH_VECTOR, None))
+    plain()
+    t_plain = _events_ms(plain, max(1, steps // 4))
+    t_batch = _events_ms(b.assemble, steps)
+    base = [c.clone() for c in coefs]
+    factor = torch.ones(1, dtype=torch.float64, device=dev)
+
+    def perturb():
+        for c, c0 in zip(coefs, base):
+            torch.mul(c0, factor, out=c)
+    graph = b.graph(pre=perturb)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 20
+    torch.cuda.synchronize()
+    e0.record()
+    for r in range(reps):
+        factor.fill_(1.0 + 0.01 * (r % 5))
+        graph.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    b.sync()
+    t_graph = e0.elapsed_time(e1) / reps
+    out = {"workload": f"{n_meshes} meshes, element counts log-uniform in [{lo:g}, {hi:g}], "
+                       "P1/P2 tri Poisson and P1/P2 tet elasticity, K + R per mesh",
+           "meshes": n_meshes, "elements": int(E_total), "setup_s": setup_s,
+           "grid_elem_pass": grids[0], "grid_gather": grids[1],
+           "ms_plain": t_plain, "ms_batched": t_batch, "ms_graph_replay": t_graph,
+           "elements_per_s_plain": E_total / (t_plain * 1e-3),
+           "elements_per_s_batched": E_total / (t_batch * 1e-3),
+           "elements_per_s_graph": E_total / (t_graph * 1e-3),
+           "batched_over_plain": t_plain / t_batch, "graph_over_plain": t_plain / t_graph,
+           "graph_replays": reps}
+    del b, wss, coefs, base, graph
+    gc.collect()
+    return out
+
+
+def bench_q4(steps):
+    """Q4 hexahedra 64^3 (262144 elements, 16.97 M DOFs), per-element
+    diffusivity lognormal(0, 0.5): assembled K + R, the matrix-free apply
+    R = K u (order-1 assembly, no K), and the adjoint of u^T K u in the
+    diffusivity (u i.i.d. N(0,1))."""
+    import gc
+    import torch
+    import getfem_gb300 as g
+    from getfem_gb300 import _lib as L
+    lib = L.lib()
+    rng = np.random.default_rng(5)
+    t0 = time.perf_counter()
+    mesh = g.Mesh.regular_unit(3, 64, "hex")
+    mf = g.MeshFem(mesh, 1, degree=4)
+    mim = g.MeshIm(mesh, "IM_GAUSS_PARALLELEPIPED(3,9)")
+    E = mesh.nb_convex()
+    dev = "cuda"
+    kappa = torch.tensor(np.exp(rng.normal(0, 0.5, E)), device=dev)
+    u = torch.tensor(rng.standard_normal(mf.nb_dof()), device=dev)
+    ws = g.GaWorkspace()
+    ws.add_fem_variable("u", mf, U=u)
+    ws.add_fem_constant("kappa", g.MeshFem(mesh, 1, degree=0), kappa)
+    ws.add_expression("kappa*Grad_u.Grad_u", mim)
+    grp = ws.groups[0]
+    h1 = ws._plan(grp, grp.order1)
+    ws._upload(h1, grp.order1, need_u=True)
+    h0 = ws._plan(grp, grp.order0)
+    ws._upload(h0, grp.order0, need_u=True)
+    L.check(lib.gfgpu_assemble(h1, 2, L.WITH_VECTOR, None))
+    L.check(lib.gfgpu_sync(h1))
+    setup_s = time.perf_counter() - t0
+    nr, nnz = C.c_int64(), C.c_int64()
+    L.check(lib.gfgpu_pattern_size(h1, C.byref(nr), C.byref(nnz)))
+    gk = torch.empty_like(kappa)
+    slot = ws.data["kappa"].slot
+
+    def kr():
+        L.check(lib.gfgpu_assemble(h1, 2, L.WITH_VECTOR, None))
+
+    def apply():
+        L.check(lib.gfgpu_assemble(h1, 1, 0, None))
+
+    def adj():
+        L.check(lib.gfgpu_potential_gradient(h0, slot, C.c_void_p(gk.data_ptr()), E, 1))
+    for f in (kr, apply, adj):
+        f()
+    t_kr = _events_ms(kr, steps)
+    t_ap = _events_ms(apply, steps)
+    t_adj = _events_ms(adj, steps)
+    out = {"workload": "Q4 hex 64^3 kappa*Grad_u.Grad_Test_u, IM_GAUSS_PARALLELEPIPED(3,9): "
+                       "K + R assembled, matrix-free R = K u, d(u^T K u)/dkappa",
+           "elements": E, "n_dof": mf.nb_dof(), "nnz": nnz.value, "setup_s": setup_s,
+           "ms_K_R": t_kr, "ms_matrix_free_apply": t_ap, "ms_adjoint_kappa": t_adj,
+           "elements_per_s_K_R": E / (t_kr * 1e-3),
+           "elements_per_s_apply": E / (t_ap * 1e-3),
+           "elements_per_s_K_R_adjoint": E / ((t_kr + t_adj) * 1e-3)}
+    del ws
+    gc.collect()
+    return out
+
+
+def bench_poisson_cg():
+    """64 x 64 P1 triangles, Grad_u.Grad_Test_u - f*Test_u, f U[-1,1],
+    homogeneous Dirichlet on the boundary: assembly + elimination + CG to
+    1e-12 (latency-bound: 4225 DOFs)."""
+    import torch
+    import getfem_gb300 as g
+    from getfem_gb300 import solvers
+    rng = np.random.default_rng(1)
+    mesh = g.Mesh.regular_unit(2, 64, "simplex")
+    mf = g.MeshFem(mesh, 1, degree=1)
+    ws = g.GaWorkspace()
+    ws.add_fem_variable("u", mf, U=np.zeros(mf.nb_dof()))
+    ws.add_fem_constant("f", mf, rng.uniform(-1, 1, mf.nb_dof()))
+    ws.add_expression("Grad_u.Grad_Test_u - f*Test_u", g.MeshIm(mesh, "IM_TRIANGLE(2)"))
+    dofs = solvers.boundary_dofs(mf)
+    solvers.solve_linear(ws, dofs)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    u, info = solvers.solve_linear(ws, dofs)
+    torch.cuda.synchronize()
+    return {"workload": "64x64 P1 triangles Poisson, boundary Dirichlet, CG (identity) to 1e-12",
+            "elements": mesh.nb_convex(), "n_dof": mf.nb_dof(),
+            "ms_assemble_and_solve": 1e3 * (time.perf_counter() - t0),
+            "cg_iterations": info["iterations"], "relative_residual": info["residual"]}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -184,6 +451,8 @@ def main():
     ap.add_argument("--ref-nx", type=int, default=12)
     ap.add_argument("--cpu-nx", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the secondary workloads (neo-Hookean, batched, Q4, CG)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -339,6 +608,27 @@ def main():
                 "d2h_bytes_per_step": 8 * nnz + 8 * mf.nb_dof(), "ms_per_step": e2e_ms},
         "gpu_launches": int(launches), "cpu_baseline": cpu, "clocks": sampler.summary(),
     }
+    if not args.no_extra and world == 1:
+        del ws
+        import gc
+        gc.collect()
+        extra = {}
+        for name, fn in (("poisson_cg", bench_poisson_cg),
+                         ("neohookean_q2_hex", lambda: bench_neohookean(10)),
+                         ("batched_512_meshes", lambda: bench_batched(10)),
+                         ("batched_small_meshes", lambda: bench_batched(
+                             10, n_meshes=4096, lo=1e2, hi=2e3)),
+                         ("q4_hex_laplacian", lambda: bench_q4(5))):
+            free0 = torch.cuda.mem_get_info()[0]
+            try:
+                extra[name] = fn()
+            except Exception as exc:  # reported, not hidden
+                extra[name] = {"error": f"{type(exc).__name__}: {exc}"}
+            gc.collect()
+            torch.cuda.synchronize()
+            torch.cuda.empty_cache()
+            extra[name]["device_free_gb_before"] = free0 / 1e9
+        line["secondary"] = extra
     print(json.dumps(line), flush=True)
 
 

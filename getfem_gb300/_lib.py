@@ -86,6 +86,10 @@ _PROTOS = {
                                           C.c_void_p, C.c_void_p]),
     "gfgpu_enumerate_dofs": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int64,
                                        C.c_void_p, C.c_void_p, C.POINTER(C.c_int64)]),
+    "gfgpu_enumerate_dofs_device": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                              C.c_int64, C.c_void_p, C.c_void_p,
+                                              C.POINTER(C.c_int64)]),
+    "gfgpu_device_available": (C.c_int, []),
     "gfgpu_nb_basis": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int32)]),
     "gfgpu_quadrature": (C.c_int, [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                    C.c_void_p, C.c_void_p]),

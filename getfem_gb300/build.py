@@ -21,7 +21,7 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 HOST_SOURCES = ["host/refelem.cc", "gfgpu_host.cc"]
 CUDA_SOURCES = ["gfgpu_api.cu", "k_simplex.cu", "k_assemble.cu", "k_probe.cu", "k_noalloc.cu",
                 "k_hex.cu", "k_gauss.cu", "k_affine_hex.cu",
-                "k_solve.cu"]
+                "k_solve.cu", "k_dofs.cu"]
 # per-file nvcc flags: the Gauss-point kernels round like the reference's
 # sequence of products and sums (no implicit contraction; explicit fma only)
 CUDA_FLAGS = {"k_hex.cu": ["-fmad=false"], "k_gauss.cu": ["-fmad=false"]}

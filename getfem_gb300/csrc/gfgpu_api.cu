@@ -58,7 +58,12 @@ template <class T>
 int dalloc(T **p, size_t n) {
   *p = nullptr;
   if (n == 0) n = 1;
-  GF_CUDA(cudaMalloc(reinterpret_cast<void **>(p), n * sizeof(T)));
+  const cudaError_t ce = cudaMalloc(reinterpret_cast<void **>(p), n * sizeof(T));
+  if (ce != cudaSuccess) {
+    set_last_error("cudaMalloc of " + std::to_string(n * sizeof(T)) + " bytes: " +
+                   cudaGetErrorString(ce));
+    return ce == cudaErrorMemoryAllocation ? GFGPU_E_NOMEM : GFGPU_E_CUDA;
+  }
   return GFGPU_OK;
 }
 
@@ -180,14 +185,15 @@ int status_from_err(int e) {
 }
 
 int build_pattern(Plan &P) {
-  // counts per row and per node
+  // counts per row and per node (int64: the scans accumulate in the input
+  // type, and the node-level total passes 2^31 on large meshes)
   GF_CUDA(cudaMemsetAsync(P.d_count, 0, (P.n_dof + 1) * sizeof(int64_t), P.stream));
-  GF_CUDA(cudaMemsetAsync(P.d_ncount, 0, (P.n_nodes + 1) * sizeof(int32_t), P.stream));
+  GF_CUDA(cudaMemsetAsync(P.d_ncount, 0, (P.n_nodes + 1) * sizeof(int64_t), P.stream));
   GF_CUDA(launch_pattern_count(P));
   size_t need = 0, need2 = 0, need3 = 0;
   cub::DeviceScan::ExclusiveSum(nullptr, need, P.d_count, P.d_rowptr, P.n_dof + 1);
   cub::DeviceScan::ExclusiveSum(nullptr, need2, P.d_ncount, P.d_nptr, P.n_nodes + 1);
-  int32_t *d_max = nullptr;
+  int64_t *d_max = nullptr;
   cub::DeviceReduce::Max(nullptr, need3, P.d_ncount, d_max, P.n_nodes + 1);
   need = std::max(need, std::max(need2, need3 + 16));
   if (need > P.cub_bytes) {
@@ -206,11 +212,11 @@ int build_pattern(Plan &P) {
   GF_CUDA(cudaMemcpyAsync(&nn, P.d_nptr + P.n_nodes, sizeof(int64_t), cudaMemcpyDeviceToHost,
                           P.stream));
   // max slots per node
-  int32_t *d_mx = reinterpret_cast<int32_t *>(P.d_count);  // reuse: counts are consumed
+  int64_t *d_mx = P.d_count;  // reuse: counts are consumed
   GF_CUDA(cub::DeviceReduce::Max(P.d_cub, P.cub_bytes, P.d_ncount, d_mx, P.n_nodes + 1, P.stream));
   P.launches++;
-  int32_t mx = 0;
-  GF_CUDA(cudaMemcpyAsync(&mx, d_mx, sizeof(int32_t), cudaMemcpyDeviceToHost, P.stream));
+  int64_t mx64 = 0;
+  GF_CUDA(cudaMemcpyAsync(&mx64, d_mx, sizeof(int64_t), cudaMemcpyDeviceToHost, P.stream));
   GF_CUDA(cudaStreamSynchronize(P.stream));
   int herr = 0;
   GF_CUDA(cudaMemcpy(&herr, P.d_err, sizeof(int), cudaMemcpyDeviceToHost));
@@ -227,8 +233,11 @@ int build_pattern(Plan &P) {
   if ((rc = dalloc(&P.d_nbits, size_t(nn)))) return rc;
   if ((rc = dalloc(&P.d_slotmap, size_t(P.n_elements) * P.nb * P.nb))) return rc;
   P.nnz = nnz;
-  P.max_slots = mx;
+  P.max_slots = int32_t(mx64);
   GF_CUDA(launch_pattern_fill(P));
+  // the node-level column lists only feed the fill
+  GF_CUDA(cudaStreamSynchronize(P.stream));
+  dfree(P.d_ncol);
   return GFGPU_OK;
 }
 
@@ -376,7 +385,7 @@ int gfgpu_plan_create(const gfgpu_space *space, const gfgpu_form *form, void *cu
     CHK(dalloc(&P->d_adj_ptr, aptr.size()));
     CHK(dalloc(&P->d_adj, adj.size()));
     CHK(dalloc(&P->d_stab, 1));
-    if (P->kmat) CHK(dalloc(&P->d_elem, size_t(E * P->lay.stride)));
+
     CHK(dalloc(&P->d_vec, size_t(S.n_dof)));
     CHK(dalloc(&P->d_pot, 1));
     CHK(dalloc(&P->d_err, 1));
@@ -550,6 +559,8 @@ int gfgpu_assemble(gfgpu_plan *P, int32_t order, int32_t flags, double *potentia
   const bool want_R = order == 1 || (flags & 2);
   int rc = check_slots(*P, want_R || P->law == LAW_NH);
   if (rc) return rc;
+  // element scratch, allocated at the first order-1 or order-2 assembly
+  if (!P->d_elem && (rc = dalloc(&P->d_elem, size_t(P->n_elements) * P->lay.stride))) return rc;
   const bool prof = (flags & GFGPU_PROFILE) != 0;
   if (prof && !P->ev[0])
     for (int i = 0; i < 4; ++i) GF_CUDA(cudaEventCreate(&P->ev[i]));
@@ -706,7 +717,6 @@ int gfgpu_batch_create(gfgpu_plan *const *plans, int32_t n, gfgpu_batch **out) {
     it.ms = P.max_slots < 1 ? 1 : P.max_slots;
     it.mad = P.max_adj < 1 ? 1 : P.max_adj;
     it.nptr = P.d_nptr;
-    it.ncol = P.d_ncol;
     it.nbits = P.d_nbits;
     it.slotmap = P.d_slotmap;
     it.rowptr = P.d_rowptr;

@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(128) pattern_kernel(
     int64_t n_nodes, KeLayout L, const int32_t *__restrict__ adj_ptr,
     const int32_t *__restrict__ adj, const int32_t *__restrict__ enode,
     const double *__restrict__ elem, int cap, int64_t *__restrict__ rowcount,
-    int32_t *__restrict__ ncount, const int64_t *__restrict__ rowptr,
+    int64_t *__restrict__ ncount, const int64_t *__restrict__ rowptr,
     int32_t *__restrict__ colidx, const int64_t *__restrict__ nptr, int32_t *__restrict__ ncol,
     uint16_t *__restrict__ nbits, int16_t *__restrict__ slotmap, int *__restrict__ err) {
   extern __shared__ int smem[];

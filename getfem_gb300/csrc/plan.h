@@ -126,7 +126,7 @@ struct Plan {
   double *d_pot = nullptr;      // 1
   int *d_err = nullptr;
   int64_t *d_count = nullptr;   // scratch row counts (n_dof + 1)
-  int32_t *d_ncount = nullptr;  // (n_nodes)
+  int64_t *d_ncount = nullptr;  // (n_nodes + 1)
   void *d_cub = nullptr;
   size_t cub_bytes = 0;
   int64_t launches = 0;
@@ -154,7 +154,6 @@ struct BatchItem {
   const int32_t *adj_ptr = nullptr, *adj = nullptr;
   int32_t ms = 1, mad = 1;
   const int64_t *nptr = nullptr;
-  const int32_t *ncol = nullptr;
   const uint16_t *nbits = nullptr;
   const int16_t *slotmap = nullptr;
   const int64_t *rowptr = nullptr;

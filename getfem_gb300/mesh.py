@@ -99,9 +99,14 @@ class MeshFem:
         self.nb = nb.value
         dofs = np.empty((self.mesh.nb_convex(), self.nb), dtype=np.int64)
         nd = C.c_int64()
-        L.check(lib.gfgpu_enumerate_dofs(self.mesh.dim, self.mesh.kind, self.degree, self.qdim,
-                                         self.mesh.nb_convex(), _ptr(self.mesh.cvpts),
-                                         _ptr(dofs), C.byref(nd)))
+        # the device numbering (a sort of node keys) where a GPU is visible
+        # and the element fits its keys; the host numbering otherwise (the
+        # two are identical, tests/test_gpu_dofs.py)
+        on_dev = (self.degree >= 1 and self.degree <= 4 and lib.gfgpu_device_available()
+                  and self.mesh.nb_points() < (1 << 25))
+        enum = lib.gfgpu_enumerate_dofs_device if on_dev else lib.gfgpu_enumerate_dofs
+        L.check(enum(self.mesh.dim, self.mesh.kind, self.degree, self.qdim,
+                     self.mesh.nb_convex(), _ptr(self.mesh.cvpts), _ptr(dofs), C.byref(nd)))
         self.dofs = dofs
         self._nb_dof = nd.value
         return self

@@ -146,6 +146,14 @@ int gfgpu_regular_unit_mesh(int32_t dim, int32_t kind, int32_t nx, const double 
 int gfgpu_enumerate_dofs(int32_t dim, int32_t kind, int32_t degree, int32_t qdim,
                          int64_t n_elements, const int64_t *cvpts,
                          int64_t *dofs, int64_t *n_dof);
+/* The same numbering computed on the device (sort of packed node keys;
+   meshes of fewer than 2^25 vertices and 2^32 element nodes, degree <= 4):
+   host arrays in and out, same results as gfgpu_enumerate_dofs. */
+int gfgpu_enumerate_dofs_device(int32_t dim, int32_t kind, int32_t degree, int32_t qdim,
+                                int64_t n_elements, const int64_t *cvpts,
+                                int64_t *dofs, int64_t *n_dof);
+/* 1 when a CUDA device is visible, else 0. */
+int gfgpu_device_available(void);
 
 /* Number of local scalar basis functions of FEM_PK/QK(dim,degree). */
 int gfgpu_nb_basis(int32_t dim, int32_t kind, int32_t degree, int32_t *nb);
