@@ -10,6 +10,7 @@ from .mesh import Mesh, MeshFem, MeshIm  # noqa: F401
 from .workspace import GaWorkspace  # noqa: F401
 from .adjoint import Potential  # noqa: F401
 from . import solvers  # noqa: F401
+from .asm import asm_generic  # noqa: F401
 
-__all__ = ["GaWorkspace", "Mesh", "MeshFem", "MeshIm", "Potential", "GfgpuError",
-           "UnsupportedExpression"]
+__all__ = ["GaWorkspace", "Mesh", "MeshFem", "MeshIm", "Potential", "asm_generic",
+           "GfgpuError", "UnsupportedExpression"]
