@@ -240,6 +240,8 @@ void build_affine_hex_tables(Plan &P) {
   P.lay.off_vec = s * P.lay.rowstride;
   P.lay.off_thr = P.lay.off_vec + P.lay.rowstride;
   P.lay.stride = P.lay.off_thr + 4;
+  P.lay.blk = 0;
+  P.lay.rowblk = P.lay.rowstride;
   P.lay.linear = true;
 }
 

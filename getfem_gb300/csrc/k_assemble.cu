@@ -85,7 +85,8 @@ __global__ void __launch_bounds__(128) pattern_kernel(
       const int lj = c / qd, b = c % qd;
       unsigned m = 0u;
       for (int a = 0; a < qd; ++a)
-        if (abs_greater(Ke[(li * qd + a) * L.rowstride + c], thr)) m |= 1u << (a * qd + b);
+        if (abs_greater(Ke[int64_t(li) * L.rowblk + ke_in_rowblk(L, a, c)], thr))
+          m |= 1u << (a * qd + b);
       if (m) atomicOr(&bits[ljs[lj]], m);
     }
     __syncwarp();
@@ -161,16 +162,18 @@ __global__ void __launch_bounds__(128) pattern_kernel(
 
 // -------------------------------------------------------------- gather
 
-__host__ __device__ __forceinline__ size_t gather_warp_bytes(int ms, int qd, int rowstride,
+constexpr int kGatherBufs = 2;  // row blocks per warp: the current one and the next
+
+__host__ __device__ __forceinline__ size_t gather_warp_bytes(int ms, int qd, int rowblk,
                                                              int mad) {
-  const size_t b = size_t(2 * qd * rowstride) * 8 + size_t(ms) * qd * qd * 8 +
-                   size_t(mad) * 4 + size_t(ms) * 2;
+  const size_t b = size_t(kGatherBufs * rowblk) * 8 + size_t(ms) * qd * qd * 8 +
+                   size_t(mad) * 8 + size_t(ms) * 2;
   return (b + 15) / 16 * 16;
 }
 
 // The row gather of one DOF node by one warp (QD components, R =
 // ceil(nb*qd/32) lane rounds over the columns of a row); `base` is the
-// warp's shared-memory area of gather_warp_bytes(ms, QD, rowstride, mad).
+// warp's shared-memory area of gather_warp_bytes(ms, QD, rowblk, mad).
 template <int QD, int R>
 __device__ __forceinline__ void gather_node(
     char *base, int64_t node, const KeLayout &L, const int32_t *__restrict__ adj_ptr,
@@ -181,11 +184,12 @@ __device__ __forceinline__ void gather_node(
     int *__restrict__ err) {
   constexpr int QQ = QD * QD;
   const int lane = threadIdx.x & 31;
-  const int nb = L.nb, S = L.s, rs = L.rowstride, blk = QD * rs;
-  double *Kbuf = reinterpret_cast<double *>(base);                // 2 x blk
-  double *acc = Kbuf + 2 * blk;                                    // ms * QQ
+  const int nb = L.nb, S = L.s, blk = L.rowblk;
+  double *Kbuf = reinterpret_cast<double *>(base);                // kGatherBufs x blk
+  double *acc = Kbuf + kGatherBufs * blk;                          // ms * QQ
   int *adjs = reinterpret_cast<int *>(acc + size_t(ms) * QQ);     // mad
-  uint16_t *bits = reinterpret_cast<uint16_t *>(adjs + mad);      // ms
+  int *adjl = adjs + mad;                                          // mad
+  uint16_t *bits = reinterpret_cast<uint16_t *>(adjl + mad);      // ms
   const int64_t s0 = nptr[node];
   const int ns = int(nptr[node + 1] - s0);
   const int a0 = adj_ptr[node], nadj = adj_ptr[node + 1] - a0;
@@ -193,7 +197,13 @@ __device__ __forceinline__ void gather_node(
     if (lane == 0) set_err(err, ERR_CAPACITY);
     return;
   }
-  for (int j = lane; j < nadj; j += kWarp) adjs[j] = adj[a0 + j];
+  // adjacency codes e*nb + li, split once (lane-parallel): adjs[j] = e,
+  // adjl[j] = li
+  for (int j = lane; j < nadj; j += kWarp) {
+    const int code = adj[a0 + j];
+    adjs[j] = code / nb;
+    adjl[j] = code - (code / nb) * nb;
+  }
   if (want_K) {
     for (int j = lane; j < ns * QQ; j += kWarp) acc[j] = 0.0;
     for (int j = lane; j < ns; j += kWarp) bits[j] = nbits[s0 + j];
@@ -201,20 +211,14 @@ __device__ __forceinline__ void gather_node(
   __syncwarp();
   const int nchunk = blk / 2;  // 16-byte chunks of the row block
   auto issue = [&](int k) {
-    const int code = adjs[k];
-    const double *src = elem + int64_t(code / nb) * L.stride + int64_t(code % nb) * blk;
-    double *dst = Kbuf + (k & 1) * blk;
+    const double *src = elem + int64_t(adjs[k]) * L.stride + int64_t(adjl[k]) * blk;
+    double *dst = Kbuf + (k % kGatherBufs) * blk;
     for (int c = lane; c < nchunk; c += kWarp) cp_async16(dst + 2 * c, src + 2 * c);
   };
   // per-lane data of an element: slots of the columns the lane handles,
   // threshold, and the element vector entry of component `lane`
-  int sl[R];
-#pragma unroll
-  for (int r = 0; r < R; ++r) sl[r] = -1;
-  double thr_d = 0.0, ve = 0.0;
   auto fetch = [&](int k, int (&s_)[R], double &t_, double &v_) {
-    const int code = adjs[k];
-    const int el = code / nb, li = code % nb;
+    const int el = adjs[k], li = adjl[k];
     const double *Ke = elem + int64_t(el) * L.stride;
 #pragma unroll
     for (int r = 0; r < R; ++r) {
@@ -224,45 +228,54 @@ __device__ __forceinline__ void gather_node(
     t_ = Ke[L.off_thr];
     v_ = (want_R && lane < QD) ? Ke[L.off_vec + li * QD + lane] : 0.0;
   };
+  // two stages: element k is processed while k+1 is in flight
+  int sl0[R];
+  double thr0 = 0.0, ve0 = 0.0;
+#pragma unroll
+  for (int r = 0; r < R; ++r) sl0[r] = -1;
   if (nadj > 0) {
     if (want_K) issue(0);
-    fetch(0, sl, thr_d, ve);
+    fetch(0, sl0, thr0, ve0);
   }
   cp_async_commit();
   double rvec = 0.0;
   for (int k = 0; k < nadj; ++k) {
-    int sl_n[R];
-    double thr_n = 0.0, ve_n = 0.0;
+    int sl1[R];
+    double thr1 = 0.0, ve1 = 0.0;
+#pragma unroll
+    for (int r = 0; r < R; ++r) sl1[r] = -1;
     if (k + 1 < nadj) {
       if (want_K) issue(k + 1);
-      fetch(k + 1, sl_n, thr_n, ve_n);
+      fetch(k + 1, sl1, thr1, ve1);
     }
     cp_async_commit();
-    cp_async_wait1();
+    cp_async_wait1();  // the group of element k is complete
     __syncwarp();
-    rvec += ve;
+    rvec += ve0;
     if (want_K) {
-      const double *Kb = Kbuf + (k & 1) * blk;
-      const long long tb = __double_as_longlong(thr_d);
+      const double *Kb = Kbuf + (k % kGatherBufs) * blk;
+      const long long tb = __double_as_longlong(thr0);
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         const int c = lane + 32 * r;
-        if (c < S && sl[r] >= 0) {
+        if (c < S && sl0[r] >= 0) {
           const int b = c % QD;
-          const unsigned sb = bits[sl[r]];
+          const unsigned sb = bits[sl0[r]];
+          const int c0 = L.blk ? (c / QD) * L.blk + b : c;
+          const int cstep = L.blk ? QD : L.rowstride;
 #pragma unroll
           for (int a = 0; a < QD; ++a) {
-            const double x = Kb[a * rs + c];
+            const double x = Kb[c0 + a * cstep];
             if (((sb >> (a * QD + b)) & 1u) && abs_greater(x, tb))
-              acc[(sl[r] * QD + a) * QD + b] += x;
+              acc[(sl0[r] * QD + a) * QD + b] += x;
           }
         }
       }
     }
     __syncwarp();
 #pragma unroll
-    for (int r = 0; r < R; ++r) sl[r] = sl_n[r];
-    thr_d = thr_n, ve = ve_n;
+    for (int r = 0; r < R; ++r) sl0[r] = sl1[r];
+    thr0 = thr1, ve0 = ve1;
   }
   if (want_K) {
 #pragma unroll
@@ -309,7 +322,7 @@ __global__ void __launch_bounds__(128) gather_kernel(
     int *__restrict__ err) {
   extern __shared__ __align__(16) double dsm[];
   const int wib = threadIdx.x >> 5;
-  char *base = reinterpret_cast<char *>(dsm) + wib * gather_warp_bytes(ms, QD, L.rowstride, mad);
+  char *base = reinterpret_cast<char *>(dsm) + wib * gather_warp_bytes(ms, QD, L.rowblk, mad);
   const int64_t node = blockIdx.x * int64_t(blockDim.x >> 5) + wib;
   if (node >= n_nodes) return;
   gather_node<QD, R>(base, node, L, adj_ptr, adj, elem, ms, mad, nptr, nbits, slotmap, rowptr,
@@ -355,7 +368,7 @@ template <int QD, int R>
 cudaError_t launch_gather_t(Plan &P, bool want_K, bool want_R) {
   const int ms = P.max_slots < 1 ? 1 : P.max_slots;
   const int mad = P.max_adj < 1 ? 1 : P.max_adj;
-  const size_t smem = size_t(kWarpsPerBlock) * gather_warp_bytes(ms, QD, P.lay.rowstride, mad);
+  const size_t smem = size_t(kWarpsPerBlock) * gather_warp_bytes(ms, QD, P.lay.rowblk, mad);
   cudaError_t ce = cudaFuncSetAttribute(gather_kernel<QD, R>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
   if (ce != cudaSuccess) return ce;
@@ -410,7 +423,7 @@ cudaError_t launch_pattern_fill(Plan &P) {
 }
 
 size_t batch_gather_warp_bytes(const BatchItem &it) {
-  return gather_warp_bytes(it.ms, it.qd, it.L.rowstride, it.mad);
+  return gather_warp_bytes(it.ms, it.qd, it.L.rowblk, it.mad);
 }
 
 cudaError_t launch_batch_gather(const BatchItem *items, const int64_t *node0, int nitems,

@@ -488,6 +488,8 @@ void gauss_element_layout(Plan &P) {
   P.lay.off_vec = s * P.lay.rowstride;
   P.lay.off_thr = P.lay.off_vec + P.lay.rowstride;
   P.lay.stride = P.lay.off_thr + 4;
+  P.lay.blk = 0;
+  P.lay.rowblk = P.qdim * P.lay.rowstride;
   P.lay.linear = P.law != LAW_NH;
   // upper-triangle entries (r << 16 | c), row-major
   P.h_tri.clear();

@@ -45,6 +45,33 @@ constexpr int kEpThreads = 32 * kEpWarps;
 
 }  // namespace
 
+// Supports of the nodes of FEM_PK(DIM,K), K <= 2, in GetFEM's node order
+// (lattice points, first coordinate fastest): the barycentric vertices with a
+// nonzero weight, ascending.  The reference-tensor terms of a node pair (i,j)
+// are supp(i) x supp(j) in this order (checked against the host tables).
+__host__ __device__ constexpr int pk_sup_n(int dim, int nb, int i) {
+  if (nb == dim + 1) return 1;  // P1: node i is vertex i
+  // P2: vertices are the nodes with a single weight
+  if (dim == 2) return (i == 0 || i == 2 || i == 5) ? 1 : 2;
+  return (i == 0 || i == 2 || i == 5 || i == 9) ? 1 : 2;
+}
+__host__ __device__ constexpr int pk_sup_v(int dim, int nb, int i, int t) {
+  if (nb == dim + 1) return i;
+  // P2 triangle: (0),(0,1),(1),(0,2),(1,2),(2); tetrahedron adds (0,3),(1,3),(2,3),(3)
+  switch (i) {
+    case 0: return 0;
+    case 1: return t == 0 ? 0 : 1;
+    case 2: return 1;
+    case 3: return t == 0 ? 0 : 2;
+    case 4: return t == 0 ? 1 : 2;
+    case 5: return 2;
+    case 6: return t == 0 ? 0 : 3;
+    case 7: return t == 0 ? 1 : 3;
+    case 8: return t == 0 ? 2 : 3;
+    default: return 3;
+  }
+}
+
 // Shared memory of one 32-element tile of the simplex element pass.
 template <int DIM, int QD, int NB>
 struct EpShared {
@@ -54,8 +81,13 @@ struct EpShared {
   double s_gval[NB * NB * kMaxPairTerms];
   double s_mass[NB * NB];
   double Gs[NG][32];     // geometry of the tile's 32 elements
-  double Tp[NTP][32];    // upper triangle of T per element
-  double Us[S][32];      // u at the element's DOFs
+  union {
+    struct {
+      double Tp[NTP][32];  // upper triangle of T per element
+      double Us[S][32];    // u at the element's DOFs
+    } a;                   // while the blocks of K_e are built
+    double Rs[kEpWarps][S][32];  // then: each warp's part of R_e
+  } x;
   long long mxs[kEpWarps][32];
   int8_t s_nterm[NB * NB];
   int8_t s_vw[NB * NB * kMaxPairTerms];
@@ -78,9 +110,10 @@ __device__ __forceinline__ void simplex_element_tile(
   auto &s_gval = sh.s_gval;
   auto &s_mass = sh.s_mass;
   auto &Gs = sh.Gs;
-  auto &Tp = sh.Tp;
+  auto &Tp = sh.x.a.Tp;
   auto &mxs = sh.mxs;
-  auto &Us = sh.Us;
+  auto &Us = sh.x.a.Us;
+  auto &Rs = sh.x.Rs;
   for (int k = threadIdx.x; k < NB * NB; k += blockDim.x) {
     s_nterm[k] = tab->nterm[k];
     s_mass[k] = tab->mass[k];
@@ -196,10 +229,7 @@ __device__ __forceinline__ void simplex_element_tile(
       }
   }
   __syncthreads();
-  // ---- warp w: rows r = w, w + 4, ... of every element of the block.
-  // Row (i,a) is built in registers, multiplied into R_e = K_e u_e + V (no
-  // threshold, as the reference's vector assembly) and written with 32-byte
-  // stores that fill whole sectors.
+  // ---- u at the element's DOFs
   for (int j = wid; j < NB; j += kEpWarps) {
     const int nd = active ? __ldg(enode + e * NB + j) : 0;
 #pragma unroll
@@ -210,63 +240,148 @@ __device__ __forceinline__ void simplex_element_tile(
   const double cm = Gs[NV * DIM + 3][lane], jf = Gs[NV * DIM + 4][lane] * fscale;
   double *o = out + e * L.stride;
   long long mx = 0;
-  for (int r = wid; r < S; r += kEpWarps) {
-    const int i = r / QD, a = r % QD;
-    double row[RS];
+  // load term of row r = (i,a): scale |J| sum_j M[i,j] f[(j,a)]
+  auto load_of = [&](int i, int a) -> double {
+    if (!(fsrc && active)) return 0.0;
+    double s = 0.0;
 #pragma unroll
     for (int j = 0; j < NB; ++j) {
-      const int pij = i * NB + j;
-      const int nt = s_nterm[pij];
-      const double mij = MASS ? cm * s_mass[pij] : 0.0;
+      const int nd = __ldg(enode + e * NB + j);
+      s += s_mass[i * NB + j] * __ldg(fsrc + int64_t(nd) * QD + a);
+    }
+    return jf * s;
+  };
+  // T[(a,v),(b,w)] from its upper triangle
+  auto tp = [&](int a, int v, int b, int w) -> double {
+    int p = a * NV + v, q = b * NV + w;
+    if (p > q) {
+      const int t = p;
+      p = q;
+      q = t;
+    }
+    return Tp[p * M - (p * (p - 1)) / 2 + (q - p)][lane];
+  };
+  if constexpr (QD == 1) {
+    // ---- scalar fields: warp w builds rows r = w, w + 4, ... in registers,
+    // adds each into R_e = K_e u_e (no threshold, as the reference's vector
+    // assembly) and writes it with 32-byte stores
+    for (int r = wid; r < S; r += kEpWarps) {
+      const int i = r;
+      double row[RS];
 #pragma unroll
-      for (int b = 0; b < QD; ++b) row[j * QD + b] = (MASS && a == b) ? mij : 0.0;
-      for (int t = 0; t < nt; ++t) {
-        const int vw = s_vw[pij * kMaxPairTerms + t];
-        const int v = vw / NV, w = vw % NV;
-        const double gv = s_gval[pij * kMaxPairTerms + t];
+      for (int j = 0; j < NB; ++j) {
+        const int pij = i * NB + j;
+        double x = MASS ? cm * s_mass[pij] : 0.0;
+        const int ni = pk_sup_n(DIM, NB, i), nj = pk_sup_n(DIM, NB, j);
 #pragma unroll
-        for (int b = 0; b < QD; ++b) {
-          int p = a * NV + v, q = b * NV + w;
-          if (p > q) {
-            const int tmp = p;
-            p = q;
-            q = tmp;
+        for (int ti = 0; ti < 2; ++ti)
+#pragma unroll
+          for (int tj = 0; tj < 2; ++tj)
+            if (ti < ni && tj < nj)
+              x += s_gval[pij * kMaxPairTerms + ti * nj + tj] *
+                 tp(0, pk_sup_v(DIM, NB, i, ti), 0, pk_sup_v(DIM, NB, j, tj));
+        row[j] = x;
+      }
+#pragma unroll
+      for (int c = S; c < RS; ++c) row[c] = 0.0;
+      double rv = load_of(i, 0);
+#pragma unroll
+      for (int c = 0; c < S; ++c) {
+        rv += row[c] * Us[c][lane];
+        const long long bitsv = __double_as_longlong(row[c]) & 0x7fffffffffffffffLL;
+        mx = bitsv > mx ? bitsv : mx;
+      }
+      if (active) {
+        if (STORE_K) {
+          double4_32a *dst = reinterpret_cast<double4_32a *>(o + r * RS);
+#pragma unroll
+          for (int c = 0; c < RS; c += 4)
+            dst[c / 4] = make_double4_32a(row[c], row[c + 1], row[c + 2], row[c + 3]);
+        }
+        o[L.off_vec + r] = rv;
+      }
+    }
+    mxs[wid][lane] = mx;
+    __syncthreads();
+  } else {
+    // ---- vector fields: node pairs (i <= j) dealt round-robin to the 4
+    // warps.  K_e is symmetric (G[i,j,v,w] = G[j,i,w,v], T symmetric), so
+    // the block K_e[(i,.),(j,.)] = sum_t g_t T[(.,v_t),(.,w_t)] (+ mass) is
+    // computed once and stored with its transpose as whole 32-byte sectors
+    // (node-block layout); each warp accumulates its blocks' part of
+    // R_e = K_e u_e in registers, and the parts are summed in warp order.
+    constexpr int BLK = QD == 2 ? 4 : 12;
+    double Rp[S];
+#pragma unroll
+    for (int c = 0; c < S; ++c) Rp[c] = 0.0;
+    int pidx = 0;
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+#pragma unroll
+      for (int j = i; j < NB; ++j, ++pidx) {
+        if (pidx % kEpWarps != wid) continue;  // warp-uniform
+        const int pij = i * NB + j;
+        const double mij = MASS ? cm * s_mass[pij] : 0.0;
+        double B[QD][QD];
+#pragma unroll
+        for (int a = 0; a < QD; ++a)
+#pragma unroll
+          for (int b = 0; b < QD; ++b) B[a][b] = (MASS && a == b) ? mij : 0.0;
+        const int ni = pk_sup_n(DIM, NB, i), nj = pk_sup_n(DIM, NB, j);
+#pragma unroll
+        for (int ti = 0; ti < 2; ++ti) {
+          if (ti >= ni) continue;
+#pragma unroll
+          for (int tj = 0; tj < 2; ++tj) {
+            if (tj >= nj) continue;
+            const int v = pk_sup_v(DIM, NB, i, ti), w = pk_sup_v(DIM, NB, j, tj);
+            const double gv = s_gval[pij * kMaxPairTerms + ti * nj + tj];
+#pragma unroll
+            for (int a = 0; a < QD; ++a)
+#pragma unroll
+              for (int b = 0; b < QD; ++b) B[a][b] += gv * tp(a, v, b, w);
           }
-          row[j * QD + b] += gv * Tp[p * M - (p * (p - 1)) / 2 + (q - p)][lane];
+        }
+#pragma unroll
+        for (int a = 0; a < QD; ++a)
+#pragma unroll
+          for (int b = 0; b < QD; ++b) {
+            Rp[i * QD + a] += B[a][b] * Us[j * QD + b][lane];
+            if (i != j) Rp[j * QD + b] += B[a][b] * Us[i * QD + a][lane];
+            const long long bitsv = __double_as_longlong(B[a][b]) & 0x7fffffffffffffffLL;
+            mx = bitsv > mx ? bitsv : mx;
+          }
+        if (STORE_K && active) {
+          double4_32a *dij = reinterpret_cast<double4_32a *>(o + (i * NB + j) * BLK);
+          double4_32a *dji = reinterpret_cast<double4_32a *>(o + (j * NB + i) * BLK);
+          if constexpr (QD == 2) {
+            dij[0] = make_double4_32a(B[0][0], B[0][1], B[1][0], B[1][1]);
+            if (i != j) dji[0] = make_double4_32a(B[0][0], B[1][0], B[0][1], B[1][1]);
+          } else {
+            dij[0] = make_double4_32a(B[0][0], B[0][1], B[0][2], B[1][0]);
+            dij[1] = make_double4_32a(B[1][1], B[1][2], B[2][0], B[2][1]);
+            dij[2] = make_double4_32a(B[2][2], 0.0, 0.0, 0.0);
+            if (i != j) {
+              dji[0] = make_double4_32a(B[0][0], B[1][0], B[2][0], B[0][1]);
+              dji[1] = make_double4_32a(B[1][1], B[2][1], B[0][2], B[1][2]);
+              dji[2] = make_double4_32a(B[2][2], 0.0, 0.0, 0.0);
+            }
+          }
         }
       }
     }
+    mxs[wid][lane] = mx;
+    __syncthreads();  // every warp is done with T and u
 #pragma unroll
-    for (int c = S; c < RS; ++c) row[c] = 0.0;
-    // load term: scale |J| sum_j M[i,j] f[(j,a)]
-    double rv = 0.0;
-    if (fsrc && active) {
-      double s = 0.0;
+    for (int c = 0; c < S; ++c) Rs[wid][c][lane] = Rp[c];
+    __syncthreads();
+    for (int r = wid; r < S; r += kEpWarps) {
+      double rv = load_of(r / QD, r % QD);
 #pragma unroll
-      for (int j = 0; j < NB; ++j) {
-        const int nd = __ldg(enode + e * NB + j);
-        s += s_mass[i * NB + j] * __ldg(fsrc + int64_t(nd) * QD + a);
-      }
-      rv = jf * s;
-    }
-#pragma unroll
-    for (int c = 0; c < S; ++c) {
-      rv += row[c] * Us[c][lane];
-      const long long bitsv = __double_as_longlong(row[c]) & 0x7fffffffffffffffLL;
-      mx = bitsv > mx ? bitsv : mx;
-    }
-    if (active) {
-      if (STORE_K) {
-        double4 *dst = reinterpret_cast<double4 *>(o + r * RS);
-#pragma unroll
-        for (int c = 0; c < RS; c += 4)
-          dst[c / 4] = make_double4(row[c], row[c + 1], row[c + 2], row[c + 3]);
-      }
-      o[L.off_vec + r] = rv;
+      for (int k = 0; k < kEpWarps; ++k) rv += Rs[k][r][lane];
+      if (active) o[L.off_vec + r] = rv;
     }
   }
-  mxs[wid][lane] = mx;
-  __syncthreads();
   if (wid == 0 && active) {
     long long m = mxs[0][lane];
 #pragma unroll
@@ -371,6 +486,17 @@ int fill_simplex_tables(int dim, int K, int qdim, const std::string &im, Simplex
         }
       }
       t.nterm[pij] = int8_t(n);
+      // the kernels unroll the terms from the compile-time node supports
+      const int ni = pk_sup_n(dim, nb, i), nj = pk_sup_n(dim, nb, j);
+      bool same = n == ni * nj;
+      for (int ti = 0; same && ti < ni; ++ti)
+        for (int tj = 0; tj < nj; ++tj)
+          same = same && t.vw[pij * kMaxPairTerms + ti * nj + tj] ==
+                             int8_t(pk_sup_v(dim, nb, i, ti) * nv + pk_sup_v(dim, nb, j, tj));
+      if (!same) {
+        errmsg = "internal: node supports differ from the element's lattice";
+        return GFGPU_E_UNSUPPORTED;
+      }
       double m = 0;
       for (int qq = 0; qq < q.nq; ++qq) m += q.w[qq] * phi[qq * nb + i] * phi[qq * nb + j];
       t.mass[pij] = m;
@@ -380,9 +506,12 @@ int fill_simplex_tables(int dim, int K, int qdim, const std::string &im, Simplex
   lay.nb = nb;
   lay.qd = qd;
   lay.s = s;
-  // rows padded to a multiple of 4 doubles: 32-byte aligned rows and blocks
+  // rows padded to a multiple of 4 doubles (scalar fields), or node blocks
+  // of 4 / 12 doubles (vector fields): whole 32-byte sectors either way
   lay.rowstride = (s + 3) & ~3;
-  lay.off_vec = s * lay.rowstride;
+  lay.blk = qd == 1 ? 0 : (qd == 2 ? 4 : 12);
+  lay.rowblk = qd == 1 ? lay.rowstride : nb * lay.blk;
+  lay.off_vec = qd == 1 ? s * lay.rowstride : nb * nb * lay.blk;
   lay.off_thr = lay.off_vec + lay.rowstride;
   lay.stride = lay.off_thr + 4;
   lay.linear = true;

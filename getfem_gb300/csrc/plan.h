@@ -43,11 +43,25 @@ struct SimplexTables {
 //         nonlinear form)
 //   thr   1e-14 max|K_e| at off_thr
 // stride is even, so every element block and every row is 16-byte aligned.
+// Two layouts of K_e:
+//   rows (blk == 0): row (li,a) at (li*qd + a) * rowstride;
+//   node blocks (blk > 0, vector fields of the simplex pass): the qd x qd
+//         block of local nodes (i,j) at (i*nb + j) * blk, entry (a,b) at
+//         a*qd + b; blk = 4 (qd 2) or 12 (qd 3, 9 entries and 3 zeros), so
+//         every block is whole 32-byte sectors.
+// Either way the rows of local node li are the rowblk doubles at
+// li * rowblk.
 struct KeLayout {
   int nb = 0, qd = 0, s = 0;
   int rowstride = 0, off_vec = 0, off_thr = 0, stride = 0;
+  int blk = 0, rowblk = 0;
   bool linear = true;  // R = K_full u + sum V_e (else R = sum V_e)
 };
+
+// offset of K_e[(li,a), c] (c = lj*qd + b) within the node row block of li
+__host__ __device__ __forceinline__ int ke_in_rowblk(const KeLayout &L, int a, int c) {
+  return L.blk ? (c / L.qd) * L.blk + a * L.qd + c % L.qd : a * L.rowstride + c;
+}
 
 struct SlotPtrs {
   const double *p[GFGPU_MAX_SLOTS];

@@ -17,3 +17,15 @@ def simplex_term_count(dim: int, degree: int, im: str | None = None):
         supp.append(sum(1 for x in w if x > 0))
     s = sum(supp)
     return s * s, len(supp)
+
+
+def simplex_upper_term_count(dim: int, degree: int) -> int:
+    """Terms over the node pairs i <= j (the symmetric element pass computes
+    each pair block once): ((sum |supp|)^2 + sum |supp|^2) / 2."""
+    supp = []
+    for c in product(range(degree + 1), repeat=dim):
+        if sum(c) > degree:
+            continue
+        w = [degree - sum(c)] + list(c)
+        supp.append(sum(1 for x in w if x > 0))
+    return (sum(supp) ** 2 + sum(x * x for x in supp)) // 2
