@@ -21,18 +21,18 @@ using namespace gfgpu;
 struct gfgpu_plan_s : public Plan {};
 
 namespace gfgpu {
-cudaError_t batch_element_pass_attr(size_t smem);
 cudaError_t batch_gather_attr(size_t smem);
 }
 
 // A batch of affine-simplex plans launched together.
 struct gfgpu_batch_s {
   std::vector<gfgpu_plan *> plans;
-  BatchItem *d_items = nullptr;     // element pass: all items
-  int64_t *d_tile0 = nullptr;       // tile offsets (nitems + 1)
-  int nitems = 0;
-  int64_t ntiles = 0, elements = 0;
-  size_t ep_smem = 0;
+  // element pass: items grouped by element type, tile offsets per group
+  BatchItem *d_eitems[kBatchElementTypes] = {};
+  int64_t *d_tile0[kBatchElementTypes] = {};
+  int en[kBatchElementTypes] = {};
+  int64_t entiles[kBatchElementTypes] = {};
+  int64_t elements = 0;
   // gather: items grouped by component count
   BatchItem *d_gitems[4] = {};
   int64_t *d_node0[4] = {};
@@ -679,13 +679,16 @@ int gfgpu_batch_create(gfgpu_plan *const *plans, int32_t n, gfgpu_batch **out) {
     gfgpu_batch_destroy(B);
     return rc;
   };
-  std::vector<BatchItem> items;
-  std::vector<int64_t> tile0(1, 0);
+  std::vector<BatchItem> eitems[kBatchElementTypes];
+  std::vector<int64_t> tile0[kBatchElementTypes];
+  for (int t = 0; t < kBatchElementTypes; ++t) tile0[t].push_back(0);
   std::vector<BatchItem> gitems[4];
   std::vector<int64_t> node0[4];
   for (int q = 0; q < 4; ++q) node0[q].push_back(0);
   int rc;
   if ((rc = dalloc(&B->d_err, 1))) return fail(rc, "");
+  if (cudaMemset(B->d_err, 0, sizeof(int)) != cudaSuccess)
+    return fail(GFGPU_E_CUDA, "gfgpu_batch_create: cudaMemset failed");
   for (int i = 0; i < n; ++i) {
     Plan &P = *plans[i];
     if (!P.affine_simplex)
@@ -724,25 +727,29 @@ int gfgpu_batch_create(gfgpu_plan *const *plans, int32_t n, gfgpu_batch **out) {
     it.vec = P.d_vec;
     if (it.etype < 0 || P.lay.s > 32)
       return fail(GFGPU_E_UNSUPPORTED, "gfgpu_batch_create: element not batched");
-    items.push_back(it);
-    tile0.push_back(tile0.back() + (P.n_elements + 31) / 32);
+    eitems[it.etype].push_back(it);
+    tile0[it.etype].push_back(tile0[it.etype].back() + (P.n_elements + 31) / 32);
     B->elements += P.n_elements;
-    B->ep_smem = std::max(B->ep_smem, simplex_batch_smem(it.etype));
     gitems[it.qd].push_back(it);
     node0[it.qd].push_back(node0[it.qd].back() + P.n_nodes);
     B->gwarp[it.qd] = std::max(B->gwarp[it.qd], batch_gather_warp_bytes(it));
     B->plans.push_back(plans[i]);
   }
-  B->nitems = n;
-  B->ntiles = tile0.back();
   auto upload = [&](void *dst, const void *src, size_t bytes) -> int {
     GF_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
     return GFGPU_OK;
   };
-  if ((rc = dalloc(&B->d_items, items.size()))) return fail(rc, "");
-  if ((rc = dalloc(&B->d_tile0, tile0.size()))) return fail(rc, "");
-  if ((rc = upload(B->d_items, items.data(), items.size() * sizeof(BatchItem)))) return fail(rc, "");
-  if ((rc = upload(B->d_tile0, tile0.data(), tile0.size() * sizeof(int64_t)))) return fail(rc, "");
+  for (int t = 0; t < kBatchElementTypes; ++t) {
+    B->en[t] = int(eitems[t].size());
+    B->entiles[t] = tile0[t].back();
+    if (!B->en[t]) continue;
+    if ((rc = dalloc(&B->d_eitems[t], eitems[t].size()))) return fail(rc, "");
+    if ((rc = dalloc(&B->d_tile0[t], tile0[t].size()))) return fail(rc, "");
+    if ((rc = upload(B->d_eitems[t], eitems[t].data(), eitems[t].size() * sizeof(BatchItem))))
+      return fail(rc, "");
+    if ((rc = upload(B->d_tile0[t], tile0[t].data(), tile0[t].size() * sizeof(int64_t))))
+      return fail(rc, "");
+  }
   for (int q = 1; q <= 3; ++q) {
     B->gn[q] = int(gitems[q].size());
     B->gnodes[q] = node0[q].back();
@@ -756,8 +763,7 @@ int gfgpu_batch_create(gfgpu_plan *const *plans, int32_t n, gfgpu_batch **out) {
   }
   size_t gmax = 0;
   for (int q = 1; q <= 3; ++q) gmax = std::max(gmax, B->gwarp[q]);
-  cudaError_t ce = batch_element_pass_attr(B->ep_smem);
-  if (ce == cudaSuccess) ce = batch_gather_attr(4 * gmax);
+  cudaError_t ce = batch_gather_attr(4 * gmax);
   if (ce != cudaSuccess)
     return fail(GFGPU_E_CUDA, std::string("gfgpu_batch_create: ") + cudaGetErrorString(ce));
   int dev = 0, sms = 0;
@@ -769,9 +775,19 @@ int gfgpu_batch_create(gfgpu_plan *const *plans, int32_t n, gfgpu_batch **out) {
   return GFGPU_OK;
 }
 
+static int batch_element_passes(gfgpu_batch *B, cudaStream_t st, int grid_ep) {
+  for (int t = 0; t < kBatchElementTypes; ++t)
+    if (B->en[t])
+      GF_CUDA(launch_batch_element_pass(B->d_eitems[t], B->d_tile0[t], B->en[t], B->entiles[t],
+                                        int(std::min<int64_t>(grid_ep, B->entiles[t])), t, st));
+  return GFGPU_OK;
+}
+
 static int batch_launch(gfgpu_batch *B, cudaStream_t st, int grid_ep, int grid_ga) {
-  GF_CUDA(launch_batch_element_pass(B->d_items, B->d_tile0, B->nitems, B->ntiles, grid_ep,
-                                    B->ep_smem, st));
+  // a fresh error word for this assembly (a memset node in a captured graph)
+  GF_CUDA(cudaMemsetAsync(B->d_err, 0, sizeof(int), st));
+  int rc = batch_element_passes(B, st, grid_ep);
+  if (rc) return rc;
   for (int q = 1; q <= 3; ++q)
     if (B->gn[q])
       GF_CUDA(launch_batch_gather(B->d_gitems[q], B->d_node0[q], B->gn[q], B->gnodes[q], q,
@@ -800,8 +816,8 @@ int gfgpu_batch_tune(gfgpu_batch *B, void *stream, int32_t *grid_ep, int32_t *gr
     float t_ep = 0, t_ga = 0;
     for (int rep = 0; rep < 3; ++rep) {
       GF_CUDA(cudaEventRecord(e0, st));
-      GF_CUDA(launch_batch_element_pass(B->d_items, B->d_tile0, B->nitems, B->ntiles, g,
-                                        B->ep_smem, st));
+      int rc = batch_element_passes(B, st, g);
+      if (rc) return rc;
       GF_CUDA(cudaEventRecord(e1, st));
       GF_CUDA(cudaEventSynchronize(e1));
       float t;
@@ -839,8 +855,10 @@ int64_t gfgpu_batch_elements(gfgpu_batch *B) { return B ? B->elements : -1; }
 
 void gfgpu_batch_destroy(gfgpu_batch *B) {
   if (!B) return;
-  dfree(B->d_items);
-  dfree(B->d_tile0);
+  for (int t = 0; t < kBatchElementTypes; ++t) {
+    dfree(B->d_eitems[t]);
+    dfree(B->d_tile0[t]);
+  }
   for (int q = 0; q < 4; ++q) {
     dfree(B->d_gitems[q]);
     dfree(B->d_node0[q]);

@@ -541,23 +541,16 @@ GFGPU_BT(12, 3, 1, 4, true) GFGPU_BT(13, 3, 1, 10, true) GFGPU_BT(14, 3, 3, 4, t
 GFGPU_BT(15, 3, 3, 10, true)
 #undef GFGPU_BT
 
+// Persistent element pass over the tiles of the meshes of one element type
+// in a batch: block b takes tiles b, b + grid, ...; the mesh of a tile is
+// found by binary search in the tile offsets.  One launch per element type
+// keeps each type's own register and shared-memory footprint.
 template <int T>
-__device__ __forceinline__ void run_batch_tile(unsigned char *dsm, const BatchItem &it,
-                                               int64_t tile) {
-  using B = BatchType<T>;
-  using SH = EpShared<B::DIM, B::QD, B::NB>;
-  simplex_element_tile<B::DIM, B::QD, B::NB, B::MASS, true>(
-      *reinterpret_cast<SH *>(dsm), tile, it.E, it.pts, it.cv, it.enode, it.tab, it.L, it.form,
-      it.slots, it.fsrc, it.fscale, it.u, it.elem, it.err);
-}
-
-// Persistent element pass over the tiles of every mesh of the batch: block b
-// takes tiles b, b + grid, ...; the mesh of a tile is found by binary search
-// in the tile offsets.
 __global__ void __launch_bounds__(kEpThreads) batch_element_pass(
     const BatchItem *__restrict__ items, const int64_t *__restrict__ tile0, int nitems,
     int64_t ntiles) {
-  extern __shared__ __align__(16) unsigned char dsm[];
+  using B = BatchType<T>;
+  __shared__ EpShared<B::DIM, B::QD, B::NB> sh;
   for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
     int lo = 0, hi = nitems - 1;
     while (lo < hi) {
@@ -566,24 +559,11 @@ __global__ void __launch_bounds__(kEpThreads) batch_element_pass(
       else hi = mid - 1;
     }
     const BatchItem &it = items[lo];
-    const int64_t tile = t - tile0[lo];
     __syncthreads();  // the previous tile is done with the shared memory
-    switch (it.etype) {
-#define GFGPU_RT(T) \
-  case T: run_batch_tile<T>(dsm, it, tile); break;
-      GFGPU_RT(0) GFGPU_RT(1) GFGPU_RT(2) GFGPU_RT(3) GFGPU_RT(4) GFGPU_RT(5) GFGPU_RT(6)
-      GFGPU_RT(7) GFGPU_RT(8) GFGPU_RT(9) GFGPU_RT(10) GFGPU_RT(11) GFGPU_RT(12) GFGPU_RT(13)
-      GFGPU_RT(14) GFGPU_RT(15)
-#undef GFGPU_RT
-      default: break;
-    }
+    simplex_element_tile<B::DIM, B::QD, B::NB, B::MASS, true>(
+        sh, t - tile0[lo], it.E, it.pts, it.cv, it.enode, it.tab, it.L, it.form, it.slots,
+        it.fsrc, it.fscale, it.u, it.elem, it.err);
   }
-}
-
-template <int T>
-size_t smem_of() {
-  using B = BatchType<T>;
-  return sizeof(EpShared<B::DIM, B::QD, B::NB>);
 }
 
 }  // namespace
@@ -594,14 +574,6 @@ int simplex_batch_type(int dim, int degree, int qdim, bool mass) {
   else base = 4 + (qdim == 1 ? 0 : 2) + (degree == 1 ? 0 : 1);
   if (degree < 1 || degree > 2 || (qdim != 1 && qdim != dim)) return -1;
   return base + (mass ? 8 : 0);
-}
-
-size_t simplex_batch_smem(int etype) {
-  static const size_t sz[kBatchTypes] = {
-      smem_of<0>(),  smem_of<1>(),  smem_of<2>(),  smem_of<3>(),  smem_of<4>(),  smem_of<5>(),
-      smem_of<6>(),  smem_of<7>(),  smem_of<8>(),  smem_of<9>(),  smem_of<10>(), smem_of<11>(),
-      smem_of<12>(), smem_of<13>(), smem_of<14>(), smem_of<15>()};
-  return etype >= 0 && etype < kBatchTypes ? sz[etype] : 0;
 }
 
 void simplex_source_of(const Plan &P, const double *&fsrc, double &fscale, bool &mass) {
@@ -619,15 +591,20 @@ void simplex_source_of(const Plan &P, const double *&fsrc, double &fscale, bool 
 }
 
 cudaError_t launch_batch_element_pass(const BatchItem *items, const int64_t *tile0, int nitems,
-                                     int64_t ntiles, int grid, size_t smem, cudaStream_t st) {
+                                     int64_t ntiles, int grid, int etype, cudaStream_t st) {
   if (ntiles == 0) return cudaSuccess;
-  batch_element_pass<<<grid, kEpThreads, smem, st>>>(items, tile0, nitems, ntiles);
+  switch (etype) {
+#define GFGPU_BL(T)                                                                  \
+  case T:                                                                            \
+    batch_element_pass<T><<<grid, kEpThreads, 0, st>>>(items, tile0, nitems, ntiles); \
+    break;
+    GFGPU_BL(0) GFGPU_BL(1) GFGPU_BL(2) GFGPU_BL(3) GFGPU_BL(4) GFGPU_BL(5) GFGPU_BL(6)
+    GFGPU_BL(7) GFGPU_BL(8) GFGPU_BL(9) GFGPU_BL(10) GFGPU_BL(11) GFGPU_BL(12) GFGPU_BL(13)
+    GFGPU_BL(14) GFGPU_BL(15)
+#undef GFGPU_BL
+    default: return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
-}
-
-cudaError_t batch_element_pass_attr(size_t smem) {
-  return cudaFuncSetAttribute(batch_element_pass, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              int(smem));
 }
 
 int build_simplex_tables(Plan &P, std::string &errmsg) {

@@ -176,10 +176,10 @@ struct BatchItem {
 
 // batched launches (k_simplex.cu, k_assemble.cu)
 int simplex_batch_type(int dim, int degree, int qdim, bool mass);
-size_t simplex_batch_smem(int etype);
 void simplex_source_of(const Plan &P, const double *&fsrc, double &fscale, bool &mass);
+constexpr int kBatchElementTypes = 16;
 cudaError_t launch_batch_element_pass(const BatchItem *items, const int64_t *tile0, int nitems,
-                                     int64_t ntiles, int grid, size_t smem, cudaStream_t st);
+                                     int64_t ntiles, int grid, int etype, cudaStream_t st);
 size_t batch_gather_warp_bytes(const BatchItem &it);
 cudaError_t launch_batch_gather(const BatchItem *items, const int64_t *node0, int nitems,
                                int64_t nnodes, int qd, int grid, size_t warp_bytes,
