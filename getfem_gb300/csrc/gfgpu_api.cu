@@ -424,6 +424,19 @@ int gfgpu_plan_create(const gfgpu_space *space, const gfgpu_form *form, void *cu
       CHK(up(P->d_hgrad, P->h_grad.data(), P->h_grad.size() * sizeof(double)));
       CHK(up(P->d_ggrad, P->h_ggrad.data(), P->h_ggrad.size() * sizeof(double)));
       CHK(up(P->d_hw, P->h_w.data(), P->h_w.size() * sizeof(double)));
+      // transposed copies for the lane-per-Gauss-point kernels
+      const int nq = P->nq, nbb = P->nb, D = P->dim;
+      std::vector<double> vt(size_t(nbb) * nq), gt(size_t(nbb) * D * nq);
+      for (int q = 0; q < nq; ++q)
+        for (int j = 0; j < nbb; ++j) {
+          vt[size_t(j) * nq + q] = P->h_val[size_t(q) * nbb + j];
+          for (int m = 0; m < D; ++m)
+            gt[(size_t(j) * D + m) * nq + q] = P->h_grad[(size_t(q) * nbb + j) * D + m];
+        }
+      CHK(dalloc(&P->d_hvalT, vt.size()));
+      CHK(dalloc(&P->d_hgradT, gt.size()));
+      CHK(up(P->d_hvalT, vt.data(), vt.size() * sizeof(double)));
+      CHK(up(P->d_hgradT, gt.data(), gt.size() * sizeof(double)));
     }
     GF_CUDA(cudaMemset(P->d_err, 0, sizeof(int)));
     GF_CUDA(cudaMemset(P->d_vec, 0, size_t(S.n_dof) * sizeof(double)));
@@ -449,6 +462,8 @@ void gfgpu_plan_destroy(gfgpu_plan *P) {
   dfree(P->d_hgrad);
   dfree(P->d_ggrad);
   dfree(P->d_hw);
+  dfree(P->d_hvalT);
+  dfree(P->d_hgradT);
   dfree(P->d_tri);
   dfree(P->d_aff);
   dfree(P->d_padj_ptr);

@@ -58,13 +58,15 @@ __device__ __forceinline__ void geo_inverse(const double *K, double *B, double &
   }
 }
 
+// phi: the base values at the Gauss point, phi_j = phi[j * ps]
 __device__ __forceinline__ double coef_val(const gfgpu_coef &c, const SlotPtrs &slots, int64_t e,
-                                           const int32_t *en, const double *phi, int nb) {
+                                           const int32_t *en, const double *phi, int nb,
+                                           int ps) {
   if (c.kind == GFGPU_COEF_CONST) return c.value;
   if (c.kind == GFGPU_COEF_ELEMENT) return c.value * slots.p[c.slot][e];
   if (c.kind == GFGPU_COEF_NODAL) {
     double s = 0.0;
-    for (int j = 0; j < nb; ++j) s += phi[j] * slots.p[c.slot][en[j]];
+    for (int j = 0; j < nb; ++j) s += phi[j * ps] * slots.p[c.slot][en[j]];
     return c.value * s;
   }
   return 0.0;
@@ -89,8 +91,9 @@ template <int DIM, int QD, int NB, int NBG, int LAW>
 __global__ void __launch_bounds__(kGpWarps * 32) gauss_potential_kernel(
     int64_t E, int nq, int mode, int wslot, const double *__restrict__ pts,
     const int32_t *__restrict__ cv, const int32_t *__restrict__ enode,
-    const double *__restrict__ hval, const double *__restrict__ hgrad,
-    const double *__restrict__ ggrad, const double *__restrict__ hw, gfgpu_form form,
+    const double *__restrict__ hval, const double *__restrict__ hvalT,
+    const double *__restrict__ hgradT, const double *__restrict__ ggrad,
+    const double *__restrict__ hw, gfgpu_form form,
     SlotPtrs slots, double *__restrict__ out_e, double *__restrict__ out_n,
     double *__restrict__ out_x, int *__restrict__ err) {
   constexpr int S = NB * QD;
@@ -137,34 +140,39 @@ __global__ void __launch_bounds__(kGpWarps * 32) gauss_potential_kernel(
     geo_inverse<DIM>(K, B, det);
     if (act && det == 0.0) set_err(err, ERR_JACOBIAN);
     const double wJ = (act && det != 0.0) ? fabs(det) * hw[qq] : 0.0;
-    // Grad_u(a,d) and u(x_q)
-    double Gu[QD][DIM], uq[QD];
+    // Grad_u in reference coordinates, Gr(a,m) = sum_j u_ja dphi_j/dxi_m, then
+    // Grad_u(a,d) = sum_m B(d,m) Gr(a,m); u(x_q).  The tables are read
+    // transposed (Gauss point fastest), so the lanes' loads coalesce.
+    double Gu[QD][DIM], Gr[QD][DIM], uq[QD];
 #pragma unroll
     for (int a = 0; a < QD; ++a) {
       uq[a] = 0.0;
 #pragma unroll
-      for (int d = 0; d < DIM; ++d) Gu[a][d] = 0.0;
+      for (int m = 0; m < DIM; ++m) Gr[a][m] = 0.0;
     }
-    const double *phi = hval + qq * NB;
+    const double *phi = hvalT + qq;  // phi_j = phi[j * nq]
     for (int j = 0; j < NB; ++j) {
-      const double *hg = hgrad + (qq * NB + j) * DIM;
-      double gj[DIM];
+      double r[DIM];
+#pragma unroll
+      for (int m = 0; m < DIM; ++m) r[m] = hgradT[int64_t(j * DIM + m) * nq + qq];
+      const double ph = phi[int64_t(j) * nq];
+#pragma unroll
+      for (int a = 0; a < QD; ++a) {
+        const double ua = us[j * QD + a];
+        uq[a] += ph * ua;
+#pragma unroll
+        for (int m = 0; m < DIM; ++m) Gr[a][m] += ua * r[m];
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < QD; ++a)
 #pragma unroll
       for (int d = 0; d < DIM; ++d) {
         double s = 0.0;
 #pragma unroll
-        for (int m = 0; m < DIM; ++m) s += hg[m] * B[d + DIM * m];
-        gj[d] = s;
+        for (int m = 0; m < DIM; ++m) s += B[d + DIM * m] * Gr[a][m];
+        Gu[a][d] = s;
       }
-#pragma unroll
-      for (int a = 0; a < QD; ++a) {
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) Gu[a][d] += us[j * QD + a] * gj[d];
-      }
-    }
-    for (int j = 0; j < NB; ++j)
-#pragma unroll
-      for (int a = 0; a < QD; ++a) uq[a] += phi[j] * us[j * QD + a];
     // integrand psi, P = dpsi/dGrad_u, and the coefficient derivatives
     double psi = 0.0, de = 0.0, dnq = 0.0;
     double P[QD][DIM];
@@ -175,8 +183,8 @@ __global__ void __launch_bounds__(kGpWarps * 32) gauss_potential_kernel(
     if constexpr (LAW == LAW_NH) {
       const gfgpu_term &T = form.terms[0];
       const double sc = T.scale;
-      const double C1 = coef_val(T.c[0], slots, e, en, phi, NB);
-      const double D1 = coef_val(T.c[1], slots, e, en, phi, NB);
+      const double C1 = coef_val(T.c[0], slots, e, en, phi, NB, nq);
+      const double D1 = coef_val(T.c[1], slots, e, en, phi, NB, nq);
       double F[9], C[9];
 #pragma unroll
       for (int i = 0; i < 3; ++i)
@@ -237,9 +245,9 @@ __global__ void __launch_bounds__(kGpWarps * 32) gauss_potential_kernel(
         const gfgpu_term &T = form.terms[t];
         const double sc = T.scale;
         if (T.kind == GFGPU_TERM_GRADGRAD) {
-          const double c0 = coef_val(T.c[0], slots, e, en, phi, NB) * sc;
-          const double c1 = coef_val(T.c[1], slots, e, en, phi, NB) * sc;
-          const double c2 = coef_val(T.c[2], slots, e, en, phi, NB) * sc;
+          const double c0 = coef_val(T.c[0], slots, e, en, phi, NB, nq) * sc;
+          const double c1 = coef_val(T.c[1], slots, e, en, phi, NB, nq) * sc;
+          const double c2 = coef_val(T.c[2], slots, e, en, phi, NB, nq) * sc;
           double v = 0.0, gg = 0.0, gt = 0.0;
 #pragma unroll
           for (int a = 0; a < QD; ++a)
@@ -261,7 +269,7 @@ __global__ void __launch_bounds__(kGpWarps * 32) gauss_potential_kernel(
           coef_dfac(T.c[2], wslot, fe, fn);
           de += sc * gt * fe, dnq += sc * gt * fn;
         } else if (T.kind == GFGPU_TERM_MASS) {
-          const double c0 = coef_val(T.c[0], slots, e, en, phi, NB) * sc;
+          const double c0 = coef_val(T.c[0], slots, e, en, phi, NB, nq) * sc;
           double uu = 0.0;
 #pragma unroll
           for (int a = 0; a < QD; ++a) {
@@ -273,20 +281,20 @@ __global__ void __launch_bounds__(kGpWarps * 32) gauss_potential_kernel(
           de += sc * uu * fe, dnq += sc * uu * fn;
         } else if (T.kind == GFGPU_TERM_SOURCE) {
           const bool none = T.c[0].kind == GFGPU_COEF_NONE;
-          const double c0 = (none ? 1.0 : coef_val(T.c[0], slots, e, en, phi, NB)) * sc;
+          const double c0 = (none ? 1.0 : coef_val(T.c[0], slots, e, en, phi, NB, nq)) * sc;
           const double *f = slots.p[T.field_slot];
           double fq[QD];
 #pragma unroll
           for (int a = 0; a < QD; ++a) fq[a] = 0.0;
           for (int j = 0; j < NB; ++j)
 #pragma unroll
-            for (int a = 0; a < QD; ++a) fq[a] += phi[j] * f[int64_t(en[j]) * QD + a];
+            for (int a = 0; a < QD; ++a) fq[a] += phi[int64_t(j) * nq] * f[int64_t(en[j]) * QD + a];
           double fu = 0.0;
           for (int j = 0; j < NB; ++j)
 #pragma unroll
             for (int a = 0; a < QD; ++a) {
-              psi += c0 * fq[a] * phi[j] * us[j * QD + a];
-              fu += fq[a] * phi[j] * us[j * QD + a];
+              psi += c0 * fq[a] * phi[int64_t(j) * nq] * us[j * QD + a];
+              fu += fq[a] * phi[int64_t(j) * nq] * us[j * QD + a];
             }
           if (!none) {
             double fe, fn;
@@ -405,7 +413,8 @@ cudaError_t launch_gp(Plan &P, int mode, int wslot, const SlotPtrs &sp, double *
                       double *ox) {
   const unsigned blocks = unsigned((P.n_elements + kGpWarps - 1) / kGpWarps);
   gauss_potential_kernel<DIM, QD, NB, NBG, LAW><<<blocks, kGpWarps * 32, 0, P.stream>>>(
-      P.n_elements, P.nq, mode, wslot, P.d_points, P.d_cv, P.d_enode, P.d_hval, P.d_hgrad,
+      P.n_elements, P.nq, mode, wslot, P.d_points, P.d_cv, P.d_enode, P.d_hval, P.d_hvalT,
+      P.d_hgradT,
       P.d_ggrad, P.d_hw, P.form, sp, oe, on, ox, P.d_err);
   return cudaGetLastError();
 }

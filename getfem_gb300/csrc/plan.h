@@ -111,6 +111,9 @@ struct Plan {
   // nq x nb x dim, geometric gradients nq x nbg x dim, weights nq
   std::vector<double> h_val, h_grad, h_ggrad, h_w;
   double *d_hval = nullptr, *d_hgrad = nullptr, *d_ggrad = nullptr, *d_hw = nullptr;
+  // the same tables transposed (Gauss point fastest): values nb x nq,
+  // reference gradients (nb*dim) x nq, for kernels with a lane per point
+  double *d_hvalT = nullptr, *d_hgradT = nullptr;
   std::vector<int32_t> h_tri;  // upper-triangle entries of K_e (Gauss kernel)
   int32_t *d_tri = nullptr;
   // parallelepiped hexahedra: reference tensors (7 x nb x nb)
