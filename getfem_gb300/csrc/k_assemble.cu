@@ -314,7 +314,7 @@ __device__ __forceinline__ void gather_node(
 
 template <int QD, int R>
 __global__ void __launch_bounds__(128) gather_kernel(
-    int64_t n_nodes, KeLayout L, const int32_t *__restrict__ adj_ptr,
+    int64_t node0, int64_t n_nodes, KeLayout L, const int32_t *__restrict__ adj_ptr,
     const int32_t *__restrict__ adj, const double *__restrict__ elem, int ms, int mad,
     const int64_t *__restrict__ nptr, const uint16_t *__restrict__ nbits,
     const int16_t *__restrict__ slotmap, const int64_t *__restrict__ rowptr,
@@ -323,7 +323,7 @@ __global__ void __launch_bounds__(128) gather_kernel(
   extern __shared__ __align__(16) double dsm[];
   const int wib = threadIdx.x >> 5;
   char *base = reinterpret_cast<char *>(dsm) + wib * gather_warp_bytes(ms, QD, L.rowblk, mad);
-  const int64_t node = blockIdx.x * int64_t(blockDim.x >> 5) + wib;
+  const int64_t node = node0 + blockIdx.x * int64_t(blockDim.x >> 5) + wib;
   if (node >= n_nodes) return;
   gather_node<QD, R>(base, node, L, adj_ptr, adj, elem, ms, mad, nptr, nbits, slotmap, rowptr,
                      vals, want_K, want_R, vec, err);
@@ -365,29 +365,30 @@ int pattern_cap(const Plan &P) {
 }
 
 template <int QD, int R>
-cudaError_t launch_gather_t(Plan &P, bool want_K, bool want_R) {
+cudaError_t launch_gather_t(Plan &P, bool want_K, bool want_R, int64_t n0, int64_t n1) {
   const int ms = P.max_slots < 1 ? 1 : P.max_slots;
   const int mad = P.max_adj < 1 ? 1 : P.max_adj;
   const size_t smem = size_t(kWarpsPerBlock) * gather_warp_bytes(ms, QD, P.lay.rowblk, mad);
   cudaError_t ce = cudaFuncSetAttribute(gather_kernel<QD, R>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
   if (ce != cudaSuccess) return ce;
-  const unsigned blocks = unsigned((P.n_nodes + kWarpsPerBlock - 1) / kWarpsPerBlock);
+  if (n1 <= n0) return cudaSuccess;
+  const unsigned blocks = unsigned((n1 - n0 + kWarpsPerBlock - 1) / kWarpsPerBlock);
   gather_kernel<QD, R><<<blocks, kWarpsPerBlock * 32, smem, P.stream>>>(
-      P.n_nodes, P.lay, P.d_adj_ptr, P.d_adj, P.d_elem, ms, mad, P.d_nptr, P.d_nbits,
+      n0, n1, P.lay, P.d_adj_ptr, P.d_adj, P.d_elem, ms, mad, P.d_nptr, P.d_nbits,
       P.d_slotmap, P.d_rowptr, P.d_vals, want_K, want_R, P.d_vec, P.d_err);
   P.launches++;
   return cudaGetLastError();
 }
 
 template <int QD>
-cudaError_t launch_gather_q(Plan &P, bool want_K, bool want_R) {
+cudaError_t launch_gather_q(Plan &P, bool want_K, bool want_R, int64_t n0, int64_t n1) {
   const int rounds = (P.lay.s + 31) / 32;
   switch (rounds) {
-    case 1: return launch_gather_t<QD, 1>(P, want_K, want_R);
-    case 2: return launch_gather_t<QD, 2>(P, want_K, want_R);
-    case 3: return launch_gather_t<QD, 3>(P, want_K, want_R);
-    case 4: return launch_gather_t<QD, 4>(P, want_K, want_R);
+    case 1: return launch_gather_t<QD, 1>(P, want_K, want_R, n0, n1);
+    case 2: return launch_gather_t<QD, 2>(P, want_K, want_R, n0, n1);
+    case 3: return launch_gather_t<QD, 3>(P, want_K, want_R, n0, n1);
+    case 4: return launch_gather_t<QD, 4>(P, want_K, want_R, n0, n1);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -461,13 +462,17 @@ cudaError_t batch_gather_attr(size_t smem) {
                               int(smem));
 }
 
-cudaError_t launch_gather(Plan &P, bool want_K, bool want_R) {
+cudaError_t launch_gather_range(Plan &P, bool want_K, bool want_R, int64_t n0, int64_t n1) {
   switch (P.qdim) {
-    case 1: return launch_gather_q<1>(P, want_K, want_R);
-    case 2: return launch_gather_q<2>(P, want_K, want_R);
-    case 3: return launch_gather_q<3>(P, want_K, want_R);
+    case 1: return launch_gather_q<1>(P, want_K, want_R, n0, n1);
+    case 2: return launch_gather_q<2>(P, want_K, want_R, n0, n1);
+    case 3: return launch_gather_q<3>(P, want_K, want_R, n0, n1);
     default: return cudaErrorInvalidValue;
   }
+}
+
+cudaError_t launch_gather(Plan &P, bool want_K, bool want_R) {
+  return launch_gather_range(P, want_K, want_R, 0, P.n_nodes);
 }
 
 }  // namespace gfgpu

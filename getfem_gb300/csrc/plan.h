@@ -78,6 +78,8 @@ enum : int {
   LAW_NH = 1    // compressible neo-Hookean PK2 term
 };
 
+constexpr int kHostChunks = 16;  // gather chunks of gfgpu_assemble_host
+
 struct Plan {
   // discretisation
   int dim = 0, kind = 0, degree = 0, qdim = 0, nb = 0, nbg = 0, nq = 0;
@@ -149,6 +151,11 @@ struct Plan {
   int64_t launches = 0;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   bool profiled = false;
+  // host-buffer assembly: row pointers on the host, a copy stream and one
+  // event per gather chunk (device-to-host copies overlap the gather)
+  std::vector<int64_t> h_rowptr;
+  cudaStream_t copy_stream[2] = {nullptr, nullptr};
+  cudaEvent_t chunk_ev[kHostChunks] = {};
 };
 
 // One mesh of a batched launch: everything the element pass and the row
@@ -193,6 +200,8 @@ cudaError_t launch_simplex_element_pass(Plan &P, bool with_u);
 cudaError_t launch_pattern_count(Plan &P);
 cudaError_t launch_pattern_fill(Plan &P);
 cudaError_t launch_gather(Plan &P, bool want_K, bool want_R);
+// the gather of DOF nodes [n0, n1) (their rows of the CSR and of R)
+cudaError_t launch_gather_range(Plan &P, bool want_K, bool want_R, int64_t n0, int64_t n1);
 int build_simplex_tables(Plan &P, std::string &err);
 int fill_simplex_tables(int dim, int degree, int qdim, const std::string &im, SimplexTables &t,
                         KeLayout &lay, int &nq, std::string &err);

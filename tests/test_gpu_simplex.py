@@ -91,6 +91,13 @@ def test_gpu_deterministic_and_fused_pass():
     L.check(lib.gfgpu_assemble_host(h, u.ctypes.data_as(C.c_void_p), None,
                                     vec2.ctypes.data_as(C.c_void_p)))
     assert np.array_equal(vec, vec2)
+    # page-locked host buffers: the gather writes them directly
+    torch = pytest.importorskip("torch")
+    pv = torch.empty(nnz.value, dtype=torch.float64).pin_memory()
+    pr = torch.empty(nr.value, dtype=torch.float64).pin_memory()
+    L.check(lib.gfgpu_assemble_host(h, u.ctypes.data_as(C.c_void_p), C.c_void_p(pv.data_ptr()),
+                                    C.c_void_p(pr.data_ptr())))
+    assert np.array_equal(pv.numpy(), vals) and np.array_equal(pr.numpy(), vec)
 
 
 def test_degenerate_element_reports_jacobian_error():
