@@ -41,7 +41,7 @@ constexpr int kLaw = 40;  // per-q neo-Hookean state for the tangent (doubles)
 constexpr int kRes = 36;  // per-q residual state (doubles)
 
 // neo-Hookean state offsets
-enum { LF = 0, LS = 9, LCI = 18, LI1 = 27, LI3, LP13, LDD, LC1, LD1, LWJ };
+enum { LF = 0, LS = 9, LCI = 18, LI1 = 27, LI3, LP13, LDD, LC1, LD1, LWJ, LK1, LK2, LA22 };
 // residual state offsets: neo-Hookean F S (9) and the term scale; isotropic
 // Grad_u (row-major, 9), div, then 3 values per term
 enum { RFS = 0, RSC = 9, RGU = 0, RDIV = 9, RTERM = 10 };
@@ -84,12 +84,13 @@ __device__ __forceinline__ double coef_at(const gfgpu_coef &c, const SlotPtrs &s
   return 0.0;
 }
 
-// dS_ij/dE_kl of the compressible neo-Hookean law from the state at q.
+// dS_ij/dE_kl of the compressible neo-Hookean law from the state at q
+// (coeff1 = 1/(3 i3), coeff2 = 4 coeff1^2 i1 and A22 = D1 / (2 |i3|^1.5) are
+// computed once per point).
 __device__ __forceinline__ double nh_dsde(const double *st, int i, int j, int k, int l) {
   const double *Ci = st + LCI;
   const double i1 = st[LI1], i3 = st[LI3], p13 = st[LP13], dd = st[LDD], C1 = st[LC1];
-  const double coeff1 = 1.0 / (3.0 * i3), coeff2 = 4.0 * coeff1 * coeff1 * i1;
-  const double A22 = st[LD1] / (2.0 * pow(fabs(i3), 1.5));
+  const double coeff1 = st[LK1], coeff2 = st[LK2], A22 = st[LA22];
   const double dij = Ci[i + 3 * j] * i3, dkl = Ci[k + 3 * l] * i3;
   const double ddi3 = i3 / 2.0 *
                       (Ci[j + 3 * i] * Ci[l + 3 * k] - Ci[j + 3 * k] * Ci[l + 3 * i] +
@@ -106,7 +107,9 @@ struct HexSmem {
   static constexpr int n_g = NQ * NB * 3, n_A = NQ * NA * NA, n_c = NQ, n_m = NQ,
                        n_r = NQ * kRes, n_u = S, n_x = NBG * 3;
   static constexpr int n_law = LAW == LAW_NH ? NQ * kLaw : 0;
-  static constexpr int n_Z = NA * S, n_GS = LAW == LAW_NH ? NQ * 81 : 0;
+  // phase B builds Z for kQG Gauss points at a time (fewer block barriers)
+  static constexpr int kQG = 3;
+  static constexpr int n_Z = kQG * NA * S, n_GS = LAW == LAW_NH ? NQ * 81 : 0;
   static constexpr int n_W = n_Z > n_GS ? n_Z : n_GS;
   static constexpr int o_g = 0, o_A = o_g + n_g, o_c = o_A + n_A, o_m = o_c + n_c,
                        o_r = o_m + n_m, o_u = o_r + n_r, o_x = o_u + n_u, o_law = o_x + n_x,
@@ -118,7 +121,7 @@ struct HexSmem {
 };
 
 template <int QD, int NB, int NBG, int NQ, int LAW, bool WANT_K>
-__global__ void __launch_bounds__(kHexThreads) hex_element_kernel(
+__global__ void __launch_bounds__(kHexThreads, 2) hex_element_kernel(
     int64_t E, const double *__restrict__ pts, const int32_t *__restrict__ cv,
     const int32_t *__restrict__ enode, const double *__restrict__ hval,
     const double *__restrict__ hgrad, const double *__restrict__ ggrad,
@@ -229,6 +232,12 @@ __global__ void __launch_bounds__(kHexThreads) hex_element_kernel(
         st[LCI + k] = Ci[k];
       }
       st[LI1] = i1, st[LI3] = i3, st[LP13] = p13, st[LDD] = dd, st[LC1] = C1, st[LD1] = D1;
+      {
+        const double coeff1 = 1.0 / (3.0 * i3);
+        st[LK1] = coeff1;
+        st[LK2] = 4.0 * coeff1 * coeff1 * i1;
+        st[LA22] = D1 / (2.0 * pow(fabs(i3), 1.5));
+      }
       st[LWJ] = wJ * sc;
 #pragma unroll
       for (int a = 0; a < 3; ++a)
@@ -352,34 +361,41 @@ __global__ void __launch_bounds__(kHexThreads) hex_element_kernel(
     double acc[NE];
 #pragma unroll
     for (int k = 0; k < NE; ++k) acc[k] = 0.0;
-    for (int q = 0; q < NQ; ++q) {
-      for (int z = tid; z < NA * S; z += kHexThreads) {
-        const int ak = z / S, cz = z % S, j = cz / QD, b = cz % QD;
+    constexpr int QG = M::kQG, NZ = NA * S;
+    for (int q0 = 0; q0 < NQ; q0 += QG) {
+      const int nqg = NQ - q0 < QG ? NQ - q0 : QG;
+      for (int z = tid; z < nqg * NZ; z += kHexThreads) {
+        const int t = z / NZ, zz = z - t * NZ, q = q0 + t;
+        const int ak = zz / S, cz = zz % S, j = cz / QD, b = cz % QD;
         const double *A = Aq + (q * NA + ak) * NA + b * 3;
         const double *gz = gq + (q * NB + j) * 3;
         W[z] = fma(A[0], gz[0], fma(A[1], gz[1], A[2] * gz[2]));
       }
       __syncthreads();
-      const double *gi = gq + q * NB * 3;
-      const double mqq = mq[q];
-#pragma unroll
-      for (int k = 0; k < NE; ++k) {
-        if (own[k]) {
-          const double *g = gi + goff[k];
-          const double *Z = W + zoff[k];
-          double t = fma(g[0], Z[0], acc[k]);
-          t = fma(g[1], Z[S], t);
-          acc[k] = fma(g[2], Z[2 * S], t);
-        }
-      }
-      if (mqq != 0.0) {
-        const double *phi = hval + q * NB;
+      for (int t = 0; t < nqg; ++t) {
+        const int q = q0 + t;
+        const double *gi = gq + q * NB * 3;
+        const double *Wt = W + t * NZ;
 #pragma unroll
         for (int k = 0; k < NE; ++k) {
-          if (own[k] && dg[k]) {
-            const int ent = tid + kHexThreads * k;
-            const int rc = tri[ent];
-            acc[k] = fma(mqq * phi[(rc >> 16) / QD], phi[(rc & 0xffff) / QD], acc[k]);
+          if (own[k]) {
+            const double *g = gi + goff[k];
+            const double *Z = Wt + zoff[k];
+            double v = fma(g[0], Z[0], acc[k]);
+            v = fma(g[1], Z[S], v);
+            acc[k] = fma(g[2], Z[2 * S], v);
+          }
+        }
+        const double mqq = mq[q];
+        if (mqq != 0.0) {
+          const double *phi = hval + q * NB;
+#pragma unroll
+          for (int k = 0; k < NE; ++k) {
+            if (own[k] && dg[k]) {
+              const int ent = tid + kHexThreads * k;
+              const int rc = tri[ent];
+              acc[k] = fma(mqq * phi[(rc >> 16) / QD], phi[(rc & 0xffff) / QD], acc[k]);
+            }
           }
         }
       }
