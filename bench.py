@@ -174,6 +174,18 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def combine_ranks(dist, world, elements, ms, e2e_ms, device):
+    """Replicas: every rank assembles its own copy of the workload.  The step
+    time is the slowest rank's (max over ranks); the throughput counts the
+    elements of all ranks over that time.  Returns (ms, e2e_ms, value, e2e)."""
+    if dist is not None and world > 1:
+        import torch
+        tt = torch.tensor([ms, e2e_ms], device=device, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms, e2e_ms = float(tt[0]), float(tt[1])
+    return ms, e2e_ms, world * elements / (ms * 1e-3), world * elements / (e2e_ms * 1e-3)
+
+
 # ------------------------------------------------------- secondary workloads
 # Each is measured after the headline line's timed region, on rank 0 of a
 # one-GPU run, with CUDA events on the plans' stream (the default stream).
@@ -536,12 +548,7 @@ def main():
     barrier()
     e2e_ms = 1e3 * (time.perf_counter() - t0) / e2e_steps
 
-    if dist is not None:
-        tt = torch.tensor([ms, e2e_ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms, e2e_ms = float(tt[0]), float(tt[1])
-    value = world * E / (ms * 1e-3)
-    e2e = world * E / (e2e_ms * 1e-3)
+    ms, e2e_ms, value, e2e = combine_ranks(dist, world, E, ms, e2e_ms, "cuda")
     if rank != 0:
         dist.destroy_process_group()
         return

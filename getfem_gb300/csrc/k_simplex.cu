@@ -89,8 +89,6 @@ struct EpShared {
     double Rs[kEpWarps][S][32];  // then: each warp's part of R_e
   } x;
   long long mxs[kEpWarps][32];
-  int8_t s_nterm[NB * NB];
-  int8_t s_vw[NB * NB * kMaxPairTerms];
 };
 
 // One tile (32 elements, 4 warps) of the element pass; every thread of the
@@ -105,8 +103,6 @@ __device__ __forceinline__ void simplex_element_tile(
   using SH = EpShared<DIM, QD, NB>;
   constexpr int NV = SH::NV, M = SH::M;
   constexpr int S = SH::S, RS = (S + 3) & ~3;
-  auto &s_nterm = sh.s_nterm;
-  auto &s_vw = sh.s_vw;
   auto &s_gval = sh.s_gval;
   auto &s_mass = sh.s_mass;
   auto &Gs = sh.Gs;
@@ -114,14 +110,10 @@ __device__ __forceinline__ void simplex_element_tile(
   auto &mxs = sh.mxs;
   auto &Us = sh.x.a.Us;
   auto &Rs = sh.x.Rs;
-  for (int k = threadIdx.x; k < NB * NB; k += blockDim.x) {
-    s_nterm[k] = tab->nterm[k];
-    s_mass[k] = tab->mass[k];
-  }
-  for (int k = threadIdx.x; k < NB * NB * kMaxPairTerms; k += blockDim.x) {
-    s_vw[k] = tab->vw[k];
+  // the term values (their (v,w) structure is compile time, pk_sup_*)
+  for (int k = threadIdx.x; k < NB * NB; k += blockDim.x) s_mass[k] = tab->mass[k];
+  for (int k = threadIdx.x; k < NB * NB * kMaxPairTerms; k += blockDim.x)
     s_gval[k] = tab->gval[k];
-  }
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int64_t e = tile * int64_t(32) + lane;
   const bool active = e < E;
