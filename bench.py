@@ -202,7 +202,7 @@ def _events_ms(fn, reps):
     return e0.elapsed_time(e1) / reps
 
 
-def bench_neohookean(steps):
+def bench_neohookean(steps, nx=32):
     """Q2 hexahedra 32^3 (32768 elements), compressible neo-Hookean, u = 8
     sinusoid modes of amplitude 0.05, per-element mu lognormal(0, 0.3): K + R
     (one pass) and the adjoint of the strain energy in mu and in the vertex
@@ -212,7 +212,7 @@ def bench_neohookean(steps):
     from getfem_gb300 import _lib as L
     lib = L.lib()
     rng = np.random.default_rng(3)
-    mesh = g.Mesh.regular_unit(3, 32, "hex")
+    mesh = g.Mesh.regular_unit(3, nx, "hex")
     mf = g.MeshFem(mesh, 3, degree=2)
     mim = g.MeshIm(mesh, "IM_GAUSS_PARALLELEPIPED(3,5)")
     xyz = mf.basic_dof_nodes()
@@ -252,7 +252,7 @@ def bench_neohookean(steps):
         adj()
     t_kr = _events_ms(kr, steps)
     t_adj = _events_ms(adj, steps)
-    out = {"workload": "Q2 hex 32^3 compressible neo-Hookean, IM_GAUSS_PARALLELEPIPED(3,5): "
+    out = {"workload": f"Q2 hex {nx}^3 compressible neo-Hookean, IM_GAUSS_PARALLELEPIPED(3,5): "
                        "K + R, then energy + dE/dmu + dE/dX (dE/du = R)",
            "elements": E, "n_dof": mf.nb_dof(),
            "ms_K_R": t_kr, "ms_adjoint": t_adj,
@@ -371,7 +371,7 @@ def bench_batched(steps, n_meshes=512, lo=1e3, hi=2e5):
     return out
 
 
-def bench_q4(steps):
+def bench_q4(steps, nx=64):
     """Q4 hexahedra 64^3 (262144 elements, 16.97 M DOFs), per-element
     diffusivity lognormal(0, 0.5): assembled K + R, the matrix-free apply
     R = K u (order-1 assembly, no K), and the adjoint of u^T K u in the
@@ -383,7 +383,7 @@ def bench_q4(steps):
     lib = L.lib()
     rng = np.random.default_rng(5)
     t0 = time.perf_counter()
-    mesh = g.Mesh.regular_unit(3, 64, "hex")
+    mesh = g.Mesh.regular_unit(3, nx, "hex")
     mf = g.MeshFem(mesh, 1, degree=4)
     mim = g.MeshIm(mesh, "IM_GAUSS_PARALLELEPIPED(3,9)")
     E = mesh.nb_convex()
@@ -420,7 +420,7 @@ def bench_q4(steps):
     t_kr = _events_ms(kr, steps)
     t_ap = _events_ms(apply, steps)
     t_adj = _events_ms(adj, steps)
-    out = {"workload": "Q4 hex 64^3 kappa*Grad_u.Grad_Test_u, IM_GAUSS_PARALLELEPIPED(3,9): "
+    out = {"workload": f"Q4 hex {nx}^3 kappa*Grad_u.Grad_Test_u, IM_GAUSS_PARALLELEPIPED(3,9): "
                        "K + R assembled, matrix-free R = K u, d(u^T K u)/dkappa",
            "elements": E, "n_dof": mf.nb_dof(), "nnz": nnz.value, "setup_s": setup_s,
            "ms_K_R": t_kr, "ms_matrix_free_apply": t_ap, "ms_adjoint_kappa": t_adj,
@@ -470,6 +470,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the secondary workloads (neo-Hookean, batched, Q4, CG)")
+    ap.add_argument("--secondary", choices=["neohookean", "q4", "batched", "cg"],
+                    help="run one secondary workload only (for profiling) and print it")
+    ap.add_argument("--sec-nx", type=int, default=0,
+                    help="mesh size of --secondary (default: the configuration's)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -478,6 +482,16 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.secondary:
+        import torch
+        torch.cuda.set_device(local)
+        nx = args.sec_nx
+        fn = {"neohookean": lambda: bench_neohookean(args.steps, nx or 32),
+              "q4": lambda: bench_q4(args.steps, nx or 64),
+              "batched": lambda: bench_batched(args.steps),
+              "cg": bench_poisson_cg}[args.secondary]
+        print(json.dumps(fn()), flush=True)
+        return
 
     import torch
     torch.cuda.set_device(local)
