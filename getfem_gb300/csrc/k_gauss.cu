@@ -81,6 +81,14 @@ __device__ __forceinline__ void coef_dfac(const gfgpu_coef &c, int ws, double &f
   if (c.kind == GFGPU_COEF_NODAL) fn = c.value;
 }
 
+// c + a b: one rounding (fma) or two (the reference's operation order; this
+// file is compiled with -fmad=false so that the unfused form stays unfused)
+template <bool FUSE>
+__device__ __forceinline__ double madd(double a, double b, double c) {
+  if constexpr (FUSE) return fma(a, b, c);
+  else return c + a * b;
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -97,6 +105,9 @@ __global__ void __launch_bounds__(kGpWarps * 32) gauss_potential_kernel(
     SlotPtrs slots, double *__restrict__ out_e, double *__restrict__ out_n,
     double *__restrict__ out_x, int *__restrict__ err) {
   constexpr int S = NB * QD;
+  // the neo-Hookean energy keeps the reference's unfused operation order
+  // (j1 - 3 cancels); the quadratic integrands use fused multiply-adds
+  constexpr bool kFuse = LAW != LAW_NH;
   __shared__ double us_all[kGpWarps][S];
   __shared__ double xs_all[kGpWarps][NBG * DIM];
   __shared__ int32_t en_all[kGpWarps][NB];
@@ -115,6 +126,10 @@ __global__ void __launch_bounds__(kGpWarps * 32) gauss_potential_kernel(
   const double *u = slots.p[GFGPU_SLOT_U];
   for (int c = lane; c < S; c += 32) us[c] = u[int64_t(en[c / QD]) * QD + c % QD];
   __syncwarp();
+  // u(x_q) is needed by the mass and source integrands only
+  bool need_val = false;
+  for (int t = 0; t < form.n_terms; ++t)
+    need_val |= form.terms[t].kind == GFGPU_TERM_MASS || form.terms[t].kind == GFGPU_TERM_SOURCE;
   double acc = 0.0;                  // energy or element-coefficient derivative
   double accx[NBG * DIM];            // shape derivative partials of this lane
 #pragma unroll
@@ -133,7 +148,8 @@ __global__ void __launch_bounds__(kGpWarps * 32) gauss_potential_kernel(
       for (int m = 0; m < DIM; ++m) {
         double s = 0.0;
 #pragma unroll
-        for (int v = 0; v < NBG; ++v) s += xs[v * DIM + d] * ggrad[(qq * NBG + v) * DIM + m];
+        for (int v = 0; v < NBG; ++v)
+          s = madd<kFuse>(xs[v * DIM + d], ggrad[(qq * NBG + v) * DIM + m], s);
         K[d + DIM * m] = s;
       }
     double B[DIM * DIM], det;
@@ -155,13 +171,18 @@ __global__ void __launch_bounds__(kGpWarps * 32) gauss_potential_kernel(
       double r[DIM];
 #pragma unroll
       for (int m = 0; m < DIM; ++m) r[m] = hgradT[int64_t(j * DIM + m) * nq + qq];
-      const double ph = phi[int64_t(j) * nq];
 #pragma unroll
       for (int a = 0; a < QD; ++a) {
         const double ua = us[j * QD + a];
-        uq[a] += ph * ua;
 #pragma unroll
-        for (int m = 0; m < DIM; ++m) Gr[a][m] += ua * r[m];
+        for (int m = 0; m < DIM; ++m) Gr[a][m] = madd<kFuse>(ua, r[m], Gr[a][m]);
+      }
+    }
+    if (need_val) {
+      for (int j = 0; j < NB; ++j) {
+        const double ph = phi[int64_t(j) * nq];
+#pragma unroll
+        for (int a = 0; a < QD; ++a) uq[a] = madd<kFuse>(ph, us[j * QD + a], uq[a]);
       }
     }
 #pragma unroll
@@ -170,7 +191,7 @@ __global__ void __launch_bounds__(kGpWarps * 32) gauss_potential_kernel(
       for (int d = 0; d < DIM; ++d) {
         double s = 0.0;
 #pragma unroll
-        for (int m = 0; m < DIM; ++m) s += B[d + DIM * m] * Gr[a][m];
+        for (int m = 0; m < DIM; ++m) s = madd<kFuse>(B[d + DIM * m], Gr[a][m], s);
         Gu[a][d] = s;
       }
     // integrand psi, P = dpsi/dGrad_u, and the coefficient derivatives
