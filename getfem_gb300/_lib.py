@@ -15,15 +15,17 @@ LIB_PATH = os.path.join(HERE, "libgfgpu.so")
 OK, E_INVALID, E_UNSUPPORTED, E_CUDA, E_JACOBIAN, E_NAN, E_TIMEOUT, E_NOMEM, E_STATE = range(9)
 SIMPLEX, HEX = 0, 1
 COEF_NONE, COEF_CONST, COEF_ELEMENT, COEF_NODAL = 0, 1, 2, 3
-TERM_GRADGRAD, TERM_MASS, TERM_SOURCE, TERM_NEOHOOKEAN = 1, 2, 3, 4
+TERM_GRADGRAD, TERM_MASS, TERM_SOURCE, TERM_NEOHOOKEAN, TERM_INTERNAL_P = 1, 2, 3, 4, 5
 MAX_TERMS = 8
 MAX_SLOTS = 8
 SLOT_U = 0
 REBUILD_PATTERN = 1
 WITH_VECTOR = 2
 PROFILE = 4
+CONDENSATION = 8
 SLOT_POINTS = -1
 RESULT_ROWPTR, RESULT_COLIDX, RESULT_VALUES, RESULT_VECTOR = 0, 1, 2, 3
+RESULT_INTERNAL, RESULT_COUPLING, RESULT_COUPLING_COLIDX = 4, 5, 6
 
 _STATUS_NAMES = {
     E_INVALID: "GFGPU_E_INVALID", E_UNSUPPORTED: "GFGPU_E_UNSUPPORTED", E_CUDA: "GFGPU_E_CUDA",
@@ -50,7 +52,7 @@ class Coef(C.Structure):
 
 class Term(C.Structure):
     _fields_ = [("kind", C.c_int32), ("field_slot", C.c_int32), ("scale", C.c_double),
-                ("c", Coef * 3)]
+                ("c", Coef * 3), ("aux_slot", C.c_int32), ("reserved", C.c_int32)]
 
 
 class Form(C.Structure):
@@ -109,6 +111,7 @@ _PROTOS = {
     "gfgpu_sync": (C.c_int, [C.c_void_p]),
     "gfgpu_launch_count": (C.c_int64, [C.c_void_p]),
     "gfgpu_copy_result": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "gfgpu_internal_size": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "gfgpu_kernel_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int32]),
     "gfgpu_fp64_peak": (C.c_int, [C.c_int32, C.POINTER(C.c_double)]),
     "gfgpu_assemble_vector_noalloc": (C.c_int, [C.POINTER(NoallocArgs), C.POINTER(Form),

@@ -122,14 +122,16 @@ bool simplex_form_supported(const gfgpu_form &f, int qdim, int dim, std::string 
 }
 
 // The forms of the Gauss-point kernels: GRADGRAD / MASS / SOURCE terms
-// with constant, per-element or nodal coefficients (LAW_ISO), or one
-// compressible neo-Hookean term on a 3-D vector field (LAW_NH).
+// with constant, per-element or nodal coefficients and at most one internal
+// pressure term (LAW_ISO), or one compressible neo-Hookean term on a 3-D
+// vector field (LAW_NH).
 bool gauss_form_supported(const gfgpu_form &f, int qdim, int dim, int &law, std::string &why) {
   if (f.n_terms < 1 || f.n_terms > GFGPU_MAX_TERMS) {
     why = "empty form";
     return false;
   }
   law = LAW_ISO;
+  int n_int = 0;
   for (int t = 0; t < f.n_terms; ++t) {
     const gfgpu_term &T = f.terms[t];
     if (T.kind == GFGPU_TERM_NEOHOOKEAN) {
@@ -156,10 +158,28 @@ bool gauss_form_supported(const gfgpu_form &f, int qdim, int dim, int &law, std:
         why = "bad source field slot";
         return false;
       }
+    } else if (T.kind == GFGPU_TERM_INTERNAL_P) {
+      if (++n_int > 1) {
+        why = "at most one internal-variable term";
+        return false;
+      }
+      if (qdim != 3 || dim != 3) {
+        why = "internal pressure terms are lowered for 3-D vector fields";
+        return false;
+      }
+      if (T.field_slot <= 0 || T.field_slot >= GFGPU_MAX_SLOTS || T.aux_slot <= 0 ||
+          T.aux_slot >= GFGPU_MAX_SLOTS || T.aux_slot == T.field_slot) {
+        why = "bad internal variable slots";
+        return false;
+      }
     } else if (T.kind != GFGPU_TERM_MASS) {
       why = "unknown term kind";
       return false;
     }
+  }
+  if (n_int && law == LAW_NH) {
+    why = "internal variables with the neo-Hookean law are not lowered";
+    return false;
   }
   return true;
 }
@@ -336,7 +356,10 @@ int gfgpu_plan_create(const gfgpu_space *space, const gfgpu_form *form, void *cu
         gauss_element_layout(*P);
       }
     }
-    P->kpot = gauss_potential_available(S.dim, S.kind, S.degree, S.qdim, P->law);
+    for (int t = 0; t < P->form.n_terms; ++t)
+      if (P->form.terms[t].kind == GFGPU_TERM_INTERNAL_P) P->ip_term = t;
+    // potentials of forms with an internal variable are not lowered
+    P->kpot = P->ip_term < 0 && gauss_potential_available(S.dim, S.kind, S.degree, S.qdim, P->law);
     if (!P->kmat && !P->kpot) {
       set_last_error("no kernel for this element, integration method and form");
       delete P;
@@ -374,6 +397,7 @@ int gfgpu_plan_create(const gfgpu_space *space, const gfgpu_form *form, void *cu
       std::vector<int32_t> fill(pptr.begin(), pptr.end() - 1);
       for (int64_t k = 0; k < E * nbg; ++k) padj[fill[cv[k]]++] = int32_t(k);
     }
+    if (P->ip_term >= 0) P->h_en = en;
     P->max_cand = int32_t(P->max_adj * nb);
     if (P->max_cand > 4096) throw std::runtime_error("node valence too large for the pattern kernel");
     if (P->nb > 128) throw std::runtime_error("more than 128 local nodes per element");
@@ -475,6 +499,8 @@ void gfgpu_plan_destroy(gfgpu_plan *P) {
   dfree(P->d_epart);
   dfree(P->d_npart);
   dfree(P->d_xpart);
+  dfree(P->d_int);
+  dfree(P->d_kqj);
   dfree(P->d_elem);
   dfree(P->d_rowptr);
   dfree(P->d_colidx);
@@ -528,6 +554,18 @@ static int check_slots(Plan &P, bool need_u) {
     set_last_error("variable u (slot 0) not set or of wrong size");
     return GFGPU_E_STATE;
   }
+  if (P.ip_term >= 0) {
+    const gfgpu_term &T = P.form.terms[P.ip_term];
+    const int64_t n_int = P.n_elements * P.nq;
+    if (!P.slot_ptr[T.field_slot] || P.slot_n[T.field_slot] != n_int) {
+      set_last_error("internal variable slot not set or of wrong size (n_elements * nq)");
+      return GFGPU_E_STATE;
+    }
+    if (P.cmode == 2 && (!P.slot_ptr[T.aux_slot] || P.slot_n[T.aux_slot] != n_int)) {
+      set_last_error("condensation needs the internal residual (aux slot, n_elements * nq)");
+      return GFGPU_E_STATE;
+    }
+  }
   for (int t = 0; t < P.form.n_terms; ++t) {
     const gfgpu_term &T = P.form.terms[t];
     for (int k = 0; k < 3; ++k)
@@ -578,10 +616,28 @@ int gfgpu_assemble(gfgpu_plan *P, int32_t order, int32_t flags, double *potentia
     set_last_error("orders 1 and 2 are not lowered for this element, integration method and form");
     return GFGPU_E_UNSUPPORTED;
   }
+  const bool condense = (flags & GFGPU_CONDENSATION) != 0;
+  if (condense && (P->ip_term < 0 || order != 2)) {
+    set_last_error("GFGPU_CONDENSATION: order 2 of a form with an internal variable only");
+    return GFGPU_E_INVALID;
+  }
+  if (P->ip_term >= 0 && order == 2 && !condense) {
+    set_last_error("order 2 of a form with an internal variable is lowered with condensation only");
+    return GFGPU_E_UNSUPPORTED;
+  }
+  P->cmode = P->ip_term < 0 ? 0 : (condense ? 2 : 1);
   const bool want_K = order == 2;
-  const bool want_R = order == 1 || (flags & 2);
+  // with condensation the vector is the condensed right-hand side
+  const bool want_R = order == 1 || (flags & 2) || condense;
   int rc = check_slots(*P, want_R || P->law == LAW_NH);
   if (rc) return rc;
+  if (P->ip_term >= 0) {
+    const size_t n_int = size_t(P->n_elements) * P->nq;
+    if (!P->d_int && (rc = dalloc(&P->d_int, n_int))) return rc;
+    if (condense && !P->d_kqj && (rc = dalloc(&P->d_kqj, n_int * P->nb * P->qdim))) return rc;
+  }
+  // a pattern built without the condensed coupling may miss its entries
+  const bool repattern = condense && P->nnz >= 0 && P->pattern_cmode != 2;
   // element scratch, allocated at the first order-1 or order-2 assembly
   if (!P->d_elem && (rc = dalloc(&P->d_elem, size_t(P->n_elements) * P->lay.stride))) return rc;
   const bool prof = (flags & GFGPU_PROFILE) != 0;
@@ -595,10 +651,11 @@ int gfgpu_assemble(gfgpu_plan *P, int32_t order, int32_t flags, double *potentia
   else if (P->affine_hex) GF_CUDA(launch_affine_hex_pass(*P, want_K || P->nnz < 0));
   else GF_CUDA(launch_hex_element_pass(*P, want_K || P->nnz < 0));
   if (prof) GF_CUDA(cudaEventRecord(P->ev[1], P->stream));
-  if ((want_K && (P->nnz < 0 || (flags & GFGPU_REBUILD_PATTERN))) || P->nnz < 0) {
+  if ((want_K && (P->nnz < 0 || (flags & GFGPU_REBUILD_PATTERN) || repattern)) || P->nnz < 0) {
     // the pattern is built at the first order-2 assembly; an order-1
     // assembly needs the node-level part of it for its row walk
     if ((rc = build_pattern(*P))) return rc;
+    P->pattern_cmode = P->cmode;
   }
   if (prof) GF_CUDA(cudaEventRecord(P->ev[2], P->stream));
   GF_CUDA(launch_gather(*P, want_K, want_R));
@@ -1004,10 +1061,46 @@ int gfgpu_kernel_times(gfgpu_plan *P, float *times, int32_t n) {
   return GFGPU_OK;
 }
 
+int gfgpu_internal_size(gfgpu_plan *P, int64_t *n_int, int64_t *row_len) {
+  if (!P || !n_int || !row_len) {
+    set_last_error("gfgpu_internal_size: bad arguments");
+    return GFGPU_E_INVALID;
+  }
+  const bool has = P->ip_term >= 0;
+  *n_int = has ? P->n_elements * P->nq : 0;
+  *row_len = has ? int64_t(P->nb) * P->qdim : 0;
+  return GFGPU_OK;
+}
+
 int gfgpu_copy_result(gfgpu_plan *P, int32_t which, void *dst) {
-  if (!P || !dst || which < 0 || which > 3) {
+  if (!P || !dst || which < 0 || which > GFGPU_RESULT_COUPLING_COLIDX) {
     set_last_error("gfgpu_copy_result: bad arguments");
     return GFGPU_E_INVALID;
+  }
+  if (which >= GFGPU_RESULT_INTERNAL) {
+    const size_t n_int = size_t(P->n_elements) * P->nq, row = size_t(P->nb) * P->qdim;
+    if (P->ip_term < 0 || !P->d_int || (which != GFGPU_RESULT_INTERNAL && !P->d_kqj)) {
+      set_last_error("no internal-variable result: assemble a form with an internal variable "
+                     "(order 1, or order 2 with GFGPU_CONDENSATION for the coupling)");
+      return GFGPU_E_STATE;
+    }
+    if (which == GFGPU_RESULT_COUPLING_COLIDX) {
+      // the element's DOFs in local order, once per Gauss point
+      std::vector<int32_t> cols(n_int * row);
+      const int nb = P->nb, qd = P->qdim, nq = P->nq;
+      for (int64_t e = 0; e < P->n_elements; ++e)
+        for (int q = 0; q < nq; ++q) {
+          int32_t *c = cols.data() + (size_t(e) * nq + q) * row;
+          for (int j = 0; j < nb; ++j)
+            for (int b = 0; b < qd; ++b) c[j * qd + b] = P->h_en[size_t(e) * nb + j] * qd + b;
+        }
+      GF_CUDA(cudaMemcpy(dst, cols.data(), cols.size() * sizeof(int32_t), cudaMemcpyDefault));
+      return GFGPU_OK;
+    }
+    const double *src = which == GFGPU_RESULT_INTERNAL ? P->d_int : P->d_kqj;
+    const size_t bytes = (which == GFGPU_RESULT_INTERNAL ? n_int : n_int * row) * sizeof(double);
+    GF_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, P->stream));
+    return check_err(*P);
   }
   if (which != GFGPU_RESULT_VECTOR && P->nnz < 0) {
     set_last_error("no pattern yet: assemble order 2 first");

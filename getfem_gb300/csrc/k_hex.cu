@@ -23,6 +23,17 @@
 //      element-matrix entries it owns (registers).
 //  C   R_e[(i,a)] = sum_q P_q[a,k] g_qik (+ mass, load).
 //
+// An internal im_data pressure (GFGPU_TERM_INTERNAL_P) lives at the Gauss
+// points, so its block K_pp of the element matrix is diagonal, one scalar per
+// point, and the reference's element-level static condensation
+// (compile_and_exec.cc:5562-5790: invert KQQ, KQJpr = KQQ^-1 KQJ, RQpr =
+// KQQ^-1 R_Q / coeff, K_IJ -= K_IQ KQJpr, R_I -= K_IQ RQpr) reduces to a
+// per-point Schur complement done in A1: with K_up = c0 Div(Test_u),
+// K_pu = scale k Div_u and K_pp = scale (1 + 3 c2 p^2), the condensed
+// tangent adds -c0 k / (1 + 3 c2 p^2) to the isotropic c0 d_ak d_bl part,
+// the condensed residual is -c0 RQpr Div(Test_u) per point, and the
+// coupling rows KQJpr = k / (1 + 3 c2 p^2) Div(phi_j) are written per point.
+//
 // All per-q quantities are scaled by w_q J.  Output: the element scratch
 // layout read by the pattern build and the row gather (K_e rows, V_e = R_e,
 // threshold 1e-14 max|K_e|).
@@ -126,7 +137,8 @@ __global__ void __launch_bounds__(kHexThreads, 2) hex_element_kernel(
     const int32_t *__restrict__ enode, const double *__restrict__ hval,
     const double *__restrict__ hgrad, const double *__restrict__ ggrad,
     const double *__restrict__ hw, const int32_t *__restrict__ tri, KeLayout L,
-    gfgpu_form form, SlotPtrs slots, double *__restrict__ out, int *__restrict__ err) {
+    gfgpu_form form, SlotPtrs slots, double *__restrict__ out, int *__restrict__ err,
+    int ipt, int cmode, double *__restrict__ out_int, double *__restrict__ out_kqj) {
   using M = HexSmem<QD, NB, NBG, NQ, LAW>;
   constexpr int S = M::S, NA = M::NA;
   extern __shared__ __align__(16) double sm[];
@@ -283,6 +295,28 @@ __global__ void __launch_bounds__(kHexThreads, 2) hex_element_kernel(
             for (int b = 0; b < QD; ++b) uq[b] += phi[j] * us[j * QD + b];
 #pragma unroll
           for (int b = 0; b < QD; ++b) tv[b] = a0 * uq[b];
+        } else if (T.kind == GFGPU_TERM_INTERNAL_P) {
+          // the internal pressure at this Gauss point (im_data index e*NQ+q)
+          const double sp = coef_at(T.c[0], slots, e, ens, phi, NB);
+          const double kb = coef_at(T.c[1], slots, e, ens, phi, NB);
+          const double c3 = coef_at(T.c[2], slots, e, ens, phi, NB);
+          const int64_t iq = e * NQ + q;
+          const double p = slots.p[T.field_slot][iq];
+          if (cmode == 2) {
+            // K_pp^-1, then KQJpr and RQpr as the reference forms them
+            const double inv = 1.0 / (sc * (1.0 + c3 * (3.0 * (p * p))));
+            if (!isfinite(inv)) set_err(err, ERR_NAN);
+            const double kq = inv * (sc * kb);
+            const double rqpr = bad ? 0.0 : (inv * slots.p[T.aux_slot][iq]) / wJ;
+            c0 += -(sp * kq);
+            tv[0] = -(sp * rqpr);
+            tv[1] = kq;
+            out_int[iq] = rqpr;
+          } else {
+            tv[0] = sp * p;
+            tv[1] = 0.0;
+            out_int[iq] = wJ * (sc * ((p + c3 * (p * p * p)) + kb * div));
+          }
         } else if (T.kind == GFGPU_TERM_SOURCE) {
           const double a0 =
               (T.c[0].kind == GFGPU_COEF_NONE ? 1.0 : coef_at(T.c[0], slots, e, ens, phi, NB)) * sc;
@@ -314,6 +348,15 @@ __global__ void __launch_bounds__(kHexThreads, 2) hex_element_kernel(
     }
   }
   __syncthreads();
+  if constexpr (LAW == LAW_ISO && QD == 3) {
+    // coupling rows KQJpr(e*NQ + q, (j, b)) = kq_q g_qjb: with QD == 3 the
+    // row entry (j, b) of point q is gq[q*S + j*3 + b]
+    if (cmode == 2 && ipt >= 0) {
+      double *ok = out_kqj + e * (NQ * S);
+      for (int z = tid; z < NQ * S; z += kHexThreads)
+        ok[z] = rq[(z / S) * kRes + RTERM + 3 * ipt + 1] * gq[z];
+    }
+  }
   if constexpr (LAW == LAW_NH && WANT_K) {
     // ---------------------------------------------------------------- A2
     for (int z = tid; z < NQ * 81; z += kHexThreads) {
@@ -437,7 +480,12 @@ __global__ void __launch_bounds__(kHexThreads, 2) hex_element_kernel(
         for (int tt = 0; tt < form.n_terms; ++tt) {
           const int kind = form.terms[tt].kind;
           const double *tv = rs + RTERM + 3 * tt;
-          if (kind == GFGPU_TERM_GRADGRAD) {
+          if (kind == GFGPU_TERM_INTERNAL_P) {
+            // order 1: p Div(Test_u); condensation: -c0 RQpr Div(Test_u)
+            t += tv[0] * g[ra];
+          } else if (cmode == 2) {
+            // the condensed vector holds the condensation terms only
+          } else if (kind == GFGPU_TERM_GRADGRAD) {
             double v = 0.0;
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
@@ -477,7 +525,7 @@ cudaError_t launch_hex_t(Plan &P, const SlotPtrs &sp, bool want_K) {
   if (ce != cudaSuccess) return ce;
   kern<<<unsigned(P.n_elements), kHexThreads, M::bytes, P.stream>>>(
       P.n_elements, P.d_points, P.d_cv, P.d_enode, P.d_hval, P.d_hgrad, P.d_ggrad, P.d_hw,
-      P.d_tri, P.lay, P.form, sp, P.d_elem, P.d_err);
+      P.d_tri, P.lay, P.form, sp, P.d_elem, P.d_err, P.ip_term, P.cmode, P.d_int, P.d_kqj);
   return cudaGetLastError();
 }
 
@@ -489,9 +537,9 @@ bool gauss_element_available(int kind, int law, int degree, int qdim, int nq) {
     if (law == LAW_NH) return qdim == 3 && nq_ok;
     return (qdim == 1 || qdim == 3) && nq_ok;
   }
-  // tetrahedra: the neo-Hookean law (the linear forms take the simplex pass)
-  return law == LAW_NH && qdim == 3 &&
-         ((degree == 2 && nq == 15) || (degree == 1 && (nq == 4 || nq == 15)));
+  // tetrahedra: the neo-Hookean law, and the isotropic forms of 3-D vector
+  // fields that the simplex pass does not take (internal variables)
+  return qdim == 3 && ((degree == 2 && nq == 15) || (degree == 1 && (nq == 4 || nq == 15)));
 }
 
 // Element scratch layout of the Gauss-point kernel.
@@ -526,6 +574,9 @@ cudaError_t launch_hex_element_pass(Plan &P, bool want_K) {
     if (P.law == LAW_NH && k == 2 && nq == 15) ce = launch_hex_t<3, 10, 4, 15, LAW_NH>(P, sp, want_K);
     else if (P.law == LAW_NH && k == 1 && nq == 4) ce = launch_hex_t<3, 4, 4, 4, LAW_NH>(P, sp, want_K);
     else if (P.law == LAW_NH && k == 1 && nq == 15) ce = launch_hex_t<3, 4, 4, 15, LAW_NH>(P, sp, want_K);
+    else if (q == 3 && k == 2 && nq == 15) ce = launch_hex_t<3, 10, 4, 15, LAW_ISO>(P, sp, want_K);
+    else if (q == 3 && k == 1 && nq == 4) ce = launch_hex_t<3, 4, 4, 4, LAW_ISO>(P, sp, want_K);
+    else if (q == 3 && k == 1 && nq == 15) ce = launch_hex_t<3, 4, 4, 15, LAW_ISO>(P, sp, want_K);
   } else if (P.law == LAW_NH) {
     if (k == 2 && nq == 27) ce = launch_hex_t<3, 27, 8, 27, LAW_NH>(P, sp, want_K);
     else if (k == 1 && nq == 8) ce = launch_hex_t<3, 8, 8, 8, LAW_NH>(P, sp, want_K);

@@ -128,6 +128,15 @@ struct Plan {
   int32_t *d_padj_ptr = nullptr, *d_padj = nullptr;
   // per-element partials of potentials and gradients (allocated on use)
   double *d_epart = nullptr, *d_npart = nullptr, *d_xpart = nullptr;
+  // internal im_data variable (GFGPU_TERM_INTERNAL_P): term index, the
+  // mode of the current pass (0 none, 1 order-1 residuals, 2 condensation),
+  // the mode the CSR pattern was built in, the per-Gauss-point results
+  // (n_elements*nq) and the coupling rows (n_elements*nq x nb*qdim)
+  int ip_term = -1;
+  int cmode = 0;
+  int pattern_cmode = -1;
+  double *d_int = nullptr, *d_kqj = nullptr;
+  std::vector<int32_t> h_en;    // E x nb DOF node ids (coupling columns)
 
   // element pass scratch
   double *d_elem = nullptr;     // E x lay.stride

@@ -306,7 +306,8 @@ class FieldInfo:
     name: str
     kind: str            # 'variable', 'element' (P0), 'nodal' (scalar field on
                          # the variable's scalar mesh_fem), 'vfield' (field on
-                         # the variable's mesh_fem), 'const'
+                         # the variable's mesh_fem), 'const', 'internal' (an
+                         # internal im_data variable, scalar per Gauss point)
     qdim: int = 1
     value: object = None  # for 'const': the numpy value
     slot: int = -1
@@ -319,6 +320,10 @@ class Lowered:
     order1: list          # terms whose order-1 assembly gives the residual
     order0: list          # potential terms
     max_order: int
+    # an internal variable's part of a displacement / pressure pair
+    # (merged into one TERM_INTERNAL_P by the workspace): {'name', 'sp'} for
+    # the u equation, {'name', 'scale', 'c3', 'kb'} for the p equation
+    internal: dict = None
 
 
 def _term(kind, scale=1.0, c=(None, None, None), field_slot=0):
@@ -368,7 +373,7 @@ class _Probe:
         for f in self.fields.values():
             if f.kind == "const":
                 e[f.name] = f.value
-            elif f.kind in ("element", "nodal"):
+            elif f.kind in ("element", "nodal", "internal"):
                 e[f.name] = theta.get(f.name, 0.0)
             elif f.kind == "vfield":
                 val = theta.get(f.name, np.zeros(f.qdim))
@@ -702,6 +707,100 @@ def _lower_potential(tree, var, dim, fields) -> "Lowered":
     return Lowered(order2=dbl, order1=dbl + src, order0=terms2 + src, max_order=0)
 
 
+def _internal_pressure_part(tree, var, dim, fields, pname):
+    """u equation of a displacement / pressure pair: the part of the weak form
+    that the internal variable p contributes must be sp p Div_Test_u, with sp
+    a constant (the reference's (-p*Id(meshdim)):Grad_Test_u has sp = -1)."""
+    Q, N = var.qdim, dim
+    P = _Probe(tree, var, dim, fields)
+    vals, grads = _basis(Q, N)
+    zQ, zG = np.zeros(Q), np.zeros((Q, N))
+    th0 = {nm: 1.0 for nm, f in fields.items() if f.kind in ("element", "nodal")}
+    rng = np.random.default_rng(11)
+    Ur, GUr = rng.uniform(-1, 1, Q), rng.uniform(-1, 1, (Q, N))
+    sp = None
+    for V, GV in [(v, zG) for v in vals] + [(zQ, g) for g in grads]:
+        for th_extra in ({}, {nm: 2.0 for nm in th0}):
+            th = dict(th0, **th_extra)
+            d1 = P.eval(V=V, GV=GV, theta=dict(th, **{pname: 1.0}), U=zQ, GU=zG) - \
+                P.eval(V=V, GV=GV, theta=th, U=zQ, GU=zG)
+            d2 = P.eval(V=V, GV=GV, theta=dict(th, **{pname: 2.0}), U=Ur, GU=GUr) - \
+                P.eval(V=V, GV=GV, theta=th, U=Ur, GU=GUr)
+            div = float(np.trace(GV)) if Q == N and Q > 1 else 0.0
+            if sp is None and div != 0.0:
+                sp = d1 / div
+            want1 = (sp or 0.0) * div
+            if abs(d1 - want1) > 1e-12 * max(1.0, abs(d1)) or \
+                    abs(d2 - 2.0 * want1) > 1e-12 * max(1.0, abs(d2)):
+                raise L.UnsupportedExpression(
+                    L.E_UNSUPPORTED, f"the internal variable {pname} must enter the "
+                    f"displacement equation as (c {pname} Id(meshdim)):Grad_Test_u")
+    if not sp:
+        raise L.UnsupportedExpression(L.E_UNSUPPORTED, f"{pname} does not couple to Test_u")
+    return float(sp)
+
+
+def _internal_equation(tree, var, dim, fields, pname):
+    """p equation: the weak form times Test_p must be
+    scale (p + c3 p^3 + kb Div_u), kb a constant or one element / nodal datum
+    times a constant, scale and c3 constants."""
+    Q, N = var.qdim, dim
+    if Q != N or Q != 3:
+        raise L.UnsupportedExpression(L.E_UNSUPPORTED,
+                                      "internal pressure equations on 3-D vector fields only")
+    scal = [nm for nm, f in fields.items() if f.kind in ("element", "nodal")]
+    zQ, zG = np.zeros(Q), np.zeros((Q, N))
+
+    def f(p, GU, theta=None, U=None):
+        th = dict(theta or {})
+        th[pname] = p
+        env = _Probe(tree, var, dim, fields).env(U=zQ if U is None else U, GU=GU, V=None,
+                                                  GV=None, theta=th)
+        env["Test_" + pname] = 1.0
+        return float(evaluate(tree, env))
+    th1 = {nm: 1.0 for nm in scal}
+    if abs(f(0.0, zG, th1)) > 0:
+        raise L.UnsupportedExpression(L.E_UNSUPPORTED,
+                                      f"constant terms in the {pname} equation are not lowered")
+    s1, s2 = f(1.0, zG, th1), f(2.0, zG, th1)
+    scale = (8.0 * s1 - s2) / 6.0
+    c3s = (s2 - 2.0 * s1) / 6.0
+    if scale == 0.0:
+        raise L.UnsupportedExpression(L.E_UNSUPPORTED, f"{pname} equation without a {pname} term")
+    for pv in (0.7, -1.3):
+        want = scale * pv + c3s * pv ** 3
+        for th in (th1, {nm: 2.5 for nm in scal}):
+            if abs(f(pv, zG, th) - want) > 1e-12 * max(1.0, abs(want)):
+                raise L.UnsupportedExpression(
+                    L.E_UNSUPPORTED, f"the {pname} equation must be scale ({pname} + "
+                    f"c {pname}^3 + k Div_u) with constant scale and c")
+
+    # the Div_u coefficient, linear in the scalar data fields
+    def kb_of(theta):
+        return np.array([f(0.0, np.diag([1.0, 0.0, 0.0]), theta)])
+    base, coeffs = _linear_in_fields(kb_of, scal, f"the Div_{var.name} coefficient")
+    entries = _coef_terms(base[0] / scale, {k: v[0] / scale for k, v in coeffs.items()}, fields)
+    if len(entries) != 1:
+        raise L.UnsupportedExpression(L.E_UNSUPPORTED,
+                                      f"the Div_{var.name} coefficient must be one field "
+                                      "times a constant")
+    # isotropy (a multiple of Div_u) and no other dependence on u or cross terms
+    rng = np.random.default_rng(5)
+    th = {nm: float(rng.uniform(0.5, 2.0)) for nm in scal}
+    kb = float(kb_of(th)[0])
+    GUr, Ur = rng.uniform(-1, 1, (Q, N)), rng.uniform(-1, 1, Q)
+    for pv in (0.0, 0.9):
+        want = scale * pv + c3s * pv ** 3 + kb * float(np.trace(GUr))
+        if abs(f(pv, GUr, th, Ur) - want) > 1e-10 * max(1.0, abs(want)):
+            raise L.UnsupportedExpression(
+                L.E_UNSUPPORTED, f"the {pname} equation depends on {var.name} other than "
+                f"through Div_{var.name}")
+    c3 = c3s / scale
+    return {"name": pname, "scale": float(scale),
+            "c3": _coef(L.COEF_CONST, 0, float(c3)) if c3 != 0 else None,
+            "kb": entries[0]}
+
+
 def lower(expr: str, var: FieldInfo, dim: int, fields: dict, add_derivative_order=2) -> Lowered:
     """Lower a GWFL expression over one fem variable to descriptor terms."""
     tree = parse(expr)
@@ -722,11 +821,34 @@ def lower(expr: str, var: FieldInfo, dim: int, fields: dict, add_derivative_orde
             continue
         if base != name and base not in fields:
             raise L.UnsupportedExpression(L.E_UNSUPPORTED, f"unknown name {s!r} in {expr!r}")
-        if base != name and s != base:
+        if base != name and s != base and not (
+                fields[base].kind == "internal" and s == "Test_" + base):
             raise L.UnsupportedExpression(L.E_UNSUPPORTED,
                                           f"derivatives of data fields ({s}) are not lowered")
     if has_test2 and not has_test:
         raise L.UnsupportedExpression(L.E_UNSUPPORTED, "Test2 without Test")
+    internal = [nm for nm, f in fields.items() if f.kind == "internal"]
+    for pname in internal:
+        if any(s in used for s in ("Grad_" + pname, "Test2_" + pname, "Grad_Test_" + pname)):
+            raise L.UnsupportedExpression(L.E_UNSUPPORTED,
+                                          f"{pname} is an im_data variable: no gradient")
+        if "Test_" + pname in used:
+            if has_test or has_test2:
+                raise L.UnsupportedExpression(
+                    L.E_UNSUPPORTED, f"Test_{pname} and Test_{name} in one expression")
+            part = _internal_equation(tree, var, dim, fields, pname)
+            return Lowered(order2=[], order1=[], order0=[], max_order=2, internal=part)
+    used_int = [nm for nm in internal if nm in used]
+    if used_int:
+        if len(used_int) > 1 or not has_test or has_test2:
+            raise L.UnsupportedExpression(L.E_UNSUPPORTED,
+                                          "one internal variable, in a residual-form term")
+        pname = used_int[0]
+        sp = _internal_pressure_part(tree, var, dim, fields, pname)
+        # the rest of the expression, with p = 0 (the probe's default)
+        terms2, terms1 = _lower_linear(tree, var, dim, fields, False)
+        return Lowered(order2=terms2, order1=terms2 + terms1, order0=[], max_order=2,
+                       internal={"name": pname, "sp": sp})
     nh = _match_neohookean(tree, var)
     nh_pot = None if has_test else _match_neohookean_potential(tree, var)
     if not has_test and nh_pot is None:
@@ -775,6 +897,7 @@ def to_form(terms: list) -> L.Form:
         T.kind = t["kind"]
         T.scale = t["scale"]
         T.field_slot = t["field_slot"]
+        T.aux_slot = t.get("aux_slot", 0)
         for k in range(3):
             c = t["c"][k]
             if c is None:

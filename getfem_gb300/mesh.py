@@ -151,3 +151,19 @@ class MeshIm:
         w = np.empty(nq.value)
         L.check(lib.gfgpu_quadrature(self.im.encode(), C.byref(d), C.byref(nq), _ptr(pts), _ptr(w)))
         return pts, w
+
+
+class ImData:
+    """Scalar data at the integration points of a mesh_im (getfem::im_data,
+    getfem/getfem_im_data.h), one value per element Gauss point; point q of
+    element e has index e * nq + q (im_data::index_of_point,
+    src/getfem_im_data.cc:110-118, for a mesh_im over all convexes)."""
+
+    def __init__(self, mim: MeshIm):
+        self.mim = mim
+
+    def nb_index(self) -> int:
+        return self.mim.mesh.nb_convex() * self.mim.nq
+
+    def nb_tensor_elem(self) -> int:
+        return 1

@@ -79,14 +79,30 @@ typedef enum {
   /* int ((Id+Grad_u)*Compressible_Neo_Hookean_PK2(Grad_u,[C1;D1])):Grad_Test_u
      (getfem_nonlinear_elasticity.cc:2319-2320, law :503-600), C1 = c[0],
      D1 = c[1]; dim 3 only */
-  GFGPU_TERM_NEOHOOKEAN = 4
+  GFGPU_TERM_NEOHOOKEAN = 4,
+  /* A displacement / pressure pair whose pressure p is an internal im_data
+     variable (ga_workspace::add_internal_im_variable, getfem/
+     getfem_generic_assembly.h:459; one scalar per element Gauss point,
+     index e*nq + q as im_data::index_of_point numbers them for a mesh_im
+     over all convexes, src/getfem_im_data.cc:110-118, :187-197):
+       u equation   (c[0] p Id(dim)) : Grad_Test_u
+       p equation   scale (p + c[2] p^3 + c[1] Div_u) Test_p
+     field_slot: p (n_elements*nq values); aux_slot: the residual of the p
+     rows that static condensation reads (the internal part of the assembled
+     vector, workspace.cc:826-833).  3-D vector fields (qdim == dim == 3),
+     Gauss-point kernel, at most one such term per form.  Order 1 assembles
+     the u residual and the p residual (gfgpu_copy_result
+     GFGPU_RESULT_INTERNAL); order 2 needs GFGPU_CONDENSATION. */
+  GFGPU_TERM_INTERNAL_P = 5
 } gfgpu_term_kind;
 
 typedef struct {
   int32_t kind;       /* gfgpu_term_kind */
-  int32_t field_slot; /* SOURCE only */
+  int32_t field_slot; /* SOURCE: the load field; INTERNAL_P: p */
   double scale;       /* overall factor of the term (e.g. -1) */
   gfgpu_coef c[3];
+  int32_t aux_slot;   /* INTERNAL_P: residual of the p rows (order 2) */
+  int32_t reserved;
 } gfgpu_term;
 
 #define GFGPU_MAX_TERMS 8
@@ -206,6 +222,19 @@ int gfgpu_device_vector(gfgpu_plan *plan, double **vec);
                                    in the same pass */
 #define GFGPU_PROFILE 4         /* record CUDA events around each kernel of
                                    this call (gfgpu_kernel_times) */
+#define GFGPU_CONDENSATION 8    /* order 2 of a form with an INTERNAL_P term:
+                                   static condensation of p
+                                   (ga_workspace::assembly(2, true),
+                                   compile_and_exec.cc:5562-5790, :8429-8640).
+                                   K <- K_uu - K_up K_pp^-1 K_pu (condensed,
+                                   into the CSR); vector <- -K_up K_pp^-1 R_p
+                                   (the prim rows of the reference's V, which
+                                   it zeroes first); GFGPU_RESULT_INTERNAL <-
+                                   K_pp^-1 R_p / (w J) per Gauss point;
+                                   GFGPU_RESULT_COUPLING <- K_pp^-1 K_pu, one
+                                   row of nb*qdim entries per Gauss point
+                                   (the internal coupling matrix KQJpr,
+                                   getfem_generic_assembly.h:409-419) */
 
 /* Assembles on the device.  order 2: K values into the plan's CSR (the
    pattern is built at the first call, or when GFGPU_REBUILD_PATTERN);
@@ -229,7 +258,21 @@ int gfgpu_assemble_host(gfgpu_plan *plan, const double *u, double *vals, double 
 #define GFGPU_RESULT_COLIDX 1
 #define GFGPU_RESULT_VALUES 2
 #define GFGPU_RESULT_VECTOR 3
+/* Forms with an INTERNAL_P term (n_int = n_elements * nq rows, index
+   e*nq + q; each coupling row has nb*qdim entries, the element's DOFs in
+   local order (node-major, component fastest), stored unsorted and without
+   the 1e-14 drop of add_elem_matrix):
+   4: internal vector (n_int double): order 1 the p residual, order 2 with
+      condensation the internal solution K_pp^-1 R_p / (w J);
+   5: coupling values (n_int * nb*qdim double), 6: their column DOFs
+      (n_int * nb*qdim int32). */
+#define GFGPU_RESULT_INTERNAL 4
+#define GFGPU_RESULT_COUPLING 5
+#define GFGPU_RESULT_COUPLING_COLIDX 6
 int gfgpu_copy_result(gfgpu_plan *plan, int32_t which, void *dst);
+/* Sizes of the internal-variable results: n_int rows, row_len entries per
+   coupling row (0, 0 for forms without an INTERNAL_P term). */
+int gfgpu_internal_size(gfgpu_plan *plan, int64_t *n_int, int64_t *row_len);
 
 /* Adjoint of the potential (order-0 assembly of the plan's form, with u and
    the data fixed) with respect to

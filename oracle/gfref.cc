@@ -26,6 +26,15 @@
 //  * OpenMP element partition with per-thread private outputs and a final
 //    reduction (src/getfem_models.cc:2686-2730,
 //    getfem/getfem_accumulated_distro.h:150-223)
+//  * an internal im_data variable p (one value per element Gauss point) and
+//    its static condensation at order 2, instruction by instruction at each
+//    Gauss point: the KIQ / KQJ / KQQ tensors copied from the term
+//    (compile_and_exec.cc:8219-8310), extraction of the cached residual
+//    (:4804-4830), ga_instruction_condensation_sub (:5562-5671: KQQ^-1,
+//    KQJpr = KQQ^-1 KQJ, RQpr = KQQ^-1 R_Q / coeff), the KQJpr rows
+//    (imd_mf assembly, :5192-5230, no coeff) and RQpr written into the
+//    internal rows (:4737-4765, initialize), condensation_super_K / _R
+//    (:5718-5790) assembled with coeff into K and the primary rows of V
 #include "gfref.h"
 #include "../getfem_gb300/csrc/host/refpoly.h"
 
@@ -76,42 +85,54 @@ struct Element {
 // -------------------------------------------------------------- quadrature
 // Point sets of the integration methods (cubature/TRIANGLE_2.IM,
 // TRIANGLE_4.IM, TETRA_2.IM, TETRA_5.IM orbits expanded; Gauss-Legendre
-// IM_GAUSS1D and its tensor product IM_GAUSS_PARALLELEPIPED).
+// IM_GAUSS1D and its tensor product IM_GAUSS_PARALLELEPIPED), in the
+// reference's order of points.
 struct Rule {
   int dim = 0;
   std::vector<std::vector<double>> pts;
   std::vector<double> w;
 };
 
-void add_orbit(Rule &r, int dim, double a, double b, double w, int type) {
-  // barycentric orbits used by the tables: type 0 = centroid, 1 = (a,a,..,1-na),
-  // 2 = (a,a,b,b) six points (3-D) with b = 1/2 - a
-  std::vector<std::vector<double>> out;
-  if (type == 0) {
-    out.push_back(std::vector<double>(dim, a));
-  } else if (type == 1) {
-    std::vector<double> bary(dim + 1, a);
-    bary[0] = 1.0 - dim * a;
-    // cartesian coordinates are bary[1..dim]; enumerate distinct permutations
-    std::sort(bary.begin(), bary.end());
-    std::vector<std::vector<double>> seen;
-    do {
-      std::vector<double> x(bary.begin() + 1, bary.end());
-      if (std::find(seen.begin(), seen.end(), x) == seen.end()) seen.push_back(x);
-    } while (std::next_permutation(bary.begin(), bary.end()));
-    out = seen;
-  } else {
-    std::vector<double> bary = {a, a, b, b};
-    std::sort(bary.begin(), bary.end());
-    std::vector<std::vector<double>> seen;
-    do {
-      std::vector<double> x(bary.begin() + 1, bary.end());
-      if (std::find(seen.begin(), seen.end(), x) == seen.end()) seen.push_back(x);
-    } while (std::next_permutation(bary.begin(), bary.end()));
-    out = seen;
+// approx_integration::add_point_full_symmetric for simplices
+// (src/getfem_integration.cc:278-303): with pt3 = (x, 1 - sum x), every
+// index vector ind (ind[0] fastest, digits 0..dim) with distinct digits gives
+// the point (pt3[ind[0]], ..., pt3[ind[dim-1]]), added unless already present
+// (add_point_norepeat, :271-276).  The points are listed in that order, which
+// is the order im_data numbers them.
+void add_full_symmetric(Rule &r, int dim, std::vector<double> x, double w) {
+  std::vector<double> pt3(x);
+  double last = 1.0;
+  for (int k = 0; k < dim; ++k) last -= x[k];
+  pt3.push_back(last);
+  std::vector<int> ind(dim, 0);
+  const size_t first = r.pts.size();
+  for (;;) {
+    std::vector<bool> used(dim + 1, false);
+    bool good = true;
+    for (int k = 0; k < dim; ++k) {
+      if (used[ind[k]]) {
+        good = false;
+        break;
+      }
+      used[ind[k]] = true;
+    }
+    if (good) {
+      std::vector<double> pt2(dim);
+      for (int k = 0; k < dim; ++k) pt2[k] = pt3[ind[k]];
+      if (std::find(r.pts.begin() + first, r.pts.end(), pt2) == r.pts.end())
+        r.pts.push_back(pt2), r.w.push_back(w);
+    }
+    int k = 0;
+    ind[0]++;
+    while (ind[k] == dim + 1) {
+      ind[k++] = 0;
+      if (k == dim) {
+        r.dim = dim;
+        return;
+      }
+      ind[k]++;
+    }
   }
-  for (auto &x : out) r.pts.push_back(x), r.w.push_back(w);
-  r.dim = dim;
 }
 
 void gauss01(int n, std::vector<double> &x, std::vector<double> &w) {
@@ -138,6 +159,16 @@ void gauss01(int n, std::vector<double> &x, std::vector<double> &w) {
     x[k] = double((1 - z) / 2);
     w[k] = double(1 / ((1 - z * z) * dp * dp));
   }
+  // IM_GAUSS1D lists its points as the symmetric pairs (x, 1 - x), x
+  // ascending, then the midpoint (the order of the reference's im_points)
+  std::vector<double> xs, ws;
+  for (int k = 0; k < n / 2; ++k) {
+    xs.push_back(x[k]), ws.push_back(w[k]);
+    xs.push_back(x[n - 1 - k]), ws.push_back(w[n - 1 - k]);
+  }
+  if (n % 2) xs.push_back(x[n / 2]), ws.push_back(w[n / 2]);
+  x = xs;
+  w = ws;
 }
 
 bool make_rule(const std::string &nm, Rule &r) {
@@ -145,18 +176,25 @@ bool make_rule(const std::string &nm, Rule &r) {
   for (char c : nm)
     if (c != ' ') s += c;
   r = Rule();
+  // the generating points and weights of cubature/TRIANGLE_2.IM,
+  // TRIANGLE_4.IM, TETRA_2.IM and TETRA_5.IM (node type 1: full symmetric;
+  // type 0: the point alone)
   if (s == "IM_TRIANGLE(2)") {
-    add_orbit(r, 2, 1. / 6, 0, 1. / 6, 1);
+    add_full_symmetric(r, 2, {1. / 6, 1. / 6}, 1. / 6);
   } else if (s == "IM_TRIANGLE(4)") {
-    add_orbit(r, 2, 0.445948490915965, 0, 0.111690794839005, 1);
-    add_orbit(r, 2, 0.091576213509771, 0, 0.054975871827661, 1);
+    add_full_symmetric(r, 2, {0.445948490915965, 0.445948490915965}, 0.111690794839005);
+    add_full_symmetric(r, 2, {0.091576213509771, 0.091576213509771}, 0.054975871827661);
   } else if (s == "IM_TETRAHEDRON(2)") {
-    add_orbit(r, 3, 0.13819660112501052, 0, 1. / 24, 1);
+    add_full_symmetric(r, 3, {0.13819660112501052, 0.13819660112501052, 0.13819660112501052},
+                       1. / 24);
   } else if (s == "IM_TETRAHEDRON(5)") {
-    add_orbit(r, 3, 0.25, 0, 0.019753086419753086, 0);
-    add_orbit(r, 3, 0.31979362782962991, 0, 0.011511367871045398, 1);
-    add_orbit(r, 3, 0.091971078052723033, 0, 0.01198951396316977, 1);
-    add_orbit(r, 3, 0.056350832689629156, 0.44364916731037084, 0.008818342151675485, 2);
+    r.pts.push_back({0.25, 0.25, 0.25}), r.w.push_back(0.019753086419753086), r.dim = 3;
+    add_full_symmetric(r, 3, {0.31979362782962991, 0.31979362782962991, 0.31979362782962991},
+                       0.011511367871045398);
+    add_full_symmetric(r, 3, {0.091971078052723033, 0.091971078052723033, 0.091971078052723033},
+                       0.01198951396316977);
+    add_full_symmetric(r, 3, {0.056350832689629156, 0.056350832689629156, 0.44364916731037084},
+                       0.008818342151675485);
   } else if (s.rfind("IM_GAUSS_PARALLELEPIPED(", 0) == 0) {
     int N = 0, K = 0;
     if (sscanf(s.c_str(), "IM_GAUSS_PARALLELEPIPED(%d,%d)", &N, &K) != 2) return false;
@@ -362,6 +400,11 @@ struct Outputs {
   std::vector<Column> K;
   std::vector<double> V;
   double E = 0;
+  // internal variable: order 1 its residual; order 2 (condensation) the
+  // internal solution RQpr and the coupling rows KQJpr (shared arrays,
+  // indexed by element Gauss point, so threads write disjoint parts)
+  bool condense = false;
+  double *Vint = nullptr, *coupling = nullptr;
 };
 
 // ga_exec restated for elements [e0, e1).
@@ -371,6 +414,10 @@ void exec_range(Problem &P, int order, int64_t e0, int64_t e1, Outputs &out) {
   const int s = nb * qd;
   std::vector<double> elem(order == 2 ? size_t(s) * s : size_t(s));
   std::vector<double> G(nbg * dim), g(nb * dim), t(order == 2 ? size_t(s) * s : size_t(s));
+  // condensation: the condensed part of the element matrix (assembled by its
+  // own instruction, with its own threshold) and the condensed vector
+  std::vector<double> elemC(out.condense ? size_t(s) * s : 0), elemR(out.condense ? s : 0);
+  std::vector<double> kiq(s), kqj(s);
   std::vector<int64_t> dofs(s);
   std::vector<size_t> sorted;
   for (int64_t e = e0; e < e1; ++e) {
@@ -378,6 +425,8 @@ void exec_range(Problem &P, int order, int64_t e0, int64_t e1, Outputs &out) {
       for (int d = 0; d < dim; ++d) G[v * dim + d] = p.points[p.cvpts[e * nbg + v] * dim + d];
     const int64_t *edofs = p.dofs + e * nb;
     std::fill(elem.begin(), elem.end(), 0.0);
+    std::fill(elemC.begin(), elemC.end(), 0.0);
+    std::fill(elemR.begin(), elemR.end(), 0.0);
     for (int q = 0; q < nq; ++q) {
       // K(d,m) = sum_v G(d,v) dphi_v/dxi_m ; J = |det K| ; B = K^{-T}
       double Km[9] = {0}, B[9];
@@ -499,6 +548,39 @@ void exec_range(Problem &P, int order, int64_t e0, int64_t e1, Outputs &out) {
             for (int j = 0; j < nb; ++j)
               for (int a = 0; a < qd; ++a) t[0] += c0 * f[a] * phi[j] * p.slots[GFGPU_SLOT_U][edofs[j] + a];
           }
+        } else if (T.kind == GFGPU_TERM_INTERNAL_P) {
+          // u equation (c0 p Id):Grad_Test_u, p equation
+          // scale (p + c2 p^3 + c1 Div_u) Test_p; p at element Gauss point q
+          const double sp = coef_at(p, T.c[0], e, edofs, phi, nb);
+          const double kb = coef_at(p, T.c[1], e, edofs, phi, nb);
+          const double c3 = coef_at(p, T.c[2], e, edofs, phi, nb);
+          const int64_t iq = e * nq + q;
+          const double pv = p.slots[T.field_slot][iq];
+          if (order == 1) {
+            double div = 0;
+            for (int j = 0; j < nb; ++j)
+              for (int b = 0; b < qd; ++b) div += p.slots[GFGPU_SLOT_U][edofs[j] + b] * g[j * dim + b];
+            for (int i = 0; i < nb; ++i)
+              for (int a = 0; a < qd; ++a) t[i * qd + a] += (sp * pv) * g[i * dim + a];
+            // ga_instruction_vector_assembly_imd: V[I + index] += coeff * t
+            out.Vint[iq] += coeff * (sc * ((pv + c3 * (pv * pv * pv)) + kb * div));
+          } else if (order == 2 && out.condense) {
+            for (int i = 0; i < nb; ++i)
+              for (int a = 0; a < qd; ++a) {
+                kiq[i * qd + a] = sp * g[i * dim + a];        // K_IQ: d/dp of the u equation
+                kqj[i * qd + a] = sc * (kb * g[i * dim + a]); // K_QJ: d/du of the p equation
+              }
+            const double kqq = sc * (1.0 + c3 * (3.0 * (pv * pv)));  // K_QQ
+            const double inv = 1.0 / kqq;                              // lu_inverse, 1 x 1
+            const double rq = p.slots[T.aux_slot][iq];                 // cached residual
+            const double rqpr = (0.0 + inv * rq) / coeff;
+            double *crow = out.coupling + size_t(iq) * s;
+            for (int c = 0; c < s; ++c) crow[c] = 0.0 + inv * kqj[c];   // KQJpr
+            out.Vint[iq] = rqpr;
+            for (int j = 0; j < s; ++j)
+              for (int i = 0; i < s; ++i) elemC[size_t(j) * s + i] += coeff * (0.0 - kiq[i] * crow[j]);
+            for (int i = 0; i < s; ++i) elemR[i] += coeff * (0.0 - kiq[i] * rqpr);
+          }
         } else if (T.kind == GFGPU_TERM_NEOHOOKEAN) {
           double C1 = coef_at(p, T.c[0], e, edofs, phi, nb);
           double D1 = coef_at(p, T.c[1], e, edofs, phi, nb);
@@ -569,12 +651,17 @@ void exec_range(Problem &P, int order, int64_t e0, int64_t e1, Outputs &out) {
       }
     }
     if (order == 2) {
-      double ninf = 0;
-      for (double v : elem) ninf = std::max(ninf, std::fabs(v));
-      if (ninf == 0) continue;
       for (int i = 0; i < nb; ++i)
         for (int a = 0; a < qd; ++a) dofs[i * qd + a] = edofs[i] + a;
-      add_elem_matrix(out.K, dofs, dofs, sorted, elem, ninf * 1e-14);
+      double ninf = 0;
+      for (double v : elem) ninf = std::max(ninf, std::fabs(v));
+      if (ninf != 0) add_elem_matrix(out.K, dofs, dofs, sorted, elem, ninf * 1e-14);
+      if (out.condense) {
+        double ninfc = 0;
+        for (double v : elemC) ninfc = std::max(ninfc, std::fabs(v));
+        if (ninfc != 0) add_elem_matrix(out.K, dofs, dofs, sorted, elemC, ninfc * 1e-14);
+        for (int k = 0; k < s; ++k) out.V[dofs[k]] += elemR[k];
+      }
     } else if (order == 1) {
       for (int i = 0; i < nb; ++i)
         for (int a = 0; a < qd; ++a) out.V[edofs[i] + a] += elem[i * qd + a];
@@ -642,7 +729,19 @@ int gfref_tables(int dim, int kind, int degree, const char *im, int *nq, double 
   return 0;
 }
 
+void *gfref_assemble_condensed(const gfref_problem *pp, int nthreads, int64_t *nnz, double *V,
+                               double *Vint, double *coupling);
+
 void *gfref_assemble_matrix(const gfref_problem *pp, int nthreads, int64_t *nnz) {
+  return gfref_assemble_condensed(pp, nthreads, nnz, nullptr, nullptr, nullptr);
+}
+
+// Order 2; with V != nullptr the static condensation of the internal
+// variable: K condensed, V (n_dof) += the condensed primary rows, Vint
+// (n_elements * nq) = RQpr, coupling (n_elements * nq * nb * qdim, element
+// DOFs in local order) = KQJpr.
+void *gfref_assemble_condensed(const gfref_problem *pp, int nthreads, int64_t *nnz, double *V,
+                               double *Vint, double *coupling) {
   Problem *P = prepare(pp);
   if (!P) return nullptr;
   int T = nthreads_of(nthreads);
@@ -656,6 +755,12 @@ void *gfref_assemble_matrix(const gfref_problem *pp, int nthreads, int64_t *nnz)
     tid = omp_get_thread_num();
 #endif
     outs[tid].K.assign(pp->n_dof, Column());
+    if (V) {
+      outs[tid].condense = true;
+      outs[tid].V.assign(pp->n_dof, 0.0);
+      outs[tid].Vint = Vint;
+      outs[tid].coupling = coupling;
+    }
     int64_t e0 = E * tid / T, e1 = E * (tid + 1) / T;
     try {
       exec_range(*P, 2, e0, e1, outs[tid]);
@@ -668,6 +773,9 @@ void *gfref_assemble_matrix(const gfref_problem *pp, int nthreads, int64_t *nnz)
   for (int t = 1; t < T; ++t)
     for (int64_t c = 0; c < pp->n_dof; ++c)
       if (!outs[t].K[c].empty()) add_column(outs[0].K[c], outs[t].K[c]);
+  if (V)
+    for (int t = 0; t < T; ++t)
+      for (int64_t i = 0; i < pp->n_dof; ++i) V[i] += outs[t].V[i];
   delete P;
   if (failed) return nullptr;
   MatrixResult *M = new MatrixResult;
@@ -699,7 +807,18 @@ void gfref_matrix_copy(void *h, int64_t *rowptr, int64_t *colidx, double *vals) 
 
 void gfref_matrix_free(void *h) { delete static_cast<MatrixResult *>(h); }
 
+int gfref_assemble_vector_internal(const gfref_problem *pp, int nthreads, double *V,
+                                   double *Vint);
+
 int gfref_assemble_vector(const gfref_problem *pp, int nthreads, double *V) {
+  return gfref_assemble_vector_internal(pp, nthreads, V, nullptr);
+}
+
+// Order 1; Vint (n_elements * nq) += the residual of an internal variable.
+int gfref_assemble_vector_internal(const gfref_problem *pp, int nthreads, double *V,
+                                   double *Vint) {
+  for (int t = 0; t < pp->form.n_terms; ++t)
+    if (pp->form.terms[t].kind == GFGPU_TERM_INTERNAL_P && !Vint) return 3;
   Problem *P = prepare(pp);
   if (!P) return 2;
   int T = nthreads_of(nthreads);
@@ -713,6 +832,7 @@ int gfref_assemble_vector(const gfref_problem *pp, int nthreads, double *V) {
     tid = omp_get_thread_num();
 #endif
     outs[tid].V.assign(pp->n_dof, 0.0);
+    outs[tid].Vint = Vint;
     int64_t e0 = E * tid / T, e1 = E * (tid + 1) / T;
     try {
       exec_range(*P, 1, e0, e1, outs[tid]);

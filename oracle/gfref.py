@@ -10,6 +10,7 @@ from __future__ import annotations
 import ctypes as C
 import os
 import subprocess
+from math import comb
 
 import numpy as np
 
@@ -31,7 +32,7 @@ class _Coef(C.Structure):
 
 class _Term(C.Structure):
     _fields_ = [("kind", C.c_int32), ("field_slot", C.c_int32), ("scale", C.c_double),
-                ("c", _Coef * 3)]
+                ("c", _Coef * 3), ("aux_slot", C.c_int32), ("reserved", C.c_int32)]
 
 
 class _Form(C.Structure):
@@ -59,6 +60,12 @@ def lib():
         L.gfref_matrix_free.argtypes = [C.c_void_p]
         L.gfref_assemble_vector.argtypes = [C.POINTER(_Problem), C.c_int, C.c_void_p]
         L.gfref_assemble_potential.argtypes = [C.POINTER(_Problem), C.c_int, C.POINTER(C.c_double)]
+        L.gfref_assemble_vector_internal.argtypes = [C.POINTER(_Problem), C.c_int, C.c_void_p,
+                                                     C.c_void_p]
+        L.gfref_assemble_condensed.restype = C.c_void_p
+        L.gfref_assemble_condensed.argtypes = [C.POINTER(_Problem), C.c_int,
+                                               C.POINTER(C.c_int64), C.c_void_p, C.c_void_p,
+                                               C.c_void_p]
         L.gfref_tables.argtypes = [C.c_int, C.c_int, C.c_int, C.c_char_p, C.POINTER(C.c_int),
                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         _lib = L
@@ -91,6 +98,7 @@ class Problem:
         for i, t in enumerate(terms):
             T = P.form.terms[i]
             T.kind, T.scale, T.field_slot = t["kind"], t["scale"], t["field_slot"]
+            T.aux_slot = t.get("aux_slot", 0)
             for k in range(3):
                 c = t["c"][k]
                 if c is not None:
@@ -101,6 +109,8 @@ class Problem:
             P.slots[s] = _p(a).value
         self.P = P
         self.n_dof = n_dof
+        nb = comb(degree + dim, dim) if kind == 0 else (degree + 1) ** dim
+        self.row_len = nb * qdim
 
     def matrix(self, nthreads: int = 1):
         import scipy.sparse as sp
@@ -120,6 +130,42 @@ class Problem:
         if lib().gfref_assemble_vector(C.byref(self.P), nthreads, _p(V)) != 0:
             raise RuntimeError("oracle assembly failed")
         return V
+
+    def _n_internal(self):
+        nq = C.c_int()
+        lib().gfref_tables(self.P.dim, self.P.kind, self.P.degree, self.P.im, C.byref(nq),
+                           None, None, None, None)
+        return self.P.n_elements * nq.value, nq.value
+
+    def vector_internal(self, nthreads: int = 1):
+        """Order 1 of a form with an internal variable: (V, internal residual)."""
+        V = np.zeros(self.n_dof)
+        Vint = np.zeros(self._n_internal()[0])
+        if lib().gfref_assemble_vector_internal(C.byref(self.P), nthreads, _p(V), _p(Vint)) != 0:
+            raise RuntimeError("oracle assembly failed")
+        return V, Vint
+
+    def condensed(self, nthreads: int = 1):
+        """Order 2 with static condensation of the internal variable (its
+        cached residual in the term's aux slot): (K, V, RQpr, KQJpr rows)."""
+        import scipy.sparse as sp
+        n_int, _ = self._n_internal()
+        s = self.row_len
+        V = np.zeros(self.n_dof)
+        Vint = np.zeros(n_int)
+        cpl = np.zeros(n_int * s)
+        nnz = C.c_int64()
+        h = lib().gfref_assemble_condensed(C.byref(self.P), nthreads, C.byref(nnz), _p(V),
+                                           _p(Vint), _p(cpl))
+        if not h:
+            raise RuntimeError("oracle assembly failed")
+        rowptr = np.empty(self.n_dof + 1, dtype=np.int64)
+        colidx = np.empty(nnz.value, dtype=np.int64)
+        vals = np.empty(nnz.value)
+        lib().gfref_matrix_copy(h, _p(rowptr), _p(colidx), _p(vals))
+        lib().gfref_matrix_free(h)
+        K = sp.csr_matrix((vals, colidx, rowptr), shape=(self.n_dof, self.n_dof))
+        return K, V, Vint, cpl.reshape(n_int, s)
 
     def potential(self, nthreads: int = 1):
         E = C.c_double()

@@ -19,10 +19,20 @@
 //                                 S  (scalar field on the same FEM),
 //                                 V  (field on the variable's FEM, qdim Q),
 //                                 C  (fixed-size constant, file length)
+//   internal=NAME expr2=GWFL   (condensation case: the variables live in a
+//       getfem::model, u plus the internal im_data variable NAME, scalar per
+//       Gauss point, values in/NAME.bin; both expressions are added to a
+//       ga_workspace over the model; the driver runs assembly(1, true) and
+//       writes R_full.bin (primary + internal rows), then, with that residual
+//       as the assembled vector, assembly(2, true) and writes the condensed K
+//       (K_*.bin), the vector Rc.bin and the internal coupling matrix
+//       (C_rowptr/C_colidx/C_vals.bin), workspace.cc:791-860)
 // The variable is always "u" (file in/u.bin, zeros when absent).
 // Jitter: when jitter=1, in/jitter.bin holds (nx+1)^dim x dim doubles in
 // lattice order (x index fastest); interior vertices are moved by it.
 #include "getfem/getfem_generic_assembly.h"
+#include "getfem/getfem_models.h"
+#include "getfem/getfem_im_data.h"
 #include "getfem/getfem_regular_meshes.h"
 #include "getfem/getfem_mesh_fem.h"
 #include "getfem/getfem_mesh_im.h"
@@ -68,6 +78,28 @@ static std::vector<std::string> split(const std::string &s, char c) {
   }
   if (!cur.empty()) out.push_back(cur);
   return out;
+}
+
+// column-major sparse matrix -> CSR files (rows sorted, columns ascending)
+template <typename MAT>
+static int64_t write_csr(const std::string &prefix, const MAT &K) {
+  size_type n = gmm::mat_nrows(K);
+  std::vector<int64_t> rowptr(n + 1, 0);
+  for (size_type j = 0; j < gmm::mat_ncols(K); ++j)
+    for (const auto &e : K.col(j)) rowptr[e.c + 1]++;
+  for (size_type i = 0; i < n; ++i) rowptr[i + 1] += rowptr[i];
+  std::vector<int64_t> colidx(rowptr[n]), fill(rowptr.begin(), rowptr.end() - 1);
+  std::vector<double> vals(rowptr[n]);
+  for (size_type j = 0; j < gmm::mat_ncols(K); ++j)
+    for (const auto &e : K.col(j)) {
+      int64_t k = fill[e.c]++;
+      colidx[k] = int64_t(j);
+      vals[k] = e.e;
+    }
+  write_file(prefix + "_rowptr.bin", rowptr);
+  write_file(prefix + "_colidx.bin", colidx);
+  write_file(prefix + "_vals.bin", vals);
+  return rowptr[n];
 }
 
 static double median(std::vector<double> v) {
@@ -182,6 +214,57 @@ int main(int argc, char **argv) {
   std::vector<double> U(ndof, 0.0);
   read_file(in + "/u.bin", U);
   if (U.size() != ndof) { fprintf(stderr, "u.bin has %zu values, need %zu\n", U.size(), size_t(ndof)); return 2; }
+
+  const std::string internal = arg("internal", "");
+  if (!internal.empty()) {
+    getfem::model md;
+    md.add_fem_variable("u", mf);
+    gmm::copy(U, md.set_real_variable("u"));
+    getfem::im_data imd(mim);
+    md.add_internal_im_variable(internal, imd);
+    std::vector<double> Pv;
+    if (!read_file(in + "/" + internal + ".bin", Pv) ||
+        Pv.size() != gmm::vect_size(md.real_variable(internal))) {
+      fprintf(stderr, "%s.bin missing or of wrong size\n", internal.c_str());
+      return 2;
+    }
+    gmm::copy(Pv, md.set_real_variable(internal));
+    for (const std::string &c : split(arg("consts", ""), ',')) {
+      std::vector<std::string> kv = split(c, ':');
+      std::vector<double> v;
+      if (!read_file(in + "/" + kv[0] + ".bin", v)) { fprintf(stderr, "missing %s\n", kv[0].c_str()); return 2; }
+      const std::string &k = kv[1];
+      if (k == "P0") md.add_initialized_fem_data(kv[0], mf0, v);
+      else if (k == "S") md.add_initialized_fem_data(kv[0], mfs, v);
+      else if (k == "V") md.add_initialized_fem_data(kv[0], mf, v);
+      else md.add_initialized_fixed_size_data(kv[0], v);
+    }
+    getfem::ga_workspace wsm(md);
+    wsm.add_expression(expr, mim);
+    const std::string expr2 = arg("expr2", "");
+    if (!expr2.empty()) wsm.add_expression(expr2, mim);
+    const size_type nprim = wsm.nb_primary_dof(), nint = wsm.nb_internal_dof();
+    std::vector<double> R(nprim + nint, 0.0);
+    wsm.set_assembled_vector(R);
+    wsm.assembly(1, true);
+    write_file(out + "/R_full.bin", R);
+    // the condensation reads the current residual from the assembled vector
+    std::vector<double> R1(R);
+    getfem::model_real_sparse_matrix K(nprim, nprim), KQ(nprim + nint, nprim);
+    wsm.set_assembled_vector(R1);
+    wsm.set_assembled_matrix(K);
+    wsm.set_internal_coupling_matrix(KQ);
+    wsm.assembly(2, true);
+    int64_t nnz = write_csr(out + "/K", K);
+    write_file(out + "/Rc.bin", R1);
+    int64_t cnnz = write_csr(out + "/C", KQ);
+    FILE *info = fopen((out + "/info.json").c_str(), "w");
+    fprintf(info, "{\"n_dof\": %zu, \"n_elements\": %zu, \"n_points\": %zu, \"n_internal\": %zu, "
+            "\"nnz\": %lld, \"coupling_nnz\": %lld}\n", size_t(ndof), size_t(E),
+            size_t(m.points().size()), size_t(nint), (long long)nnz, (long long)cnnz);
+    fclose(info);
+    return 0;
+  }
   ws.add_fem_variable("u", mf, gmm::sub_interval(0, ndof), U);
   std::map<std::string, std::vector<double>> cst;
   for (const std::string &c : split(arg("consts", ""), ',')) {

@@ -19,8 +19,15 @@ RTOL = 1e-12
 FLOOR = 1e-3
 
 
-def golden_names():
-    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+def golden_names(condensed=False):
+    """Fixture names: the plain assembly cases, or (condensed=True) the
+    internal-variable condensation cases (they carry R_full / Rc)."""
+    out = []
+    for p in sorted(glob.glob(os.path.join(GOLDEN, "*.npz"))):
+        with np.load(p) as z:
+            if ("Rc" in z.files) == condensed:
+                out.append(os.path.basename(p)[:-4])
+    return out
 
 
 def load(name):
@@ -99,3 +106,40 @@ def vec_errors(a, b):
     scale = np.maximum(np.abs(b), FLOOR * np.max(np.abs(b)))
     scale[scale == 0] = 1.0
     return np.abs(a - b) / scale
+
+
+def build_condensed_case(rec):
+    """Mesh, MeshFem, MeshIm and a GaWorkspace holding u, the internal
+    variable p and both expressions of a condensation fixture."""
+    m = rec["meta"]
+    kind = "simplex" if m["gt"] == "PK" else "hex"
+    mesh = g.Mesh.regular_unit(m["dim"], m["nx"], kind, jitter=rec.get("jitter"))
+    mf = g.MeshFem(mesh, m["qdim"], degree=m["degree"])
+    mim = g.MeshIm(mesh, m["im"])
+    ws = g.GaWorkspace()
+    ws.add_fem_variable("u", mf, U=rec["in_u"])
+    ws.add_internal_im_variable("p", g.ImData(mim), rec["in_p"])
+    for cname, ck in m["consts"].items():
+        v = rec["in_" + cname]
+        if ck == "P0":
+            ws.add_fem_constant(cname, g.MeshFem(mesh, 1, degree=0), v)
+        else:
+            ws.add_fixed_size_constant(cname, v)
+    ws.add_expression(m["expr"], mim)
+    ws.add_expression(m["expr2"], mim)
+    return mesh, mf, mim, ws
+
+
+def csr_errors(A, B):
+    """Errors of A against the reference B on the union of their patterns,
+    scaled by max(|b|, FLOOR * max|row of B|): entries one side stores and
+    the other drops must be below the floor."""
+    import scipy.sparse as sp
+    A = sp.csr_matrix(A)
+    B = sp.csr_matrix(B)
+    D = (A - B).tocoo()
+    rmax = np.asarray(abs(B).max(axis=1).todense()).ravel()
+    b = np.asarray(B[D.row, D.col]).ravel()
+    scale = np.maximum(np.abs(b), FLOOR * rmax[D.row])
+    scale[scale == 0] = 1.0
+    return np.abs(D.data) / scale if D.nnz else np.zeros(1)

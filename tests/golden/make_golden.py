@@ -77,6 +77,18 @@ CASES = [
 CASES.append(("p1tri_poisson_cg", 2, "PK", 1, 1, "IM_TRIANGLE(2)", 64,
               "Grad_u.Grad_Test_u - f*Test_u", {"f": "V"}, False, "zero"))
 EXTRA = {"p1tri_poisson_cg": ["solve=cg", "resmax=1e-12", "maxiter=100000"]}
+# Mixed displacement / pressure forms with the pressure p an internal im_data
+# variable (one value per element Gauss point), condensed at order 2: the
+# formulation of the reference's condensation test (tests/test_condensation.cc,
+# DIFFICULTY 0 and 1) on 3-D meshes.
+UP_A = "(-p*Id(3)+2*G*(Sym(Grad_u)-Div_u*Id(3)/3)):Grad_Test_u"
+# name, dim, gt, degree, qdim, im, nx, u-equation, p-equation, consts, jitter
+CONDENSE_CASES = [
+    ("q2hex_up_condensed", 3, "QK", 2, 3, "IM_GAUSS_PARALLELEPIPED(3,5)", 2,
+     UP_A, "(p+K*Div_u)*Test_p", {"G": "P0", "K": "C"}, True),
+    ("p2tet_up_condensed_nl", 3, "PK", 2, 3, "IM_TETRAHEDRON(5)", 2,
+     UP_A, "((p+1e3*pow(p,3))+K*Div_u)*Test_p", {"G": "C", "K": "P0"}, True),
+]
 ORDERS = {"q2hex_nh_potential": "0,1,2", "p2tet_nh_potential": "0,1,2",
           "q2hex_kappa_potential": "0,1,2", "p2tri_energy_potential": "0,1,2"}
 
@@ -173,6 +185,65 @@ def make_case(case, seed):
     print(name, "ndof", info["n_dof"], "nnz", info["nnz"])
 
 
+def make_condensed_case(case, seed):
+    """The reference's assembly(1, true) and assembly(2, true) over a model
+    holding u and the internal variable p (ref_driver internal=p)."""
+    name, dim, gt, deg, qdim, im, nx, expr_a, expr_b, consts, jitter = case
+    import getfem_gb300 as g
+    rng = np.random.default_rng(seed)
+    kind = "simplex" if gt == "PK" else "hex"
+    h = 1.0 / nx
+    jit = rng.uniform(-0.1 * h, 0.1 * h, ((nx + 1) ** dim, dim)) if jitter else None
+    mesh = g.Mesh.regular_unit(dim, nx, kind, jitter=jit)
+    mf = g.MeshFem(mesh, qdim, degree=deg)
+    ndof, E = mf.nb_dof(), mesh.nb_convex()
+    nq = g.MeshIm(mesh, im).nq
+    inputs = {"u": rng.standard_normal(ndof) * 0.05, "p": rng.standard_normal(E * nq) * 0.05}
+    for cname, ck in consts.items():
+        inputs[cname] = np.exp(rng.normal(0.0, 0.2, E)) if ck == "P0" else np.array([1.5])
+    with tempfile.TemporaryDirectory() as td:
+        ind, outd = os.path.join(td, "in"), os.path.join(td, "out")
+        os.makedirs(ind)
+        os.makedirs(outd)
+        for k, v in inputs.items():
+            np.asarray(v, dtype=np.float64).tofile(os.path.join(ind, k + ".bin"))
+        if jit is not None:
+            jit.astype(np.float64).tofile(os.path.join(ind, "jitter.bin"))
+        cs = ",".join(f"{k}:{v}" for k, v in consts.items())
+        cmd = [DRIVER, f"dim={dim}", f"nx={nx}", f"gt={gt}", f"fem={deg}", f"qdim={qdim}",
+               f"im={im}", f"in={ind}", f"out={outd}", f"expr={expr_a}", f"expr2={expr_b}",
+               "internal=p", f"jitter={1 if jit is not None else 0}", f"consts={cs}"]
+        subprocess.run(cmd, check=True)
+        info = json.load(open(os.path.join(outd, "info.json")))
+
+        def rd(fn, dt=np.float64):
+            return np.fromfile(os.path.join(outd, fn), dtype=dt)
+        rec = dict(
+            points=rd("points.bin").reshape(-1, dim),
+            cvpts=rd("cvpts.bin", np.int64).reshape(E, -1),
+            dofs=rd("dofs.bin", np.int64).reshape(E, -1),
+            R_full=rd("R_full.bin"),
+            K_rowptr=rd("K_rowptr.bin", np.int64),
+            K_colidx=rd("K_colidx.bin", np.int64).astype(np.int32),
+            K_vals=rd("K_vals.bin"),
+            Rc=rd("Rc.bin"),
+            C_rowptr=rd("C_rowptr.bin", np.int64),
+            C_colidx=rd("C_colidx.bin", np.int64).astype(np.int32),
+            C_vals=rd("C_vals.bin"),
+        )
+    for k, v in inputs.items():
+        rec["in_" + k] = np.asarray(v, dtype=np.float64)
+    if jit is not None:
+        rec["jitter"] = jit
+    meta = dict(name=name, dim=dim, gt=gt, degree=deg, qdim=qdim, im=im, nx=nx, expr=expr_a,
+                expr2=expr_b, consts=consts, n_dof=info["n_dof"], nnz=info["nnz"],
+                n_internal=info["n_internal"], seed=seed)
+    assert info["n_internal"] == E * nq
+    rec["meta"] = np.array(json.dumps(meta))
+    np.savez_compressed(os.path.join(OUT, name + ".npz"), **rec)
+    print(name, "ndof", info["n_dof"], "nnz", info["nnz"], "internal", info["n_internal"])
+
+
 def main():
     if not os.path.exists(DRIVER):
         sys.exit(f"{DRIVER} missing: make -C oracle/refbuild REF=/root/reference")
@@ -180,6 +251,9 @@ def main():
     for i, case in enumerate(CASES):
         if not only or case[0] in only:
             make_case(case, 1000 + i)
+    for i, case in enumerate(CONDENSE_CASES):
+        if not only or case[0] in only:
+            make_condensed_case(case, 2000 + i)
 
 
 if __name__ == "__main__":
