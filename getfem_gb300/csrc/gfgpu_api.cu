@@ -201,10 +201,16 @@ int status_from_err(int e) {
     set_last_error("device wait timed out");
     return GFGPU_E_TIMEOUT;
   }
+  if (e & ERR_PATTERN) {
+    set_last_error("element entries outside the cached CSR pattern (entries that were zero "
+                   "when the pattern was built are nonzero now)");
+    return GFGPU_E_STATE;
+  }
   return GFGPU_OK;
 }
 
 int build_pattern(Plan &P) {
+  P.pattern_builds++;
   // counts per row and per node (int64: the scans accumulate in the input
   // type, and the node-level total passes 2^31 on large meshes)
   GF_CUDA(cudaMemsetAsync(P.d_count, 0, (P.n_dof + 1) * sizeof(int64_t), P.stream));
@@ -265,10 +271,23 @@ int build_pattern(Plan &P) {
   return GFGPU_OK;
 }
 
-int check_err(Plan &P) {
+// Waits for the plan's stream and maps its error word to a status.  With
+// repair, an ERR_PATTERN alone (the last gather met element entries the
+// cached pattern lacks) is resolved as the reference would store them: the
+// pattern is rebuilt from the current element matrices (the reference
+// rebuilds K's sparse columns at every assembly) and the gather runs again.
+int check_err(Plan &P, bool repair = false) {
   int herr = 0;
   GF_CUDA(cudaStreamSynchronize(P.stream));
   GF_CUDA(cudaMemcpy(&herr, P.d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (repair && herr == ERR_PATTERN) {
+    GF_CUDA(cudaMemsetAsync(P.d_err, 0, sizeof(int), P.stream));
+    int rc = build_pattern(P);
+    if (rc) return rc;
+    GF_CUDA(launch_gather(P, true, P.last_want_R));
+    GF_CUDA(cudaStreamSynchronize(P.stream));
+    GF_CUDA(cudaMemcpy(&herr, P.d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  }
   return status_from_err(herr);
 }
 
@@ -398,6 +417,16 @@ int gfgpu_plan_create(const gfgpu_space *space, const gfgpu_form *form, void *cu
       for (int64_t k = 0; k < E * nbg; ++k) padj[fill[cv[k]]++] = int32_t(k);
     }
     if (P->ip_term >= 0) P->h_en = en;
+    // host-buffer assembly: for each gather chunk of DOF nodes, one past the
+    // largest element adjacent to it (adjacency codes are sorted by element)
+    P->h_chunk_eend.assign(kHostChunks, 0);
+    for (int c = 0; c < kHostChunks; ++c) {
+      const int64_t n0 = P->n_nodes * c / kHostChunks, n1 = P->n_nodes * (c + 1) / kHostChunks;
+      int64_t eend = c ? P->h_chunk_eend[c - 1] : 0;
+      for (int64_t i = n0; i < n1; ++i)
+        if (aptr[i + 1] > aptr[i]) eend = std::max<int64_t>(eend, adj[aptr[i + 1] - 1] / nb + 1);
+      P->h_chunk_eend[c] = eend;
+    }
     P->max_cand = int32_t(P->max_adj * nb);
     if (P->max_cand > 4096) throw std::runtime_error("node valence too large for the pattern kernel");
     if (P->nb > 128) throw std::runtime_error("more than 128 local nodes per element");
@@ -658,6 +687,7 @@ int gfgpu_assemble(gfgpu_plan *P, int32_t order, int32_t flags, double *potentia
     P->pattern_cmode = P->cmode;
   }
   if (prof) GF_CUDA(cudaEventRecord(P->ev[2], P->stream));
+  P->last_want_R = want_R;
   GF_CUDA(launch_gather(*P, want_K, want_R));
   if (prof) GF_CUDA(cudaEventRecord(P->ev[3], P->stream));
   P->profiled = prof;
@@ -949,7 +979,7 @@ void gfgpu_batch_destroy(gfgpu_batch *B) {
 
 int gfgpu_sync(gfgpu_plan *P) {
   if (!P) return GFGPU_E_INVALID;
-  return check_err(*P);
+  return check_err(*P, true);
 }
 
 int gfgpu_assemble_host(gfgpu_plan *P, const double *u, double *vals, double *vec) {
@@ -979,12 +1009,23 @@ int gfgpu_assemble_host(gfgpu_plan *P, const double *u, double *vals, double *ve
       GF_CUDA(cudaEventCreateWithFlags(&P->chunk_ev[c], cudaEventDisableTiming));
   }
   GF_CUDA(cudaMemsetAsync(P->d_err, 0, sizeof(int), P->stream));
-  if (P->affine_simplex) GF_CUDA(launch_simplex_element_pass(*P, true));
-  else if (P->affine_hex) GF_CUDA(launch_affine_hex_pass(*P, true));
-  else GF_CUDA(launch_hex_element_pass(*P, true));
+  // Affine simplices: the element pass runs in element ranges, each just far
+  // enough for the next gather chunk (h_chunk_eend), so the copies of the
+  // first chunks overlap the element pass of the later ones.
+  int64_t tiles_done = 0;
+  if (P->affine_hex) GF_CUDA(launch_affine_hex_pass(*P, true));
+  else if (!P->affine_simplex) GF_CUDA(launch_hex_element_pass(*P, true));
   const int qd = P->qdim;
   for (int c = 0; c < kHostChunks; ++c) {
     const int64_t n0 = P->n_nodes * c / kHostChunks, n1 = P->n_nodes * (c + 1) / kHostChunks;
+    if (P->affine_simplex) {
+      const int64_t need = c == kHostChunks - 1 ? (P->n_elements + 31) / 32
+                                                : (P->h_chunk_eend[c] + 31) / 32;
+      if (need > tiles_done) {
+        GF_CUDA(launch_simplex_element_pass(*P, true, tiles_done, need));
+        tiles_done = need;
+      }
+    }
     GF_CUDA(launch_gather_range(*P, true, vec != nullptr, n0, n1));
     cudaStream_t cs = P->copy_stream[c & 1];
     GF_CUDA(cudaEventRecord(P->chunk_ev[c], P->stream));
@@ -1000,7 +1041,24 @@ int gfgpu_assemble_host(gfgpu_plan *P, const double *u, double *vals, double *ve
   }
   GF_CUDA(cudaStreamSynchronize(P->copy_stream[0]));
   GF_CUDA(cudaStreamSynchronize(P->copy_stream[1]));
-  return check_err(*P);
+  P->last_want_R = vec != nullptr;
+  const int64_t nnz0 = P->nnz, builds0 = P->pattern_builds;
+  int rc2 = check_err(*P, true);
+  if (rc2 != GFGPU_OK || P->pattern_builds == builds0) return rc2;
+  if (P->nnz != nnz0) {
+    // the pattern grew: the caller's buffer is sized for the old one
+    set_last_error("the CSR pattern grew (entries that were zero at the pattern build are "
+                   "nonzero now): read gfgpu_pattern_size / the new pattern and call again");
+    return GFGPU_E_STATE;
+  }
+  if (vals) {
+    // rebuilt with the same size: copy the repaired values again
+    GF_CUDA(cudaMemcpy(vals, P->d_vals, size_t(P->nnz) * sizeof(double),
+                       cudaMemcpyDeviceToHost));
+    if (vec) GF_CUDA(cudaMemcpy(vec, P->d_vec, size_t(P->n_dof) * sizeof(double),
+                                cudaMemcpyDeviceToHost));
+  }
+  return rc2;
 }
 
 int gfgpu_pattern_size(gfgpu_plan *P, int64_t *n_rows, int64_t *nnz) {
@@ -1106,6 +1164,9 @@ int gfgpu_copy_result(gfgpu_plan *P, int32_t which, void *dst) {
     set_last_error("no pattern yet: assemble order 2 first");
     return GFGPU_E_STATE;
   }
+  // the last assembly must be complete (and its pattern repaired) first
+  int rc = check_err(*P, true);
+  if (rc) return rc;
   const void *src = nullptr;
   size_t bytes = 0;
   switch (which) {

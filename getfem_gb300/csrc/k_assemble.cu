@@ -239,6 +239,9 @@ __device__ __forceinline__ void gather_node(
   }
   cp_async_commit();
   double rvec = 0.0;
+  // an entry above its element's threshold without a slot: the cached
+  // pattern (built from earlier element matrices) misses it
+  bool miss = false;
   for (int k = 0; k < nadj; ++k) {
     int sl1[R];
     double thr1 = 0.0, ve1 = 0.0;
@@ -258,16 +261,18 @@ __device__ __forceinline__ void gather_node(
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         const int c = lane + 32 * r;
-        if (c < S && sl0[r] >= 0) {
+        if (c < S) {
           const int b = c % QD;
-          const unsigned sb = bits[sl0[r]];
+          const unsigned sb = sl0[r] >= 0 ? bits[sl0[r]] : 0u;
           const int c0 = L.blk ? (c / QD) * L.blk + b : c;
           const int cstep = L.blk ? QD : L.rowstride;
 #pragma unroll
           for (int a = 0; a < QD; ++a) {
             const double x = Kb[c0 + a * cstep];
-            if (((sb >> (a * QD + b)) & 1u) && abs_greater(x, tb))
-              acc[(sl0[r] * QD + a) * QD + b] += x;
+            if (abs_greater(x, tb)) {
+              if ((sb >> (a * QD + b)) & 1u) acc[(sl0[r] * QD + a) * QD + b] += x;
+              else miss = true;
+            }
           }
         }
       }
@@ -277,6 +282,7 @@ __device__ __forceinline__ void gather_node(
     for (int r = 0; r < R; ++r) sl0[r] = sl1[r];
     thr0 = thr1, ve0 = ve1;
   }
+  if (__any_sync(0xffffffffu, miss) && lane == 0) set_err(err, ERR_PATTERN);
   if (want_K) {
 #pragma unroll
     for (int a = 0; a < QD; ++a) {

@@ -393,10 +393,11 @@ __global__ void __launch_bounds__(kEpThreads) simplex_element_pass(
     int64_t E, const double *__restrict__ pts, const int32_t *__restrict__ cv,
     const int32_t *__restrict__ enode, const SimplexTables *__restrict__ tab, KeLayout L,
     gfgpu_form form, SlotPtrs slots, const double *__restrict__ fsrc, double fscale,
-    const double *__restrict__ u, double *__restrict__ out, int *__restrict__ err) {
+    const double *__restrict__ u, double *__restrict__ out, int *__restrict__ err,
+    int64_t tile0) {
   __shared__ EpShared<DIM, QD, NB> sh;
-  simplex_element_tile<DIM, QD, NB, MASS, STORE_K>(sh, blockIdx.x, E, pts, cv, enode, tab, L,
-                                                   form, slots, fsrc, fscale, u, out, err);
+  simplex_element_tile<DIM, QD, NB, MASS, STORE_K>(sh, tile0 + blockIdx.x, E, pts, cv, enode,
+                                                   tab, L, form, slots, fsrc, fscale, u, out, err);
 }
 
 }  // namespace
@@ -603,10 +604,13 @@ int build_simplex_tables(Plan &P, std::string &errmsg) {
   return fill_simplex_tables(P.dim, P.degree, P.qdim, P.im, P.stab, P.lay, P.nq, errmsg);
 }
 
-cudaError_t launch_simplex_element_pass(Plan &P, bool with_u) {
+cudaError_t launch_simplex_element_pass(Plan &P, bool with_u, int64_t tile0, int64_t tile1) {
   if (P.n_elements == 0) return cudaSuccess;
   const int threads = kEpThreads;
-  const unsigned blocks = unsigned((P.n_elements + 31) / 32);  // 32 elements per block
+  const int64_t ntiles = (P.n_elements + 31) / 32;  // 32 elements per block
+  if (tile1 < 0 || tile1 > ntiles) tile1 = ntiles;
+  if (tile1 <= tile0) return cudaSuccess;
+  const unsigned blocks = unsigned(tile1 - tile0);
   SlotPtrs sp;
   for (int i = 0; i < GFGPU_MAX_SLOTS; ++i) sp.p[i] = P.slot_ptr[i];
   const double *fsrc = nullptr;
@@ -625,11 +629,11 @@ cudaError_t launch_simplex_element_pass(Plan &P, bool with_u) {
     if (mass)                                                                                  \
       simplex_element_pass<D, Q, N, true, true><<<blocks, threads, 0, P.stream>>>(             \
           P.n_elements, P.d_points, P.d_cv, P.d_enode, P.d_stab, P.lay, P.form, sp, fsrc,      \
-          fscale, with_u ? P.slot_ptr[GFGPU_SLOT_U] : nullptr, P.d_elem, P.d_err);             \
+          fscale, with_u ? P.slot_ptr[GFGPU_SLOT_U] : nullptr, P.d_elem, P.d_err, tile0);      \
     else                                                                                       \
     simplex_element_pass<D, Q, N, false, true><<<blocks, threads, 0, P.stream>>>(              \
         P.n_elements, P.d_points, P.d_cv, P.d_enode, P.d_stab, P.lay, P.form, sp, fsrc, fscale, \
-        with_u ? P.slot_ptr[GFGPU_SLOT_U] : nullptr, P.d_elem, P.d_err);                     \
+        with_u ? P.slot_ptr[GFGPU_SLOT_U] : nullptr, P.d_elem, P.d_err, tile0);              \
   } while (0)
   const int d = P.dim, k = P.degree, q = P.qdim;
   if (d == 2 && k == 1 && q == 1) GFGPU_EP(2, 1, 3);
@@ -678,10 +682,10 @@ cudaError_t launch_simplex_vector_pass(int dim, int degree, int qdim, int64_t E,
   do {                                                                                          \
     if (mass)                                                                                   \
       simplex_element_pass<D, Q, N, true, false><<<blocks, kEpThreads, 0, stream>>>(            \
-          E, pts, cv, enode, tab, L, form, sp, fsrc, fscale, slot[GFGPU_SLOT_U], vout, err);    \
+          E, pts, cv, enode, tab, L, form, sp, fsrc, fscale, slot[GFGPU_SLOT_U], vout, err, 0); \
     else                                                                                        \
       simplex_element_pass<D, Q, N, false, false><<<blocks, kEpThreads, 0, stream>>>(           \
-          E, pts, cv, enode, tab, L, form, sp, fsrc, fscale, slot[GFGPU_SLOT_U], vout, err);    \
+          E, pts, cv, enode, tab, L, form, sp, fsrc, fscale, slot[GFGPU_SLOT_U], vout, err, 0); \
   } while (0)
   const int d = dim, k = degree, q = qdim;
   if (d == 2 && k == 1 && q == 1) GFGPU_VP(2, 1, 3);

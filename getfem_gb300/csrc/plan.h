@@ -15,7 +15,9 @@ enum : int {
   ERR_JACOBIAN = 1,   // det K == 0
   ERR_NAN = 2,        // non-finite value
   ERR_CAPACITY = 4,   // a node touches more DOF nodes than the kernel holds
-  ERR_TIMEOUT = 8
+  ERR_TIMEOUT = 8,
+  ERR_PATTERN = 16    // an element entry above its drop threshold has no slot in
+                      // the cached CSR pattern (the pattern must grow)
 };
 
 // Terms of the sparse barycentric reference tensor of a P_K simplex:
@@ -134,6 +136,8 @@ struct Plan {
   // (n_elements*nq) and the coupling rows (n_elements*nq x nb*qdim)
   int ip_term = -1;
   int cmode = 0;
+  bool last_want_R = false;     // the last gather's vector flag (pattern repair)
+  int64_t pattern_builds = 0;
   int pattern_cmode = -1;
   double *d_int = nullptr, *d_kqj = nullptr;
   std::vector<int32_t> h_en;    // E x nb DOF node ids (coupling columns)
@@ -163,6 +167,9 @@ struct Plan {
   // host-buffer assembly: row pointers on the host, a copy stream and one
   // event per gather chunk (device-to-host copies overlap the gather)
   std::vector<int64_t> h_rowptr;
+  // per gather chunk of DOF nodes: one past the largest element adjacent to
+  // a node of the chunk (the element pass runs ahead of the gather that far)
+  std::vector<int64_t> h_chunk_eend;
   cudaStream_t copy_stream[2] = {nullptr, nullptr};
   cudaEvent_t chunk_ev[kHostChunks] = {};
 };
@@ -205,7 +212,9 @@ cudaError_t launch_batch_gather(const BatchItem *items, const int64_t *node0, in
                                cudaStream_t st);
 
 // kernels (k_simplex.cu)
-cudaError_t launch_simplex_element_pass(Plan &P, bool with_u);
+// tiles [tile0, tile1) of 32 elements (tile1 < 0: to the last element)
+cudaError_t launch_simplex_element_pass(Plan &P, bool with_u, int64_t tile0 = 0,
+                                        int64_t tile1 = -1);
 cudaError_t launch_pattern_count(Plan &P);
 cudaError_t launch_pattern_fill(Plan &P);
 cudaError_t launch_gather(Plan &P, bool want_K, bool want_R);

@@ -207,7 +207,12 @@ int gfgpu_set_data(gfgpu_plan *plan, int32_t slot, const double *values, int64_t
    the device at the first order-2 assembly with the reference's rule: an
    element entry e is inserted only if |e| > 1e-14 * max|elem|
    (compile_and_exec.cc:4889, :5453), the union over elements is kept, and
-   entries that sum to zero stay stored. */
+   entries that sum to zero stay stored.  Later assemblies reuse it; when an
+   element entry above its threshold has no slot in it (an entry that was
+   exactly zero at the build, e.g. a tangent at u = 0), the gather flags it
+   and gfgpu_sync rebuilds the pattern from the current element matrices and
+   gathers again (pointers from gfgpu_device_csr and earlier sizes are then
+   stale).  gfgpu_assemble_host returns GFGPU_E_STATE if its pattern grew. */
 int gfgpu_pattern_size(gfgpu_plan *plan, int64_t *n_rows, int64_t *nnz);
 int gfgpu_pattern_copy(gfgpu_plan *plan, int64_t *rowptr, int32_t *colidx);
 /* Device pointers of the plan's CSR (valid until the plan is destroyed or

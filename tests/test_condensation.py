@@ -170,7 +170,7 @@ def random_pair(kind, nx, degree, im, nonlinear, kb_kind, seed):
                                   ("simplex", 3, 2, "IM_TETRAHEDRON(5)", True, "const"),
                                   ("simplex", 3, 1, "IM_TETRAHEDRON(2)", False, "nodal")])
 def test_gpu_condensation_matches_oracle(case):
-    rng, mesh, mf, mim, ws = random_pair(*case, seed=hash(case) % 1000)
+    rng, mesh, mf, mim, ws = random_pair(*case, seed=sum(map(ord, str(case))) % 1000)
     n, nq = mf.nb_dof(), mim.nq
     grp = ws.groups[0]
     ip = grp.internal_term(ws)
@@ -210,3 +210,44 @@ def test_condensed_linear_pair_is_elasticity():
     Ke = ws2.assembled_matrix()
     assert abs(Kc - Ke).max() <= 1e-12 * abs(Ke).max()
     assert Kc.shape == (n, n)
+
+
+@pytest.mark.gpu
+def test_condensed_newton_converges():
+    """Newton on the nonlinear pair through the condensed system, as the
+    model does with internal variables: K' du = -(R_u + Vc), then
+    dp = -RQpr - KQJpr du per Gauss point.  The full residual (u rows off
+    the clamped face, and every p row) goes to zero quadratically."""
+    import scipy.sparse.linalg as spla
+    rng, mesh, mf, mim, ws = random_pair("simplex", 3, 2, "IM_TETRAHEDRON(5)", True, "const", 3)
+    n = mf.nb_dof()
+    ws.clear_expressions()
+    f = rng.standard_normal(n)
+    ws.add_fem_constant("f", mf, f)
+    ws.add_expression("(-p*Id(3)+2*G*(Sym(Grad_u)-Div_u*Id(3)/3)):Grad_Test_u - f.Test_u", mim)
+    ws.add_expression("((p+1e3*pow(p,3))+K*Div_u)*Test_p", mim)
+    # clamp the DOFs of the nodes on the face x = 0 (DOF 3 k + b: node k, component b)
+    free = ~np.repeat(np.abs(mf.basic_dof_nodes()[:, 0]) < 1e-9, 3)
+    assert free.sum() < n
+    u = np.zeros(n)
+    p = np.zeros(ws.nb_internal_dof())
+    norms = []
+    for it in range(10):
+        ws.set_variable_value("u", u)
+        ws.set_variable_value("p", p)
+        ws.assembly(1, condensation=True)
+        R = ws.assembled_vector().copy()
+        norms.append(max(np.abs(R[:n][free]).max(), np.abs(R[n:]).max()))
+        if norms[-1] <= 1e-13 * norms[0]:
+            break
+        ws.assembly(2, condensation=True)
+        Kc = ws.assembled_matrix().tocsr()
+        Vc = ws.assembled_vector()
+        KQJ = ws.internal_coupling_matrix().tocsr()[n:]
+        du = np.zeros(n)
+        du[free] = spla.spsolve(Kc[free][:, free].tocsc(), -(R[:n] + Vc[:n])[free])
+        u = u + du
+        p = p + (-Vc[n:] - KQJ @ du)
+    assert norms[-1] <= 1e-12 * norms[0], norms
+    # quadratic convergence in the last steps
+    assert len(norms) <= 10 and norms[-2] <= 1e-4 * norms[0], norms

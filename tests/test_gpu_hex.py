@@ -75,6 +75,31 @@ def test_hex_neohookean_jittered(mu_kind):
     check_against_oracle(mesh, mf, mim, ws)
 
 
+def test_pattern_grows_when_new_entries_appear():
+    """At u = 0 the neo-Hookean tangent of an unjittered Q2 mesh has exact
+    zeros (F = I: an isotropic tangent with per-element mu); at u != 0 those
+    entries are nonzero.  The reference rebuilds K's columns at every
+    assembly, so the second assembly must hold them: the gather flags the
+    entries missing from the cached pattern and the sync rebuilds it."""
+    rng, mesh, mf, mim = hex_case(2, 2, 3, "IM_GAUSS_PARALLELEPIPED(3,5)", 8, jitter=False)
+    ws = g.GaWorkspace()
+    ws.add_fem_variable("u", mf, U=np.zeros(mf.nb_dof()))
+    ws.add_fem_constant("mu", g.MeshFem(mesh, 1, degree=0),
+                        np.exp(rng.normal(0, 0.3, mesh.nb_convex())))
+    ws.add_fixed_size_constant("D1", np.array([1.5]))
+    ws.add_expression(NH, mim)
+    ws.assembly(2)
+    nnz0 = ws.assembled_matrix().nnz
+    xyz = mf.basic_dof_nodes()
+    ws.set_variable_value("u", 0.05 * np.sin(xyz @ rng.uniform(-3, 3, (3, 3))).ravel())
+    ws.assembly(2)
+    K = ws.assembled_matrix()
+    Ko = oracle_problem(mesh, mf, mim, ws.groups[0].order2, slots_of(ws)).matrix(nthreads=4)
+    assert Ko.nnz > nnz0
+    assert_same_pattern(K, Ko)
+    assert value_errors(K, Ko).max() <= RTOL
+
+
 def test_hex_neohookean_q1_reduced():
     rng, mesh, mf, mim = hex_case(4, 1, 3, "IM_GAUSS_PARALLELEPIPED(3,3)", 5)
     ws = g.GaWorkspace()
