@@ -119,8 +119,7 @@ __global__ void __launch_bounds__(kAffThreads) affine_hex_kernel(
       for (int p = 1; p < kAffTables; ++p) v = fma(c[p], tabs[p * NN + idx], v);
       o[r * L.rowstride + col] = v;
       if (r != col) o[col * L.rowstride + r] = v;
-      const unsigned long long bits =
-          static_cast<unsigned long long>(__double_as_longlong(v)) & 0x7fffffffffffffffull;
+      const unsigned long long bits = abs_key(v);
       mx = bits > mx ? bits : mx;
     }
     atomicMax(&smax, mx);
@@ -155,7 +154,7 @@ __global__ void __launch_bounds__(kAffThreads) affine_hex_kernel(
   }
   if constexpr (WANT_K) {
     if (tid == 0) {
-      const double m = __longlong_as_double(static_cast<long long>(smax));
+      const double m = abs_of_key(smax);
       if (!isfinite(m)) set_err(err, ERR_NAN);
       o[L.off_thr] = m * 1e-14;
     }

@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(128) pattern_kernel(
   for (int k = a0; k < a1; ++k) {
     const int el = adj[k] / nb, li = adj[k] % nb;
     const double *Ke = elem + int64_t(el) * L.stride;
-    const long long thr = __double_as_longlong(Ke[L.off_thr]);
+    const unsigned long long thr = abs_key(Ke[L.off_thr]);
     for (int j = lane; j < nb; j += kWarp) ljs[j] = bsearch_slot(cand, ns, enode[int64_t(el) * nb + j]);
     __syncwarp();
     for (int c = lane; c < nb * qd; c += kWarp) {
@@ -257,7 +257,7 @@ __device__ __forceinline__ void gather_node(
     rvec += ve0;
     if (want_K) {
       const double *Kb = Kbuf + (k % kGatherBufs) * blk;
-      const long long tb = __double_as_longlong(thr0);
+      const unsigned long long tb = abs_key(thr0);
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         const int c = lane + 32 * r;

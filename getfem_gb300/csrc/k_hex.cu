@@ -453,8 +453,7 @@ __global__ void __launch_bounds__(kHexThreads, 2) hex_element_kernel(
         const int r = rc >> 16, c = rc & 0xffff;
         o[r * L.rowstride + c] = acc[k];
         if (r != c) o[c * L.rowstride + r] = acc[k];
-        const unsigned long long bits =
-            static_cast<unsigned long long>(__double_as_longlong(acc[k])) & 0x7fffffffffffffffull;
+        const unsigned long long bits = abs_key(acc[k]);
         mx = bits > mx ? bits : mx;
       }
     }
@@ -508,7 +507,7 @@ __global__ void __launch_bounds__(kHexThreads, 2) hex_element_kernel(
   if constexpr (WANT_K) {
     __syncthreads();
     if (tid == 0) {
-      const double m = __longlong_as_double(static_cast<long long>(smax));
+      const double m = abs_of_key(smax);
       if (!isfinite(m)) set_err(err, ERR_NAN);
       o[L.off_thr] = m * 1e-14;
     }

@@ -88,7 +88,7 @@ struct EpShared {
     } a;                   // while the blocks of K_e are built
     double Rs[kEpWarps][S][32];  // then: each warp's part of R_e
   } x;
-  long long mxs[kEpWarps][32];
+  unsigned long long mxs[kEpWarps][32];
 };
 
 // One tile (32 elements, 4 warps) of the element pass; every thread of the
@@ -231,7 +231,7 @@ __device__ __forceinline__ void simplex_element_tile(
   __syncthreads();
   const double cm = Gs[NV * DIM + 3][lane], jf = Gs[NV * DIM + 4][lane] * fscale;
   double *o = out + e * L.stride;
-  long long mx = 0;
+  unsigned long long mx = 0ull;  // abs_key of the largest |entry|
   // load term of row r = (i,a): scale |J| sum_j M[i,j] f[(j,a)]
   auto load_of = [&](int i, int a) -> double {
     if (!(fsrc && active)) return 0.0;
@@ -280,8 +280,8 @@ __device__ __forceinline__ void simplex_element_tile(
 #pragma unroll
       for (int c = 0; c < S; ++c) {
         rv += row[c] * Us[c][lane];
-        const long long bitsv = __double_as_longlong(row[c]) & 0x7fffffffffffffffLL;
-        mx = bitsv > mx ? bitsv : mx;
+        const unsigned long long kv = abs_key(row[c]);
+        mx = kv > mx ? kv : mx;
       }
       if (active) {
         if (STORE_K) {
@@ -340,8 +340,8 @@ __device__ __forceinline__ void simplex_element_tile(
           for (int b = 0; b < QD; ++b) {
             Rp[i * QD + a] += B[a][b] * Us[j * QD + b][lane];
             if (i != j) Rp[j * QD + b] += B[a][b] * Us[i * QD + a][lane];
-            const long long bitsv = __double_as_longlong(B[a][b]) & 0x7fffffffffffffffLL;
-            mx = bitsv > mx ? bitsv : mx;
+            const unsigned long long kv = abs_key(B[a][b]);
+            mx = kv > mx ? kv : mx;
           }
         if (STORE_K && active) {
           double4_32a *dij = reinterpret_cast<double4_32a *>(o + (i * NB + j) * BLK);
@@ -375,10 +375,10 @@ __device__ __forceinline__ void simplex_element_tile(
     }
   }
   if (wid == 0 && active) {
-    long long m = mxs[0][lane];
+    unsigned long long m = mxs[0][lane];
 #pragma unroll
     for (int k = 1; k < kEpWarps; ++k) m = mxs[k][lane] > m ? mxs[k][lane] : m;
-    const double mxd = __longlong_as_double(m);
+    const double mxd = abs_of_key(m);
     if (!isfinite(mxd)) set_err(err, ERR_NAN);
     if (STORE_K) o[L.off_thr] = mxd * 1e-14;
 #pragma unroll
