@@ -268,6 +268,18 @@ int build_pattern(Plan &P) {
   P.h_rowptr.resize(size_t(P.n_dof + 1));
   GF_CUDA(cudaMemcpy(P.h_rowptr.data(), P.d_rowptr, size_t(P.n_dof + 1) * sizeof(int64_t),
                      cudaMemcpyDeviceToHost));
+  // pattern slots per valence bucket of the row gather
+  if (!P.h_order.empty()) {
+    std::vector<int64_t> nptr(size_t(P.n_nodes + 1));
+    GF_CUDA(cudaMemcpy(nptr.data(), P.d_nptr, nptr.size() * sizeof(int64_t),
+                       cudaMemcpyDeviceToHost));
+    P.bucket_ms.assign(P.h_bucket.size() - 1, 0);
+    for (size_t b = 0; b + 1 < P.h_bucket.size(); ++b)
+      for (int64_t i = P.h_bucket[b]; i < P.h_bucket[b + 1]; ++i) {
+        const int32_t n = P.h_order[size_t(i)];
+        P.bucket_ms[b] = std::max<int32_t>(P.bucket_ms[b], int32_t(nptr[n + 1] - nptr[n]));
+      }
+  }
   return GFGPU_OK;
 }
 
@@ -417,6 +429,34 @@ int gfgpu_plan_create(const gfgpu_space *space, const gfgpu_form *form, void *cu
       for (int64_t k = 0; k < E * nbg; ++k) padj[fill[cv[k]]++] = int32_t(k);
     }
     if (P->ip_term >= 0) P->h_en = en;
+    // valence buckets of the row gather (ceil(log2(adjacent elements)))
+    {
+      auto bucket_of = [](int32_t v) {
+        int b = 0;
+        while ((int64_t(1) << b) < v) ++b;
+        return b;
+      };
+      std::vector<int64_t> cnt(34, 0);
+      std::vector<int32_t> mad(33, 0);
+      for (int64_t i = 0; i < P->n_nodes; ++i) {
+        const int32_t v = aptr[i + 1] - aptr[i];
+        const int b = bucket_of(v);
+        cnt[b + 1]++;
+        mad[b] = std::max(mad[b], v);
+      }
+      for (int b = 0; b < 33; ++b) cnt[b + 1] += cnt[b];
+      P->h_order.assign(size_t(P->n_nodes), 0);
+      std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
+      for (int64_t i = 0; i < P->n_nodes; ++i)
+        P->h_order[size_t(fill[bucket_of(aptr[i + 1] - aptr[i])]++)] = int32_t(i);
+      P->h_bucket.assign(1, 0);
+      P->bucket_mad.clear();
+      for (int b = 0; b < 33; ++b)
+        if (cnt[b + 1] > cnt[b]) {
+          P->h_bucket.push_back(cnt[b + 1]);
+          P->bucket_mad.push_back(mad[b]);
+        }
+    }
     // host-buffer assembly: for each gather chunk of DOF nodes, one past the
     // largest element adjacent to it (adjacency codes are sorted by element)
     P->h_chunk_eend.assign(kHostChunks, 0);
@@ -467,6 +507,10 @@ int gfgpu_plan_create(const gfgpu_space *space, const gfgpu_form *form, void *cu
     if (!P->h_tri.empty()) {
       CHK(dalloc(&P->d_tri, P->h_tri.size()));
       CHK(up(P->d_tri, P->h_tri.data(), P->h_tri.size() * sizeof(int32_t)));
+    }
+    if (!P->h_order.empty()) {
+      CHK(dalloc(&P->d_order, P->h_order.size()));
+      CHK(up(P->d_order, P->h_order.data(), P->h_order.size() * sizeof(int32_t)));
     }
     CHK(dalloc(&P->d_padj_ptr, pptr.size()));
     CHK(dalloc(&P->d_padj, padj.size()));
@@ -530,6 +574,7 @@ void gfgpu_plan_destroy(gfgpu_plan *P) {
   dfree(P->d_xpart);
   dfree(P->d_int);
   dfree(P->d_kqj);
+  dfree(P->d_order);
   dfree(P->d_elem);
   dfree(P->d_rowptr);
   dfree(P->d_colidx);

@@ -318,19 +318,22 @@ __device__ __forceinline__ void gather_node(
   }
 }
 
+// Warps take the nodes i0, i0 + 1, ... < i1 of `order` (or the nodes i
+// themselves when order is null).
 template <int QD, int R>
 __global__ void __launch_bounds__(128) gather_kernel(
-    int64_t node0, int64_t n_nodes, KeLayout L, const int32_t *__restrict__ adj_ptr,
-    const int32_t *__restrict__ adj, const double *__restrict__ elem, int ms, int mad,
-    const int64_t *__restrict__ nptr, const uint16_t *__restrict__ nbits,
-    const int16_t *__restrict__ slotmap, const int64_t *__restrict__ rowptr,
-    double *__restrict__ vals, bool want_K, bool want_R, double *__restrict__ vec,
-    int *__restrict__ err) {
+    int64_t i0, int64_t i1, const int32_t *__restrict__ order, KeLayout L,
+    const int32_t *__restrict__ adj_ptr, const int32_t *__restrict__ adj,
+    const double *__restrict__ elem, int ms, int mad, const int64_t *__restrict__ nptr,
+    const uint16_t *__restrict__ nbits, const int16_t *__restrict__ slotmap,
+    const int64_t *__restrict__ rowptr, double *__restrict__ vals, bool want_K, bool want_R,
+    double *__restrict__ vec, int *__restrict__ err) {
   extern __shared__ __align__(16) double dsm[];
   const int wib = threadIdx.x >> 5;
   char *base = reinterpret_cast<char *>(dsm) + wib * gather_warp_bytes(ms, QD, L.rowblk, mad);
-  const int64_t node = node0 + blockIdx.x * int64_t(blockDim.x >> 5) + wib;
-  if (node >= n_nodes) return;
+  const int64_t i = i0 + blockIdx.x * int64_t(blockDim.x >> 5) + wib;
+  if (i >= i1) return;
+  const int64_t node = order ? int64_t(order[i]) : i;
   gather_node<QD, R>(base, node, L, adj_ptr, adj, elem, ms, mad, nptr, nbits, slotmap, rowptr,
                      vals, want_K, want_R, vec, err);
 }
@@ -371,30 +374,42 @@ int pattern_cap(const Plan &P) {
 }
 
 template <int QD, int R>
-cudaError_t launch_gather_t(Plan &P, bool want_K, bool want_R, int64_t n0, int64_t n1) {
-  const int ms = P.max_slots < 1 ? 1 : P.max_slots;
-  const int mad = P.max_adj < 1 ? 1 : P.max_adj;
+cudaError_t launch_gather_t(Plan &P, bool want_K, bool want_R, int64_t i0, int64_t i1,
+                            const int32_t *order, int ms, int mad) {
+  ms = ms < 1 ? 1 : ms;
+  mad = mad < 1 ? 1 : mad;
   const size_t smem = size_t(kWarpsPerBlock) * gather_warp_bytes(ms, QD, P.lay.rowblk, mad);
   cudaError_t ce = cudaFuncSetAttribute(gather_kernel<QD, R>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
   if (ce != cudaSuccess) return ce;
-  if (n1 <= n0) return cudaSuccess;
-  const unsigned blocks = unsigned((n1 - n0 + kWarpsPerBlock - 1) / kWarpsPerBlock);
+  if (i1 <= i0) return cudaSuccess;
+  const unsigned blocks = unsigned((i1 - i0 + kWarpsPerBlock - 1) / kWarpsPerBlock);
   gather_kernel<QD, R><<<blocks, kWarpsPerBlock * 32, smem, P.stream>>>(
-      n0, n1, P.lay, P.d_adj_ptr, P.d_adj, P.d_elem, ms, mad, P.d_nptr, P.d_nbits,
+      i0, i1, order, P.lay, P.d_adj_ptr, P.d_adj, P.d_elem, ms, mad, P.d_nptr, P.d_nbits,
       P.d_slotmap, P.d_rowptr, P.d_vals, want_K, want_R, P.d_vec, P.d_err);
   P.launches++;
   return cudaGetLastError();
 }
 
 template <int QD>
-cudaError_t launch_gather_q(Plan &P, bool want_K, bool want_R, int64_t n0, int64_t n1) {
+cudaError_t launch_gather_q(Plan &P, bool want_K, bool want_R, int64_t i0, int64_t i1,
+                            const int32_t *order, int ms, int mad) {
   const int rounds = (P.lay.s + 31) / 32;
   switch (rounds) {
-    case 1: return launch_gather_t<QD, 1>(P, want_K, want_R, n0, n1);
-    case 2: return launch_gather_t<QD, 2>(P, want_K, want_R, n0, n1);
-    case 3: return launch_gather_t<QD, 3>(P, want_K, want_R, n0, n1);
-    case 4: return launch_gather_t<QD, 4>(P, want_K, want_R, n0, n1);
+    case 1: return launch_gather_t<QD, 1>(P, want_K, want_R, i0, i1, order, ms, mad);
+    case 2: return launch_gather_t<QD, 2>(P, want_K, want_R, i0, i1, order, ms, mad);
+    case 3: return launch_gather_t<QD, 3>(P, want_K, want_R, i0, i1, order, ms, mad);
+    case 4: return launch_gather_t<QD, 4>(P, want_K, want_R, i0, i1, order, ms, mad);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_gather_list(Plan &P, bool want_K, bool want_R, int64_t i0, int64_t i1,
+                               const int32_t *order, int ms, int mad) {
+  switch (P.qdim) {
+    case 1: return launch_gather_q<1>(P, want_K, want_R, i0, i1, order, ms, mad);
+    case 2: return launch_gather_q<2>(P, want_K, want_R, i0, i1, order, ms, mad);
+    case 3: return launch_gather_q<3>(P, want_K, want_R, i0, i1, order, ms, mad);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -469,15 +484,22 @@ cudaError_t batch_gather_attr(size_t smem) {
 }
 
 cudaError_t launch_gather_range(Plan &P, bool want_K, bool want_R, int64_t n0, int64_t n1) {
-  switch (P.qdim) {
-    case 1: return launch_gather_q<1>(P, want_K, want_R, n0, n1);
-    case 2: return launch_gather_q<2>(P, want_K, want_R, n0, n1);
-    case 3: return launch_gather_q<3>(P, want_K, want_R, n0, n1);
-    default: return cudaErrorInvalidValue;
-  }
+  return launch_gather_list(P, want_K, want_R, n0, n1, nullptr, P.max_slots, P.max_adj);
 }
 
+// The whole gather: one launch per valence bucket (nodes with similar
+// element counts, so the 4 warps of a block finish together and each launch
+// reserves only its own bucket's shared memory), else one launch over all
+// nodes.
 cudaError_t launch_gather(Plan &P, bool want_K, bool want_R) {
+  if (P.d_order && P.bucket_ms.size() + 1 == P.h_bucket.size()) {
+    for (size_t b = 0; b + 1 < P.h_bucket.size(); ++b) {
+      cudaError_t ce = launch_gather_list(P, want_K, want_R, P.h_bucket[b], P.h_bucket[b + 1],
+                                          P.d_order, P.bucket_ms[b], P.bucket_mad[b]);
+      if (ce != cudaSuccess) return ce;
+    }
+    return cudaSuccess;
+  }
   return launch_gather_range(P, want_K, want_R, 0, P.n_nodes);
 }
 

@@ -170,6 +170,14 @@ struct Plan {
   // per gather chunk of DOF nodes: one past the largest element adjacent to
   // a node of the chunk (the element pass runs ahead of the gather that far)
   std::vector<int64_t> h_chunk_eend;
+  // valence buckets of the row gather: DOF nodes ordered by bucket
+  // (ceil(log2(number of adjacent elements))), node order kept within a
+  // bucket; bucket b is d_order[h_bucket[b] .. h_bucket[b+1]) with at most
+  // bucket_ms[b] pattern slots (set at the pattern build) and bucket_mad[b]
+  // adjacent elements per node
+  int32_t *d_order = nullptr;
+  std::vector<int64_t> h_bucket;
+  std::vector<int32_t> h_order, bucket_ms, bucket_mad;
   cudaStream_t copy_stream[2] = {nullptr, nullptr};
   cudaEvent_t chunk_ev[kHostChunks] = {};
 };
