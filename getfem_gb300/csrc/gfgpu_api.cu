@@ -261,9 +261,10 @@ int build_pattern(Plan &P) {
   P.nnz = nnz;
   P.max_slots = int32_t(mx64);
   GF_CUDA(launch_pattern_fill(P));
-  // the node-level column lists only feed the fill
+  // the node-level column lists feed the fill, and (affine simplices) the
+  // row gather's K u of the fused K + R assembly
   GF_CUDA(cudaStreamSynchronize(P.stream));
-  dfree(P.d_ncol);
+  if (!P.affine_simplex) dfree(P.d_ncol);
   // row pointers on the host (chunked copies of gfgpu_assemble_host)
   P.h_rowptr.resize(size_t(P.n_dof + 1));
   GF_CUDA(cudaMemcpy(P.h_rowptr.data(), P.d_rowptr, size_t(P.n_dof + 1) * sizeof(int64_t),
@@ -719,7 +720,12 @@ int gfgpu_assemble(gfgpu_plan *P, int32_t order, int32_t flags, double *potentia
     for (int i = 0; i < 4; ++i) GF_CUDA(cudaEventCreate(&P->ev[i]));
   GF_CUDA(cudaMemsetAsync(P->d_err, 0, sizeof(int), P->stream));
   if (prof) GF_CUDA(cudaEventRecord(P->ev[0], P->stream));
-  if (P->affine_simplex) GF_CUDA(launch_simplex_element_pass(*P, want_R));
+  // affine simplices with K stored: V_e holds the loads, and the row gather
+  // adds K u from the node's assembled rows (nnz FMAs instead of K_e u_e in
+  // the FP64-bound element pass)
+  P->r_from_rows = P->affine_simplex && want_K;
+  if (P->affine_simplex)
+    GF_CUDA(launch_simplex_element_pass(*P, want_R, 0, -1, !P->r_from_rows));
   // the Gauss kernel skips the tangent and K_e when only the vector is
   // wanted and the pattern (which reads the K_e thresholds) exists
   else if (P->affine_hex) GF_CUDA(launch_affine_hex_pass(*P, want_K || P->nnz < 0));
@@ -1058,6 +1064,7 @@ int gfgpu_assemble_host(gfgpu_plan *P, const double *u, double *vals, double *ve
   // enough for the next gather chunk (h_chunk_eend), so the copies of the
   // first chunks overlap the element pass of the later ones.
   int64_t tiles_done = 0;
+  P->r_from_rows = P->affine_simplex;
   if (P->affine_hex) GF_CUDA(launch_affine_hex_pass(*P, true));
   else if (!P->affine_simplex) GF_CUDA(launch_hex_element_pass(*P, true));
   const int qd = P->qdim;
@@ -1067,7 +1074,7 @@ int gfgpu_assemble_host(gfgpu_plan *P, const double *u, double *vals, double *ve
       const int64_t need = c == kHostChunks - 1 ? (P->n_elements + 31) / 32
                                                 : (P->h_chunk_eend[c] + 31) / 32;
       if (need > tiles_done) {
-        GF_CUDA(launch_simplex_element_pass(*P, true, tiles_done, need));
+        GF_CUDA(launch_simplex_element_pass(*P, true, tiles_done, need, false));
         tiles_done = need;
       }
     }

@@ -181,7 +181,8 @@ __device__ __forceinline__ void gather_node(
     const int64_t *__restrict__ nptr, const uint16_t *__restrict__ nbits,
     const int16_t *__restrict__ slotmap, const int64_t *__restrict__ rowptr,
     double *__restrict__ vals, bool want_K, bool want_R, double *__restrict__ vec,
-    int *__restrict__ err) {
+    int *__restrict__ err, const int32_t *__restrict__ ncol = nullptr,
+    const double *__restrict__ u = nullptr) {
   constexpr int QQ = QD * QD;
   const int lane = threadIdx.x & 31;
   const int nb = L.nb, S = L.s, blk = L.rowblk;
@@ -283,6 +284,31 @@ __device__ __forceinline__ void gather_node(
     thr0 = thr1, ve0 = ve1;
   }
   if (__any_sync(0xffffffffu, miss) && lane == 0) set_err(err, ERR_PATTERN);
+  // ncol given (fused K + R of a linear form): the element vectors held the
+  // loads only; add K u over the node's assembled rows (slot s: column node
+  // ncol[s0 + s]; entries never added are zero), summed in a fixed order
+  double rk = 0.0;
+  if (ncol && want_K && want_R) {
+    double part[QD];
+#pragma unroll
+    for (int a = 0; a < QD; ++a) part[a] = 0.0;
+    for (int j = lane; j < ns; j += kWarp) {
+      const int64_t cn = ncol[s0 + j];
+      double uc[QD];
+#pragma unroll
+      for (int b = 0; b < QD; ++b) uc[b] = u[cn * QD + b];
+#pragma unroll
+      for (int a = 0; a < QD; ++a)
+#pragma unroll
+        for (int b = 0; b < QD; ++b) part[a] = fma(acc[(j * QD + a) * QD + b], uc[b], part[a]);
+    }
+#pragma unroll
+    for (int a = 0; a < QD; ++a) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) part[a] += __shfl_xor_sync(0xffffffffu, part[a], o);
+      if (lane == a) rk = part[a];
+    }
+  }
   if (want_K) {
 #pragma unroll
     for (int a = 0; a < QD; ++a) {
@@ -313,6 +339,7 @@ __device__ __forceinline__ void gather_node(
     }
   }
   if (want_R && lane < QD) {
+    rvec += rk;
     if (!isfinite(rvec)) set_err(err, ERR_NAN);
     vec[node * QD + lane] = rvec;
   }
@@ -327,7 +354,8 @@ __global__ void __launch_bounds__(128) gather_kernel(
     const double *__restrict__ elem, int ms, int mad, const int64_t *__restrict__ nptr,
     const uint16_t *__restrict__ nbits, const int16_t *__restrict__ slotmap,
     const int64_t *__restrict__ rowptr, double *__restrict__ vals, bool want_K, bool want_R,
-    double *__restrict__ vec, int *__restrict__ err) {
+    double *__restrict__ vec, int *__restrict__ err, const int32_t *__restrict__ ncol,
+    const double *__restrict__ u) {
   extern __shared__ __align__(16) double dsm[];
   const int wib = threadIdx.x >> 5;
   char *base = reinterpret_cast<char *>(dsm) + wib * gather_warp_bytes(ms, QD, L.rowblk, mad);
@@ -335,7 +363,7 @@ __global__ void __launch_bounds__(128) gather_kernel(
   if (i >= i1) return;
   const int64_t node = order ? int64_t(order[i]) : i;
   gather_node<QD, R>(base, node, L, adj_ptr, adj, elem, ms, mad, nptr, nbits, slotmap, rowptr,
-                     vals, want_K, want_R, vec, err);
+                     vals, want_K, want_R, vec, err, ncol, u);
 }
 
 // Persistent row gather over the DOF nodes of every mesh of a batch (R = 1:
@@ -386,7 +414,8 @@ cudaError_t launch_gather_t(Plan &P, bool want_K, bool want_R, int64_t i0, int64
   const unsigned blocks = unsigned((i1 - i0 + kWarpsPerBlock - 1) / kWarpsPerBlock);
   gather_kernel<QD, R><<<blocks, kWarpsPerBlock * 32, smem, P.stream>>>(
       i0, i1, order, P.lay, P.d_adj_ptr, P.d_adj, P.d_elem, ms, mad, P.d_nptr, P.d_nbits,
-      P.d_slotmap, P.d_rowptr, P.d_vals, want_K, want_R, P.d_vec, P.d_err);
+      P.d_slotmap, P.d_rowptr, P.d_vals, want_K, want_R, P.d_vec, P.d_err,
+      P.r_from_rows ? P.d_ncol : nullptr, P.slot_ptr[GFGPU_SLOT_U]);
   P.launches++;
   return cudaGetLastError();
 }

@@ -93,7 +93,9 @@ struct EpShared {
 
 // One tile (32 elements, 4 warps) of the element pass; every thread of the
 // block calls it (it synchronises the block).
-template <int DIM, int QD, int NB, bool MASS, bool STORE_K>
+// KU: V_e holds K_e u_e + the load (else the load only: the fused K + R
+// assembly forms K u from the assembled rows in the row gather)
+template <int DIM, int QD, int NB, bool MASS, bool STORE_K, bool KU = true>
 __device__ __forceinline__ void simplex_element_tile(
     EpShared<DIM, QD, NB> &sh, int64_t tile, int64_t E, const double *__restrict__ pts,
     const int32_t *__restrict__ cv, const int32_t *__restrict__ enode,
@@ -222,11 +224,13 @@ __device__ __forceinline__ void simplex_element_tile(
   }
   __syncthreads();
   // ---- u at the element's DOFs
-  for (int j = wid; j < NB; j += kEpWarps) {
-    const int nd = active ? __ldg(enode + e * NB + j) : 0;
+  if (KU) {
+    for (int j = wid; j < NB; j += kEpWarps) {
+      const int nd = active ? __ldg(enode + e * NB + j) : 0;
 #pragma unroll
-    for (int b = 0; b < QD; ++b)
-      Us[j * QD + b][lane] = (active && u) ? __ldg(u + int64_t(nd) * QD + b) : 0.0;
+      for (int b = 0; b < QD; ++b)
+        Us[j * QD + b][lane] = (active && u) ? __ldg(u + int64_t(nd) * QD + b) : 0.0;
+    }
   }
   __syncthreads();
   const double cm = Gs[NV * DIM + 3][lane], jf = Gs[NV * DIM + 4][lane] * fscale;
@@ -279,7 +283,7 @@ __device__ __forceinline__ void simplex_element_tile(
       double rv = load_of(i, 0);
 #pragma unroll
       for (int c = 0; c < S; ++c) {
-        rv += row[c] * Us[c][lane];
+        if (KU) rv += row[c] * Us[c][lane];
         const unsigned long long kv = abs_key(row[c]);
         mx = kv > mx ? kv : mx;
       }
@@ -338,8 +342,10 @@ __device__ __forceinline__ void simplex_element_tile(
         for (int a = 0; a < QD; ++a)
 #pragma unroll
           for (int b = 0; b < QD; ++b) {
-            Rp[i * QD + a] += B[a][b] * Us[j * QD + b][lane];
-            if (i != j) Rp[j * QD + b] += B[a][b] * Us[i * QD + a][lane];
+            if (KU) {
+              Rp[i * QD + a] += B[a][b] * Us[j * QD + b][lane];
+              if (i != j) Rp[j * QD + b] += B[a][b] * Us[i * QD + a][lane];
+            }
             const unsigned long long kv = abs_key(B[a][b]);
             mx = kv > mx ? kv : mx;
           }
@@ -364,13 +370,17 @@ __device__ __forceinline__ void simplex_element_tile(
     }
     mxs[wid][lane] = mx;
     __syncthreads();  // every warp is done with T and u
+    if (KU) {
 #pragma unroll
-    for (int c = 0; c < S; ++c) Rs[wid][c][lane] = Rp[c];
-    __syncthreads();
+      for (int c = 0; c < S; ++c) Rs[wid][c][lane] = Rp[c];
+      __syncthreads();
+    }
     for (int r = wid; r < S; r += kEpWarps) {
       double rv = load_of(r / QD, r % QD);
+      if (KU) {
 #pragma unroll
-      for (int k = 0; k < kEpWarps; ++k) rv += Rs[k][r][lane];
+        for (int k = 0; k < kEpWarps; ++k) rv += Rs[k][r][lane];
+      }
       if (active) o[L.off_vec + r] = rv;
     }
   }
@@ -388,7 +398,7 @@ __device__ __forceinline__ void simplex_element_tile(
 
 namespace {
 
-template <int DIM, int QD, int NB, bool MASS, bool STORE_K>
+template <int DIM, int QD, int NB, bool MASS, bool STORE_K, bool KU>
 __global__ void __launch_bounds__(kEpThreads) simplex_element_pass(
     int64_t E, const double *__restrict__ pts, const int32_t *__restrict__ cv,
     const int32_t *__restrict__ enode, const SimplexTables *__restrict__ tab, KeLayout L,
@@ -396,7 +406,7 @@ __global__ void __launch_bounds__(kEpThreads) simplex_element_pass(
     const double *__restrict__ u, double *__restrict__ out, int *__restrict__ err,
     int64_t tile0) {
   __shared__ EpShared<DIM, QD, NB> sh;
-  simplex_element_tile<DIM, QD, NB, MASS, STORE_K>(sh, tile0 + blockIdx.x, E, pts, cv, enode,
+  simplex_element_tile<DIM, QD, NB, MASS, STORE_K, KU>(sh, tile0 + blockIdx.x, E, pts, cv, enode,
                                                    tab, L, form, slots, fsrc, fscale, u, out, err);
 }
 
@@ -604,7 +614,8 @@ int build_simplex_tables(Plan &P, std::string &errmsg) {
   return fill_simplex_tables(P.dim, P.degree, P.qdim, P.im, P.stab, P.lay, P.nq, errmsg);
 }
 
-cudaError_t launch_simplex_element_pass(Plan &P, bool with_u, int64_t tile0, int64_t tile1) {
+cudaError_t launch_simplex_element_pass(Plan &P, bool with_u, int64_t tile0, int64_t tile1,
+                                        bool ku) {
   if (P.n_elements == 0) return cudaSuccess;
   const int threads = kEpThreads;
   const int64_t ntiles = (P.n_elements + 31) / 32;  // 32 elements per block
@@ -624,16 +635,16 @@ cudaError_t launch_simplex_element_pass(Plan &P, bool with_u, int64_t tile0, int
     }
     if (T.kind == GFGPU_TERM_MASS) mass = true;
   }
+#define GFGPU_EP1(D, Q, N, MS, KUV)                                                            \
+  simplex_element_pass<D, Q, N, MS, true, KUV><<<blocks, threads, 0, P.stream>>>(              \
+      P.n_elements, P.d_points, P.d_cv, P.d_enode, P.d_stab, P.lay, P.form, sp, fsrc, fscale,   \
+      with_u ? P.slot_ptr[GFGPU_SLOT_U] : nullptr, P.d_elem, P.d_err, tile0)
 #define GFGPU_EP(D, Q, N)                                                                      \
   do {                                                                                         \
-    if (mass)                                                                                  \
-      simplex_element_pass<D, Q, N, true, true><<<blocks, threads, 0, P.stream>>>(             \
-          P.n_elements, P.d_points, P.d_cv, P.d_enode, P.d_stab, P.lay, P.form, sp, fsrc,      \
-          fscale, with_u ? P.slot_ptr[GFGPU_SLOT_U] : nullptr, P.d_elem, P.d_err, tile0);      \
-    else                                                                                       \
-    simplex_element_pass<D, Q, N, false, true><<<blocks, threads, 0, P.stream>>>(              \
-        P.n_elements, P.d_points, P.d_cv, P.d_enode, P.d_stab, P.lay, P.form, sp, fsrc, fscale, \
-        with_u ? P.slot_ptr[GFGPU_SLOT_U] : nullptr, P.d_elem, P.d_err, tile0);              \
+    if (mass && ku) GFGPU_EP1(D, Q, N, true, true);                                            \
+    else if (mass) GFGPU_EP1(D, Q, N, true, false);                                            \
+    else if (ku) GFGPU_EP1(D, Q, N, false, true);                                              \
+    else GFGPU_EP1(D, Q, N, false, false);                                                     \
   } while (0)
   const int d = P.dim, k = P.degree, q = P.qdim;
   if (d == 2 && k == 1 && q == 1) GFGPU_EP(2, 1, 3);
@@ -646,6 +657,7 @@ cudaError_t launch_simplex_element_pass(Plan &P, bool with_u, int64_t tile0, int
   else if (d == 3 && k == 2 && q == 3) GFGPU_EP(3, 3, 10);
   else return cudaErrorInvalidValue;
 #undef GFGPU_EP
+#undef GFGPU_EP1
   P.launches++;
   return cudaGetLastError();
 }
@@ -681,10 +693,10 @@ cudaError_t launch_simplex_vector_pass(int dim, int degree, int qdim, int64_t E,
 #define GFGPU_VP(D, Q, N)                                                                       \
   do {                                                                                          \
     if (mass)                                                                                   \
-      simplex_element_pass<D, Q, N, true, false><<<blocks, kEpThreads, 0, stream>>>(            \
+      simplex_element_pass<D, Q, N, true, false, true><<<blocks, kEpThreads, 0, stream>>>(      \
           E, pts, cv, enode, tab, L, form, sp, fsrc, fscale, slot[GFGPU_SLOT_U], vout, err, 0); \
     else                                                                                        \
-      simplex_element_pass<D, Q, N, false, false><<<blocks, kEpThreads, 0, stream>>>(           \
+      simplex_element_pass<D, Q, N, false, false, true><<<blocks, kEpThreads, 0, stream>>>(     \
           E, pts, cv, enode, tab, L, form, sp, fsrc, fscale, slot[GFGPU_SLOT_U], vout, err, 0); \
   } while (0)
   const int d = dim, k = degree, q = qdim;

@@ -137,6 +137,9 @@ struct Plan {
   int ip_term = -1;
   int cmode = 0;
   bool last_want_R = false;     // the last gather's vector flag (pattern repair)
+  // the fused K + R assembly of an affine-simplex plan: V_e holds the load
+  // only and the row gather adds K u from the assembled rows (d_ncol kept)
+  bool r_from_rows = false;
   int64_t pattern_builds = 0;
   int pattern_cmode = -1;
   double *d_int = nullptr, *d_kqj = nullptr;
@@ -220,9 +223,10 @@ cudaError_t launch_batch_gather(const BatchItem *items, const int64_t *node0, in
                                cudaStream_t st);
 
 // kernels (k_simplex.cu)
-// tiles [tile0, tile1) of 32 elements (tile1 < 0: to the last element)
+// tiles [tile0, tile1) of 32 elements (tile1 < 0: to the last element);
+// ku: V_e includes K_e u_e (false: the load only, K u formed by the gather)
 cudaError_t launch_simplex_element_pass(Plan &P, bool with_u, int64_t tile0 = 0,
-                                        int64_t tile1 = -1);
+                                        int64_t tile1 = -1, bool ku = true);
 cudaError_t launch_pattern_count(Plan &P);
 cudaError_t launch_pattern_fill(Plan &P);
 cudaError_t launch_gather(Plan &P, bool want_K, bool want_R);
