@@ -450,13 +450,21 @@ int gfgpu_plan_create(const gfgpu_space *space, const gfgpu_form *form, void *cu
       std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
       for (int64_t i = 0; i < P->n_nodes; ++i)
         P->h_order[size_t(fill[bucket_of(aptr[i + 1] - aptr[i])]++)] = int32_t(i);
+      // buckets of fewer nodes than one wave of blocks join the next one (a
+      // launch of a few blocks is mostly tail)
+      const int64_t small = 152 * 8 * 4;
       P->h_bucket.assign(1, 0);
       P->bucket_mad.clear();
-      for (int b = 0; b < 33; ++b)
-        if (cnt[b + 1] > cnt[b]) {
-          P->h_bucket.push_back(cnt[b + 1]);
-          P->bucket_mad.push_back(mad[b]);
-        }
+      int32_t carry = 0;
+      for (int b = 0; b < 33; ++b) {
+        if (cnt[b + 1] == cnt[b]) continue;
+        carry = std::max(carry, mad[b]);
+        const bool last = cnt[b + 1] == cnt[33];
+        if (cnt[b + 1] - P->h_bucket.back() < small && !last) continue;
+        P->h_bucket.push_back(cnt[b + 1]);
+        P->bucket_mad.push_back(carry);
+        carry = 0;
+      }
     }
     // host-buffer assembly: for each gather chunk of DOF nodes, one past the
     // largest element adjacent to it (adjacency codes are sorted by element)

@@ -407,9 +407,18 @@ cudaError_t launch_gather_t(Plan &P, bool want_K, bool want_R, int64_t i0, int64
   ms = ms < 1 ? 1 : ms;
   mad = mad < 1 ? 1 : mad;
   const size_t smem = size_t(kWarpsPerBlock) * gather_warp_bytes(ms, QD, P.lay.rowblk, mad);
-  cudaError_t ce = cudaFuncSetAttribute(gather_kernel<QD, R>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  // the dynamic shared-memory limit of this instantiation, raised only when
+  // a launch needs more (per device; a host call between launches otherwise)
+  static int limit[16] = {};
+  int dev = 0;
+  cudaError_t ce = cudaGetDevice(&dev);
   if (ce != cudaSuccess) return ce;
+  if (dev < 0 || dev >= 16 || int(smem) > limit[dev]) {
+    ce = cudaFuncSetAttribute(gather_kernel<QD, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              int(smem));
+    if (ce != cudaSuccess) return ce;
+    if (dev >= 0 && dev < 16) limit[dev] = int(smem);
+  }
   if (i1 <= i0) return cudaSuccess;
   const unsigned blocks = unsigned((i1 - i0 + kWarpsPerBlock - 1) / kWarpsPerBlock);
   gather_kernel<QD, R><<<blocks, kWarpsPerBlock * 32, smem, P.stream>>>(
