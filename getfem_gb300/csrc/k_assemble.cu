@@ -162,6 +162,36 @@ __global__ void __launch_bounds__(128) pattern_kernel(
 
 // -------------------------------------------------------------- gather
 
+// Sums v[0..Q) over the 32 lanes; lane a < Q returns the total of v[a].
+// Recursive halving: the first levels exchange half of the components, so
+// Q = 3 (padded to 4) takes 6 FP64 adds per lane instead of 15 (a butterfly
+// per component).  Fixed order: deterministic.
+template <int Q>
+__device__ __forceinline__ double warp_sum_components(const double (&v)[Q], int lane) {
+  if constexpr (Q == 1) {
+    double x = v[0];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    return x;
+  } else {
+    // 4 slots: after level 16 a lane keeps the pair {2h, 2h + 1}, after
+    // level 8 the component c = 2h + h2, summed over its 8-lane group
+    const double w0 = v[0], w1 = Q > 1 ? v[1] : 0.0, w2 = Q > 2 ? v[2] : 0.0,
+                 w3 = Q > 3 ? v[3] : 0.0;
+    const bool h = (lane >> 4) & 1, h2 = (lane >> 3) & 1;
+    double k0 = h ? w2 : w0, k1 = h ? w3 : w1;
+    const double s0 = h ? w0 : w2, s1 = h ? w1 : w3;
+    k0 += __shfl_xor_sync(0xffffffffu, s0, 16);
+    k1 += __shfl_xor_sync(0xffffffffu, s1, 16);
+    double x = h2 ? k1 : k0;
+    x += __shfl_xor_sync(0xffffffffu, h2 ? k0 : k1, 8);
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    // component a sits in lanes 8a .. 8a + 7
+    return __shfl_sync(0xffffffffu, x, (lane & 3) * 8);
+  }
+}
+
 constexpr int kGatherBufs = 2;  // row blocks per warp: the current one and the next
 
 __host__ __device__ __forceinline__ size_t gather_warp_bytes(int ms, int qd, int rowblk,
@@ -302,12 +332,7 @@ __device__ __forceinline__ void gather_node(
 #pragma unroll
         for (int b = 0; b < QD; ++b) part[a] = fma(acc[(j * QD + a) * QD + b], uc[b], part[a]);
     }
-#pragma unroll
-    for (int a = 0; a < QD; ++a) {
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) part[a] += __shfl_xor_sync(0xffffffffu, part[a], o);
-      if (lane == a) rk = part[a];
-    }
+    rk = warp_sum_components<QD>(part, lane);
   }
   if (want_K) {
 #pragma unroll
