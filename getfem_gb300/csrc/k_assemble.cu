@@ -196,8 +196,10 @@ constexpr int kGatherBufs = 2;  // row blocks per warp: the current one and the 
 
 __host__ __device__ __forceinline__ size_t gather_warp_bytes(int ms, int qd, int rowblk,
                                                              int mad) {
+  // row blocks, slot accumulators, element-vector staging (mad * qd),
+  // adjacency split, keep bits
   const size_t b = size_t(kGatherBufs * rowblk) * 8 + size_t(ms) * qd * qd * 8 +
-                   size_t(mad) * 8 + size_t(ms) * 2;
+                   size_t(mad) * qd * 8 + size_t(mad) * 8 + size_t(ms) * 2;
   return (b + 15) / 16 * 16;
 }
 
@@ -218,7 +220,8 @@ __device__ __forceinline__ void gather_node(
   const int nb = L.nb, S = L.s, blk = L.rowblk;
   double *Kbuf = reinterpret_cast<double *>(base);                // kGatherBufs x blk
   double *acc = Kbuf + kGatherBufs * blk;                          // ms * QQ
-  int *adjs = reinterpret_cast<int *>(acc + size_t(ms) * QQ);     // mad
+  double *vbuf = acc + size_t(ms) * QQ;                            // mad * QD
+  int *adjs = reinterpret_cast<int *>(vbuf + size_t(mad) * QD);   // mad
   int *adjl = adjs + mad;                                          // mad
   uint16_t *bits = reinterpret_cast<uint16_t *>(adjl + mad);      // ms
   const int64_t s0 = nptr[node];
@@ -285,7 +288,12 @@ __device__ __forceinline__ void gather_node(
     cp_async_commit();
     cp_async_wait1();  // the group of element k is complete
     __syncwarp();
-    rvec += ve0;
+    // fused K + R: the element vectors are staged and summed with K u below
+    if (ncol && want_K) {
+      if (lane < QD) vbuf[k * QD + lane] = ve0;
+    } else {
+      rvec += ve0;
+    }
     if (want_K) {
       const double *Kb = Kbuf + (k % kGatherBufs) * blk;
       const unsigned long long tb = abs_key(thr0);
@@ -322,6 +330,18 @@ __device__ __forceinline__ void gather_node(
     double part[QD];
 #pragma unroll
     for (int a = 0; a < QD; ++a) part[a] = 0.0;
+    {
+      // staged element vectors: lanes < (32/QD)*QD step over them keeping
+      // the component lane % QD (one add per 32 entries)
+      constexpr int kStep = (kWarp / QD) * QD;
+      const int ca = lane % QD;
+      double pl = 0.0;
+      if (lane < kStep)
+        for (int t = lane; t < nadj * QD; t += kStep) pl += vbuf[t];
+#pragma unroll
+      for (int a = 0; a < QD; ++a)
+        if (a == ca) part[a] = pl;
+    }
     for (int j = lane; j < ns; j += kWarp) {
       const int64_t cn = ncol[s0 + j];
       double uc[QD];
