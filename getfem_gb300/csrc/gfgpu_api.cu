@@ -894,6 +894,9 @@ int gfgpu_batch_create(gfgpu_plan *const *plans, int32_t n, gfgpu_batch **out) {
     it.rowptr = P.d_rowptr;
     it.vals = P.d_vals;
     it.vec = P.d_vec;
+    it.ncol = P.d_ncol;
+    if (!it.ncol)
+      return fail(GFGPU_E_STATE, "gfgpu_batch_create: the plan's node column lists are missing");
     if (it.etype < 0 || P.lay.s > 32)
       return fail(GFGPU_E_UNSUPPORTED, "gfgpu_batch_create: element not batched");
     eitems[it.etype].push_back(it);

@@ -433,7 +433,7 @@ __global__ void __launch_bounds__(128) batch_gather_kernel(
     __syncwarp();
     gather_node<QD, 1>(base, g - node0[lo], it.L, it.adj_ptr, it.adj, it.elem, it.ms, it.mad,
                        it.nptr, it.nbits, it.slotmap, it.rowptr, it.vals, true, true, it.vec,
-                       it.err);
+                       it.err, it.ncol, it.u);
   }
 }
 

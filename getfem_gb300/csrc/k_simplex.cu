@@ -563,7 +563,8 @@ __global__ void __launch_bounds__(kEpThreads) batch_element_pass(
     }
     const BatchItem &it = items[lo];
     __syncthreads();  // the previous tile is done with the shared memory
-    simplex_element_tile<B::DIM, B::QD, B::NB, B::MASS, true>(
+    // K u is formed by the batched gather from the assembled rows
+    simplex_element_tile<B::DIM, B::QD, B::NB, B::MASS, true, false>(
         sh, t - tile0[lo], it.E, it.pts, it.cv, it.enode, it.tab, it.L, it.form, it.slots,
         it.fsrc, it.fscale, it.u, it.elem, it.err);
   }

@@ -209,6 +209,9 @@ struct BatchItem {
   const int16_t *slotmap = nullptr;
   const int64_t *rowptr = nullptr;
   double *vals = nullptr, *vec = nullptr;
+  // node-level column lists: the gather forms K u from the assembled rows
+  // (the element pass leaves it out)
+  const int32_t *ncol = nullptr;
 };
 
 // batched launches (k_simplex.cu, k_assemble.cu)
