@@ -24,7 +24,12 @@
 //    results are bit-reproducible.  The vector is R = sum V_e, where each
 //    element kernel has put its whole contribution (K_e u_e + load for a
 //    linear form, with no threshold as in the reference's vector assembly,
-//    or the element residual of a nonlinear form) into V_e.
+//    or the element residual of a nonlinear form) into V_e; in the fused
+//    K + R assembly of affine simplices V_e holds the load only and the warp
+//    adds K u over the node's assembled rows.  The nodes are launched in
+//    buckets of similar valence (number of adjacent elements), each launch
+//    with its own shared-memory footprint.
+#include <atomic>
 #include <cub/cub.cuh>
 
 #include "k_common.cuh"
@@ -454,15 +459,19 @@ cudaError_t launch_gather_t(Plan &P, bool want_K, bool want_R, int64_t i0, int64
   const size_t smem = size_t(kWarpsPerBlock) * gather_warp_bytes(ms, QD, P.lay.rowblk, mad);
   // the dynamic shared-memory limit of this instantiation, raised only when
   // a launch needs more (per device; a host call between launches otherwise)
-  static int limit[16] = {};
+  static std::atomic<int> limit[16];
   int dev = 0;
   cudaError_t ce = cudaGetDevice(&dev);
   if (ce != cudaSuccess) return ce;
-  if (dev < 0 || dev >= 16 || int(smem) > limit[dev]) {
+  if (dev < 0 || dev >= 16 || int(smem) > limit[dev].load()) {
     ce = cudaFuncSetAttribute(gather_kernel<QD, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               int(smem));
     if (ce != cudaSuccess) return ce;
-    if (dev >= 0 && dev < 16) limit[dev] = int(smem);
+    if (dev >= 0 && dev < 16) {
+      int cur = limit[dev].load();
+      while (int(smem) > cur && !limit[dev].compare_exchange_weak(cur, int(smem))) {
+      }
+    }
   }
   if (i1 <= i0) return cudaSuccess;
   const unsigned blocks = unsigned((i1 - i0 + kWarpsPerBlock - 1) / kWarpsPerBlock);
