@@ -413,19 +413,43 @@ def bench_q4(steps, nx=64):
     def apply():
         L.check(lib.gfgpu_assemble(h1, 1, 0, None))
 
+    def apply_sf():
+        # opt-in: exact tensor-product basis, 1D contractions
+        L.check(lib.gfgpu_assemble(h1, 1, L.SUM_FACTORISATION, None))
+
     def adj():
         L.check(lib.gfgpu_potential_gradient(h0, slot, C.c_void_p(gk.data_ptr()), E, 1))
-    for f in (kr, apply, adj):
+    for f in (kr, apply, apply_sf, adj):
         f()
     t_kr = _events_ms(kr, steps)
     t_ap = _events_ms(apply, steps)
     t_adj = _events_ms(adj, steps)
+    t_sf = _events_ms(apply_sf, steps)
+    # deviation of the sum-factorised apply from the reference-exact one
+    dvec = C.c_void_p()
+    L.check(lib.gfgpu_device_vector(h1, C.byref(dvec)))
+    n = mf.nb_dof()
+
+    def vec_now():
+        L.check(lib.gfgpu_sync(h1))
+        v = torch.empty(n, dtype=torch.float64, device="cuda")
+        L.check(lib.gfgpu_copy_result(h1, L.RESULT_VECTOR, C.c_void_p(v.data_ptr())))
+        return v
+    apply()
+    r_ref = vec_now()
+    apply_sf()
+    r_sf = vec_now()
+    scale = torch.maximum(r_ref.abs(), 1e-3 * r_ref.abs().max())
+    sf_dev = float(((r_sf - r_ref).abs() / scale).max())
     out = {"workload": f"Q4 hex {nx}^3 kappa*Grad_u.Grad_Test_u, IM_GAUSS_PARALLELEPIPED(3,9): "
                        "K + R assembled, matrix-free R = K u, d(u^T K u)/dkappa",
            "elements": E, "n_dof": mf.nb_dof(), "nnz": nnz.value, "setup_s": setup_s,
            "ms_K_R": t_kr, "ms_matrix_free_apply": t_ap, "ms_adjoint_kappa": t_adj,
+           "ms_matrix_free_apply_sum_factorised": t_sf,
+           "sum_factorised_max_rel_deviation": sf_dev,
            "elements_per_s_K_R": E / (t_kr * 1e-3),
            "elements_per_s_apply": E / (t_ap * 1e-3),
+           "elements_per_s_apply_sum_factorised": E / (t_sf * 1e-3),
            "elements_per_s_K_R_adjoint": E / ((t_kr + t_adj) * 1e-3)}
     del ws
     gc.collect()

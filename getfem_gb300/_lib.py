@@ -23,6 +23,7 @@ REBUILD_PATTERN = 1
 WITH_VECTOR = 2
 PROFILE = 4
 CONDENSATION = 8
+SUM_FACTORISATION = 16
 SLOT_POINTS = -1
 RESULT_ROWPTR, RESULT_COLIDX, RESULT_VALUES, RESULT_VECTOR = 0, 1, 2, 3
 RESULT_INTERNAL, RESULT_COUPLING, RESULT_COUPLING_COLIDX = 4, 5, 6

@@ -383,6 +383,7 @@ int gfgpu_plan_create(const gfgpu_space *space, const gfgpu_form *form, void *cu
         P->affine_hex = true;
         P->kmat = true;
         build_affine_hex_tables(*P);
+        build_affine_hex_sumfac(*P);
       } else {
         P->kmat = S.dim == 3 && gauss_element_available(S.kind, P->law, S.degree, S.qdim, P->nq);
         gauss_element_layout(*P);
@@ -513,6 +514,10 @@ int gfgpu_plan_create(const gfgpu_space *space, const gfgpu_form *form, void *cu
       CHK(dalloc(&P->d_aff, P->h_aff.size()));
       CHK(up(P->d_aff, P->h_aff.data(), P->h_aff.size() * sizeof(double)));
     }
+    if (!P->h_sf.empty()) {
+      CHK(dalloc(&P->d_sf, P->h_sf.size()));
+      CHK(up(P->d_sf, P->h_sf.data(), P->h_sf.size() * sizeof(double)));
+    }
     if (!P->h_tri.empty()) {
       CHK(dalloc(&P->d_tri, P->h_tri.size()));
       CHK(up(P->d_tri, P->h_tri.data(), P->h_tri.size() * sizeof(int32_t)));
@@ -576,6 +581,7 @@ void gfgpu_plan_destroy(gfgpu_plan *P) {
   dfree(P->d_hgradT);
   dfree(P->d_tri);
   dfree(P->d_aff);
+  dfree(P->d_sf);
   dfree(P->d_padj_ptr);
   dfree(P->d_padj);
   dfree(P->d_epart);
@@ -709,6 +715,7 @@ int gfgpu_assemble(gfgpu_plan *P, int32_t order, int32_t flags, double *potentia
     return GFGPU_E_UNSUPPORTED;
   }
   P->cmode = P->ip_term < 0 ? 0 : (condense ? 2 : 1);
+  P->sf_requested = (flags & GFGPU_SUM_FACTORISATION) != 0;
   const bool want_K = order == 2;
   // with condensation the vector is the condensed right-hand side
   const bool want_R = order == 1 || (flags & 2) || condense;

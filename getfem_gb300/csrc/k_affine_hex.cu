@@ -18,8 +18,19 @@
 // One CTA per element.  K_e is symmetric: each thread owns upper-triangle
 // entries (tables read coalesced from L2) and writes both (r,c) and (c,r).
 // V_e = K_e u_e + load is then formed by one warp per row from the rows just
-// written (or, for a vector-only pass, from the tables directly).
+// written.
+//
+// The vector-only pass (matrix-free R = K u + load) is sum-factorised: the
+// FEM_QK(3,K) basis is the tensor product of the FEM_PK(1,K) basis
+// (tproduct_femi, getfem_fem.cc:792-826) and IM_GAUSS_PARALLELEPIPED the
+// tensor product of IM_GAUSS1D, so the reference's per-point sums
+//   V_e[i] = sum_q w_q |J| (grad phi_i . c1 B^T B grad u(q) + phi_i h(q)),
+//   h = c_m u + c_f f,
+// are done as 1D contractions, direction by direction: about 11 k FMAs per
+// Q4 element instead of the 110 k of forming each K_e entry from 7 tables.
 #include <cmath>
+#include <cstdio>
+#include <cstring>
 
 #include "host/refelem.h"
 #include "k_common.cuh"
@@ -161,6 +172,187 @@ __global__ void __launch_bounds__(kAffThreads) affine_hex_kernel(
   }
 }
 
+// 1D tables of the sum factorisation: values and derivatives of the 1D
+// basis at the 1D Gauss points (N[q][a], D[q][a]), the 1D weights, and the
+// tensor index a + P1 (b + P1 c) of each local DOF
+template <int P1, int Q1>
+struct SumFac {
+  double N[Q1][P1], D[Q1][P1], w[Q1];
+  int perm[P1 * P1 * P1];
+};
+
+constexpr int kSfThreads = 128;
+
+template <int P1, int Q1, bool HASV>
+__global__ void __launch_bounds__(kSfThreads) affine_hex_apply_kernel(
+    int64_t E, const double *__restrict__ pts, const int32_t *__restrict__ cv,
+    const int32_t *__restrict__ enode, const SumFac<P1, Q1> *__restrict__ sf,
+    const double *__restrict__ ggrad0, KeLayout L, gfgpu_form form, SlotPtrs slots,
+    double *__restrict__ out, int *__restrict__ err) {
+  constexpr int NB = P1 * P1 * P1;
+  constexpr int M3 = (P1 > Q1 ? P1 : Q1) * (P1 > Q1 ? P1 : Q1) * (P1 > Q1 ? P1 : Q1);
+  __shared__ double sN[Q1][P1], sD[Q1][P1], sw[Q1];
+  __shared__ double cM[6], cJ;            // c1 |J| B^T B (upper), |J|
+  __shared__ double U[M3], Hd[M3];        // u and h = c_m u + c_f f (tensor order)
+  __shared__ double A0[M3], A1[M3], A2[M3], A3[M3];
+  __shared__ double B0[M3], B1[M3], B2[M3], B3[M3];
+  const int64_t e = blockIdx.x;
+  const int tid = threadIdx.x;
+  if (e >= E) return;
+  for (int t = tid; t < Q1 * P1; t += kSfThreads) {
+    sN[t / P1][t % P1] = sf->N[t / P1][t % P1];
+    sD[t / P1][t % P1] = sf->D[t / P1][t % P1];
+  }
+  if (tid < Q1) sw[tid] = sf->w[tid];
+  const double *u = slots.p[GFGPU_SLOT_U];
+  int src_slot = -1;
+  double cm = 0.0, csrc = 0.0, c1 = 0.0;
+  for (int t = 0; t < form.n_terms; ++t) {
+    const gfgpu_term &T = form.terms[t];
+    auto val = [&](const gfgpu_coef &c) {
+      if (c.kind == GFGPU_COEF_CONST) return c.value;
+      if (c.kind == GFGPU_COEF_ELEMENT) return c.value * slots.p[c.slot][e];
+      return 0.0;
+    };
+    if (T.kind == GFGPU_TERM_GRADGRAD) c1 += T.scale * val(T.c[1]);
+    else if (T.kind == GFGPU_TERM_MASS) cm += T.scale * val(T.c[0]);
+    else if (T.kind == GFGPU_TERM_SOURCE) {
+      src_slot = T.field_slot;
+      csrc += T.scale * (T.c[0].kind == GFGPU_COEF_NONE ? 1.0 : val(T.c[0]));
+    }
+  }
+  for (int i = tid; i < NB; i += kSfThreads) {
+    const int32_t n = enode[e * NB + i];
+    const int p = sf->perm[i];
+    const double ui = u ? u[n] : 0.0;
+    U[p] = ui;
+    if (HASV) Hd[p] = cm * ui + (src_slot >= 0 ? csrc * slots.p[src_slot][n] : 0.0);
+  }
+  if (tid == 0) {
+    double K[9];
+    for (int d = 0; d < 3; ++d)
+      for (int m = 0; m < 3; ++m) {
+        double s = 0.0;
+        for (int v = 0; v < 8; ++v) s += pts[int64_t(cv[e * 8 + v]) * 3 + d] * ggrad0[v * 3 + m];
+        K[d + 3 * m] = s;
+      }
+    const double a0 = K[4] * K[8] - K[5] * K[7];
+    const double a1 = K[5] * K[6] - K[3] * K[8];
+    const double a2 = K[3] * K[7] - K[4] * K[6];
+    const double det = K[0] * a0 + K[1] * a1 + K[2] * a2;
+    if (det == 0.0) set_err(err, ERR_JACOBIAN);
+    double B[9];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+        B[i + 3 * j] = (K[i1 + 3 * j1] * K[i2 + 3 * j2] - K[i1 + 3 * j2] * K[i2 + 3 * j1]) / det;
+      }
+    const double J = det == 0.0 ? 0.0 : fabs(det);
+    const int pm[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+    for (int k = 0; k < 6; ++k) {
+      double s = 0.0;
+      for (int d = 0; d < 3; ++d) s += B[d + 3 * pm[k][0]] * B[d + 3 * pm[k][1]];
+      cM[k] = c1 * J * s;
+    }
+    cJ = J;
+  }
+  __syncthreads();
+  // ---- x: A0 = N_x u, A1 = D_x u, A2 = N_x h          [c][b][qx]
+  for (int t = tid; t < P1 * P1 * Q1; t += kSfThreads) {
+    const int qx = t % Q1, cb = t / Q1;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+#pragma unroll
+    for (int a = 0; a < P1; ++a) {
+      const double x = U[cb * P1 + a];
+      s0 = fma(sN[qx][a], x, s0);
+      s1 = fma(sD[qx][a], x, s1);
+      if (HASV) s2 = fma(sN[qx][a], Hd[cb * P1 + a], s2);
+    }
+    A0[t] = s0, A1[t] = s1;
+    if (HASV) A2[t] = s2;
+  }
+  __syncthreads();
+  // ---- y: B0 = N_y A1 (d/dx), B1 = D_y A0 (d/dy), B2 = N_y A0 (d/dz), B3 = N_y A2
+  for (int t = tid; t < P1 * Q1 * Q1; t += kSfThreads) {
+    const int qx = t % Q1, qy = (t / Q1) % Q1, c = t / (Q1 * Q1);
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+#pragma unroll
+    for (int b = 0; b < P1; ++b) {
+      const int k = (c * P1 + b) * Q1 + qx;
+      s0 = fma(sN[qy][b], A1[k], s0);
+      s1 = fma(sD[qy][b], A0[k], s1);
+      s2 = fma(sN[qy][b], A0[k], s2);
+      if (HASV) s3 = fma(sN[qy][b], A2[k], s3);
+    }
+    B0[t] = s0, B1[t] = s1, B2[t] = s2;
+    if (HASV) B3[t] = s3;
+  }
+  __syncthreads();
+  // ---- z: gradient and value at the Gauss points, then the fluxes
+  // (A0..A3 reused as fx, fy, fz, fh on [qz][qy][qx])
+  for (int t = tid; t < Q1 * Q1 * Q1; t += kSfThreads) {
+    const int qx = t % Q1, qy = (t / Q1) % Q1, qz = t / (Q1 * Q1);
+    double gx = 0.0, gy = 0.0, gz = 0.0, hv = 0.0;
+#pragma unroll
+    for (int c = 0; c < P1; ++c) {
+      const int k = (c * Q1 + qy) * Q1 + qx;
+      gx = fma(sN[qz][c], B0[k], gx);
+      gy = fma(sN[qz][c], B1[k], gy);
+      gz = fma(sD[qz][c], B2[k], gz);
+      if (HASV) hv = fma(sN[qz][c], B3[k], hv);
+    }
+    const double w = sw[qx] * sw[qy] * sw[qz];
+    A0[t] = w * (cM[0] * gx + cM[3] * gy + cM[4] * gz);
+    A1[t] = w * (cM[3] * gx + cM[1] * gy + cM[5] * gz);
+    A2[t] = w * (cM[4] * gx + cM[5] * gy + cM[2] * gz);
+    if (HASV) A3[t] = w * cJ * hv;
+  }
+  __syncthreads();
+  // ---- z^T: B0 = N_z^T fx, B1 = N_z^T fy, B2 = D_z^T fz + N_z^T fh   [c][qy][qx]
+  for (int t = tid; t < P1 * Q1 * Q1; t += kSfThreads) {
+    const int qx = t % Q1, qy = (t / Q1) % Q1, c = t / (Q1 * Q1);
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+#pragma unroll
+    for (int qz = 0; qz < Q1; ++qz) {
+      const int k = (qz * Q1 + qy) * Q1 + qx;
+      s0 = fma(sN[qz][c], A0[k], s0);
+      s1 = fma(sN[qz][c], A1[k], s1);
+      s2 = fma(sD[qz][c], A2[k], s2);
+      if (HASV) s2 = fma(sN[qz][c], A3[k], s2);
+    }
+    B0[t] = s0, B1[t] = s1, B2[t] = s2;
+  }
+  __syncthreads();
+  // ---- y^T: A0 = N_y^T B0 (-> D_x^T), A1 = D_y^T B1 + N_y^T B2 (-> N_x^T)   [c][b][qx]
+  for (int t = tid; t < P1 * P1 * Q1; t += kSfThreads) {
+    const int qx = t % Q1, b = (t / Q1) % P1, c = t / (Q1 * P1);
+    double s0 = 0.0, s1 = 0.0;
+#pragma unroll
+    for (int qy = 0; qy < Q1; ++qy) {
+      const int k = (c * Q1 + qy) * Q1 + qx;
+      s0 = fma(sN[qy][b], B0[k], s0);
+      s1 = fma(sD[qy][b], B1[k], s1);
+      s1 = fma(sN[qy][b], B2[k], s1);
+    }
+    A0[t] = s0, A1[t] = s1;
+  }
+  __syncthreads();
+  // ---- x^T: V_e = D_x^T A0 + N_x^T A1, written in local DOF order
+  double *o = out + e * L.stride;
+  for (int i = tid; i < NB; i += kSfThreads) {
+    const int p = sf->perm[i];
+    const int a = p % P1, cb = p / P1;
+    double s = 0.0;
+#pragma unroll
+    for (int qx = 0; qx < Q1; ++qx) {
+      s = fma(sD[qx][a], A0[cb * Q1 + qx], s);
+      s = fma(sN[qx][a], A1[cb * Q1 + qx], s);
+    }
+    if (!isfinite(s)) set_err(err, ERR_NAN);
+    o[L.off_vec + i] = s;
+  }
+}
+
 }  // namespace
 
 // The forms of this kernel: scalar GRADGRAD (c1), MASS and SOURCE terms with
@@ -246,12 +438,111 @@ void build_affine_hex_tables(Plan &P) {
 
 bool affine_hex_available(int degree) { return degree == 1 || degree == 2 || degree == 3 || degree == 4; }
 
+namespace {
+
+// The 1D tables of the sum factorisation, checked against the 3-D tables
+// (values and gradients at every Gauss point): false (no sum factorisation)
+// if the basis or the rule does not factor to 1e-9.  *exact: they agree to
+// 1e-14 (values) / 1e-13 (gradients).  The reference evaluates the QK basis
+// from its expanded monomial coefficients; for K >= 3 that evaluation is off
+// the exact tensor product by 1e-12 (K = 3) to 1.5e-10 (K = 4), so only
+// K <= 2 reproduces the reference's sums to its own rounding.
+template <int P1, int Q1>
+bool make_sumfac(const Plan &P, int K1d, std::vector<double> &blob, bool *exact) {
+  SumFac<P1, Q1> t{};
+  RefElement e1(1, SIMPLEX, P1 - 1), e3(3, HEX, P1 - 1);
+  Quadrature q1;
+  if (!quadrature_by_name("IM_GAUSS1D(" + std::to_string(K1d) + ")", q1) || q1.nq != Q1 ||
+      e1.nb != P1 || e3.nb != P1 * P1 * P1 || P.nq != Q1 * Q1 * Q1)
+    return false;
+  for (int q = 0; q < Q1; ++q) {
+    double v[P1], g[P1];
+    e1.eval(&q1.pts[q], v, g);
+    for (int j = 0; j < P1; ++j) {
+      const int a = e1.lattice[j];
+      t.N[q][a] = v[j];
+      t.D[q][a] = g[j];
+    }
+    t.w[q] = q1.w[q];
+  }
+  for (int i = 0; i < e3.nb; ++i)
+    t.perm[i] = e3.lattice[i * 3] + P1 * (e3.lattice[i * 3 + 1] + P1 * e3.lattice[i * 3 + 2]);
+  // the 3-D rule is the tensor product, first coordinate fastest
+  double ev = 0.0, eg = 0.0;
+  for (int q = 0; q < P.nq; ++q) {
+    const int qx = q % Q1, qy = (q / Q1) % Q1, qz = q / (Q1 * Q1);
+    if (std::fabs(P.h_w[q] - t.w[qx] * t.w[qy] * t.w[qz]) > 1e-15) return false;
+    for (int i = 0; i < e3.nb; ++i) {
+      const int a = e3.lattice[i * 3], b = e3.lattice[i * 3 + 1], c = e3.lattice[i * 3 + 2];
+      const double v = t.N[qx][a] * t.N[qy][b] * t.N[qz][c];
+      const double g[3] = {t.D[qx][a] * t.N[qy][b] * t.N[qz][c],
+                           t.N[qx][a] * t.D[qy][b] * t.N[qz][c],
+                           t.N[qx][a] * t.N[qy][b] * t.D[qz][c]};
+      ev = std::max(ev, std::fabs(v - P.h_val[size_t(q) * P.nb + i]));
+      for (int d = 0; d < 3; ++d)
+        eg = std::max(eg, std::fabs(g[d] - P.h_grad[(size_t(q) * P.nb + i) * 3 + d]));
+    }
+  }
+  if (ev > 1e-9 || eg > 1e-8) return false;
+  *exact = ev <= 1e-14 && eg <= 1e-13;
+  blob.assign((sizeof(t) + 7) / 8, 0.0);
+  std::memcpy(blob.data(), &t, sizeof(t));
+  return true;
+}
+
+}  // namespace
+
+// Sum-factorisation tables of a parallelepiped plan (P.h_sf; empty if the
+// element / rule pair is not one of the instantiated ones or does not factor).
+void build_affine_hex_sumfac(Plan &P) {
+  P.h_sf.clear();
+  int N = 0, K = 0;
+  if (sscanf(P.im.c_str(), "IM_GAUSS_PARALLELEPIPED(%d,%d)", &N, &K) != 2 || N != 3) return;
+  const int P1 = P.degree + 1, Q1 = K / 2 + 1;
+  bool ok = false, exact = false;
+  if (P1 == 2 && Q1 == 2) ok = make_sumfac<2, 2>(P, K, P.h_sf, &exact);
+  else if (P1 == 2 && Q1 == 3) ok = make_sumfac<2, 3>(P, K, P.h_sf, &exact);
+  else if (P1 == 3 && Q1 == 3) ok = make_sumfac<3, 3>(P, K, P.h_sf, &exact);
+  else if (P1 == 4 && Q1 == 4) ok = make_sumfac<4, 4>(P, K, P.h_sf, &exact);
+  else if (P1 == 5 && Q1 == 5) ok = make_sumfac<5, 5>(P, K, P.h_sf, &exact);
+  if (!ok) P.h_sf.clear();
+  P.sf_exact = ok && exact;
+}
+
 cudaError_t launch_affine_hex_pass(Plan &P, bool want_K) {
   if (P.n_elements == 0) return cudaSuccess;
   SlotPtrs sp;
   for (int i = 0; i < GFGPU_MAX_SLOTS; ++i) sp.p[i] = P.slot_ptr[i];
   if (P.slot_n[GFGPU_SLOT_U] != P.n_dof) sp.p[GFGPU_SLOT_U] = nullptr;
   const unsigned grid = unsigned(P.n_elements);
+  if (!want_K && P.d_sf && (P.sf_exact || P.sf_requested)) {
+    // vector only: sum factorisation
+    bool hasv = false;
+    for (int t = 0; t < P.form.n_terms; ++t)
+      hasv |= P.form.terms[t].kind == GFGPU_TERM_MASS || P.form.terms[t].kind == GFGPU_TERM_SOURCE;
+    const int P1 = P.degree + 1, Q1 = int(std::lround(std::cbrt(double(P.nq))));
+#define SFK(A, B)                                                                               \
+  do {                                                                                         \
+    const auto *tab = reinterpret_cast<const SumFac<A, B> *>(P.d_sf);                          \
+    if (hasv)                                                                                  \
+      affine_hex_apply_kernel<A, B, true><<<grid, kSfThreads, 0, P.stream>>>(                   \
+          P.n_elements, P.d_points, P.d_cv, P.d_enode, tab, P.d_ggrad, P.lay, P.form, sp,     \
+          P.d_elem, P.d_err);                                                                  \
+    else                                                                                       \
+      affine_hex_apply_kernel<A, B, false><<<grid, kSfThreads, 0, P.stream>>>(                  \
+          P.n_elements, P.d_points, P.d_cv, P.d_enode, tab, P.d_ggrad, P.lay, P.form, sp,     \
+          P.d_elem, P.d_err);                                                                  \
+  } while (0)
+    if (P1 == 2 && Q1 == 2) SFK(2, 2);
+    else if (P1 == 2 && Q1 == 3) SFK(2, 3);
+    else if (P1 == 3 && Q1 == 3) SFK(3, 3);
+    else if (P1 == 4 && Q1 == 4) SFK(4, 4);
+    else if (P1 == 5 && Q1 == 5) SFK(5, 5);
+    else return cudaErrorInvalidValue;
+#undef SFK
+    P.launches++;
+    return cudaGetLastError();
+  }
 #define AFF(NB)                                                                                \
   do {                                                                                         \
     if (want_K)                                                                                \

@@ -124,6 +124,12 @@ struct Plan {
   bool affine_hex = false;
   std::vector<double> h_aff;
   double *d_aff = nullptr;
+  // sum factorisation of the vector-only pass (tensor-product basis on a
+  // parallelepiped): 1D tables, empty when the basis does not factor
+  std::vector<double> h_sf;
+  double *d_sf = nullptr;
+  bool sf_exact = false;      // the 1D tables reproduce the reference's 3-D ones
+  bool sf_requested = false;  // GFGPU_SUM_FACTORISATION on the current call
   bool kmat = true;        // an element-matrix kernel exists (orders 1 and 2)
   bool kpot = false;       // the Gauss-point potential kernel exists (order 0)
   // point -> (element, vertex) adjacency, codes e * nbg + v sorted by e
@@ -249,6 +255,7 @@ bool affine_hex_form_ok(const gfgpu_form &f, int qdim);
 bool mesh_is_parallelepiped(const double *pts, const int64_t *cv, int64_t E);
 bool affine_hex_available(int degree);
 void build_affine_hex_tables(Plan &P);
+void build_affine_hex_sumfac(Plan &P);
 cudaError_t launch_affine_hex_pass(Plan &P, bool want_K);
 // Gauss-point element kernels (k_hex.cu)
 bool gauss_element_available(int kind, int law, int degree, int qdim, int nq);

@@ -227,6 +227,15 @@ int gfgpu_device_vector(gfgpu_plan *plan, double **vec);
                                    in the same pass */
 #define GFGPU_PROFILE 4         /* record CUDA events around each kernel of
                                    this call (gfgpu_kernel_times) */
+#define GFGPU_SUM_FACTORISATION 16 /* order 1 on parallelepiped hexahedra with a
+                                   scalar form and the pattern built: the
+                                   matrix-free R = K u + load by 1D
+                                   contractions with the exact tensor-product
+                                   basis, also for FEM_QK(3,3|4), where the
+                                   reference's monomial evaluation of the basis
+                                   is off the tensor product by 1e-12..1.5e-10
+                                   (so R differs from the reference's at that
+                                   level); FEM_QK(3,1|2) use it by default */
 #define GFGPU_CONDENSATION 8    /* order 2 of a form with an INTERNAL_P term:
                                    static condensation of p
                                    (ga_workspace::assembly(2, true),

@@ -152,3 +152,82 @@ def test_hex_deterministic():
     K1 = ws.assembled_matrix().copy()
     ws.assembly(2)
     assert np.array_equal(K1.data, ws.assembled_matrix().data)
+
+
+AFFINE_SF = [
+    # degree, im, expression, data: parallelepiped meshes (no jitter), so the
+    # vector-only pass is sum-factorised
+    (4, "IM_GAUSS_PARALLELEPIPED(3,9)", "kappa*Grad_u.Grad_Test_u", {"kappa": "P0"}),
+    (4, "IM_GAUSS_PARALLELEPIPED(3,9)", "kappa*Grad_u.Grad_Test_u + 2*u*Test_u - f*Test_u",
+     {"kappa": "P0", "f": "V"}),
+    (2, "IM_GAUSS_PARALLELEPIPED(3,5)", "kappa*Grad_u.Grad_Test_u - f*Test_u",
+     {"kappa": "P0", "f": "V"}),
+    (1, "IM_GAUSS_PARALLELEPIPED(3,3)", "3*Grad_u.Grad_Test_u + u*Test_u", {}),
+    (3, "IM_GAUSS_PARALLELEPIPED(3,7)", "kappa*Grad_u.Grad_Test_u", {"kappa": "P0"}),
+]
+
+
+@pytest.mark.parametrize("case", range(len(AFFINE_SF)))
+def test_vector_pass_after_pattern(case):
+    """A repeated order-1 assembly (pattern built) on parallelepipeds takes the
+    vector-only pass: sum-factorised for FEM_QK(3,1|2), whose 1D tables
+    reproduce the reference's 3-D basis tables to 1e-14; element tables for
+    K >= 3.  Both match the oracle's per-point sums."""
+    degree, im, expr, data = AFFINE_SF[case]
+    mesh, mf, mim, ws, rng = affine_sf_case(case)
+    Ro = oracle_problem(mesh, mf, mim, ws.groups[0].order1, slots_of(ws)).vector(nthreads=4)
+    ws.assembly(1)   # first: element matrices formed (the plan's pattern is built)
+    e1 = vec_errors(ws.assembled_vector(), Ro).max()
+    ws.assembly(1)   # vector only
+    e2 = vec_errors(ws.assembled_vector(), Ro).max()
+    assert e1 <= RTOL and e2 <= RTOL, (e1, e2)
+
+
+def affine_sf_case(case):
+    degree, im, expr, data = AFFINE_SF[case]
+    rng = np.random.default_rng(40 + case)
+    nx = 3 if degree <= 2 else 2
+    # a sheared but parallelepiped mesh: an affine map of the unit cube
+    mesh = g.Mesh.regular_unit(3, nx, "hex")
+    A = np.array([[1.0, 0.2, 0.1], [0.0, 0.9, 0.15], [0.05, 0.0, 1.1]])
+    mesh.points = np.ascontiguousarray(mesh.points @ A.T)
+    mf = g.MeshFem(mesh, 1, degree=degree)
+    mim = g.MeshIm(mesh, im)
+    ws = g.GaWorkspace()
+    ws.add_fem_variable("u", mf, U=rng.standard_normal(mf.nb_dof()))
+    for nm, kind in data.items():
+        if kind == "P0":
+            ws.add_fem_constant(nm, g.MeshFem(mesh, 1, degree=0),
+                                np.exp(rng.normal(0, 0.5, mesh.nb_convex())))
+        else:
+            ws.add_fem_constant(nm, mf, rng.uniform(-1, 1, mf.nb_dof()))
+    ws.add_expression(expr, mim)
+    return mesh, mf, mim, ws, rng
+
+
+@pytest.mark.parametrize("case", [0, 1, 4])
+def test_opt_in_sum_factorisation_high_order(case):
+    """GFGPU_SUM_FACTORISATION on FEM_QK(3,3|4): the exact tensor-product
+    basis instead of the reference's monomial evaluation of it (off by up to
+    1.5e-10 at K = 4).  R stays within 1e-8 of the reference-exact pass
+    (relative, floor 1e-3 of the largest entry) and the call is repeatable
+    bit for bit."""
+    import ctypes as C
+    from getfem_gb300 import _lib as L
+    mesh, mf, mim, ws, rng = affine_sf_case(case)
+    ws.assembly(1)
+    ws.assembly(1)
+    Rref = ws.assembled_vector().copy()
+    grp = ws.groups[0]
+    h = ws._plan(grp, grp.order1)
+    lib = L.lib()
+    out = []
+    for _ in range(2):
+        L.check(lib.gfgpu_assemble(h, 1, L.SUM_FACTORISATION, None))
+        L.check(lib.gfgpu_sync(h))
+        v = np.empty(mf.nb_dof())
+        L.check(lib.gfgpu_copy_result(h, L.RESULT_VECTOR, v.ctypes.data_as(C.c_void_p)))
+        out.append(v)
+    assert np.array_equal(out[0], out[1])
+    err = vec_errors(out[0], Rref).max()
+    assert 0.0 < err <= 1e-8, err
