@@ -43,6 +43,50 @@ namespace {
 constexpr int kAffThreads = 256;
 constexpr int kAffTables = 7;  // G_00, G_11, G_22, G_01, G_02, G_12, Mhat
 
+// Geometry of parallelepiped element e, lane-parallel in one warp (an FP64
+// warp instruction occupies the pipe as long with one active lane as with
+// 32): K(d,m) = sum_v x_v[d] dphi_v/dxi_m on lanes 0-8, det and B = K^{-T}
+// (cofactor / det) on lanes 0-8, M = B^T B upper triangle (00, 11, 22, 01,
+// 02, 12) on lanes 0-5.  Writes g[0..8] = K, g[9..17] = B, g[18..23] = M,
+// g[24] = |det| (0 for a degenerate element, which sets ERR_JACOBIAN).
+__device__ __forceinline__ void parallelepiped_geometry(int lane, int64_t e,
+                                                        const double *__restrict__ pts,
+                                                        const int32_t *__restrict__ cv,
+                                                        const double *__restrict__ ggrad0,
+                                                        double *g, int *err) {
+  if (lane < 9) {
+    const int d = lane % 3, m = lane / 3;
+    double s = 0.0;
+    for (int v = 0; v < 8; ++v) s += pts[int64_t(cv[e * 8 + v]) * 3 + d] * ggrad0[v * 3 + m];
+    g[lane] = s;
+  }
+  __syncwarp();
+  if (lane < 9) {
+    const double *K = g;
+    const double a0 = K[4] * K[8] - K[5] * K[7];
+    const double a1 = K[5] * K[6] - K[3] * K[8];
+    const double a2 = K[3] * K[7] - K[4] * K[6];
+    const double det = K[0] * a0 + K[1] * a1 + K[2] * a2;
+    const int i = lane % 3, j = lane / 3;
+    const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+    g[9 + lane] = (K[i1 + 3 * j1] * K[i2 + 3 * j2] - K[i1 + 3 * j2] * K[i2 + 3 * j1]) / det;
+    if (lane == 0) {
+      if (det == 0.0) set_err(err, ERR_JACOBIAN);
+      g[24] = det == 0.0 ? 0.0 : fabs(det);
+    }
+  }
+  __syncwarp();
+  if (lane < 6) {
+    const int m = lane < 3 ? lane : (lane == 5 ? 1 : 0);
+    const int n = lane < 3 ? lane : (lane == 3 ? 1 : 2);
+    const double *B = g + 9;
+    double s = 0.0;
+    for (int d = 0; d < 3; ++d) s += B[d + 3 * m] * B[d + 3 * n];
+    g[18 + lane] = s;
+  }
+  __syncwarp();
+}
+
 template <int NB, bool WANT_K>
 __global__ void __launch_bounds__(kAffThreads) affine_hex_kernel(
     int64_t E, const double *__restrict__ pts, const int32_t *__restrict__ cv,
@@ -55,6 +99,7 @@ __global__ void __launch_bounds__(kAffThreads) affine_hex_kernel(
   __shared__ double cf;              // load factor c_f |J|
   __shared__ double us[NB], fs[NB];
   __shared__ unsigned long long smax;
+  __shared__ double geo[25];         // K, B, B^T B, |J|
   const int64_t e = blockIdx.x;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const double *u = slots.p[GFGPU_SLOT_U];
@@ -66,53 +111,29 @@ __global__ void __launch_bounds__(kAffThreads) affine_hex_kernel(
     us[j] = u ? u[n] : 0.0;
     fs[j] = src_slot >= 0 ? slots.p[src_slot][n] : 0.0;
   }
-  if (tid == 0) {
-    smax = 0ull;
-    // K(d,m) = sum_v x_v[d] dphi_v/dxi_m (constant on a parallelepiped)
-    double K[9];
-    for (int d = 0; d < 3; ++d)
-      for (int m = 0; m < 3; ++m) {
-        double s = 0.0;
-        for (int v = 0; v < 8; ++v) s += pts[int64_t(cv[e * 8 + v]) * 3 + d] * ggrad0[v * 3 + m];
-        K[d + 3 * m] = s;
+  if (wid == 0) {
+    parallelepiped_geometry(lane, e, pts, cv, ggrad0, geo, err);
+    if (lane == 0) {
+      smax = 0ull;
+      const double J = geo[24];
+      double c1 = 0.0, cm = 0.0, csrc = 0.0;
+      for (int t = 0; t < form.n_terms; ++t) {
+        const gfgpu_term &T = form.terms[t];
+        auto val = [&](const gfgpu_coef &c) {
+          if (c.kind == GFGPU_COEF_CONST) return c.value;
+          if (c.kind == GFGPU_COEF_ELEMENT) return c.value * slots.p[c.slot][e];
+          return 0.0;
+        };
+        if (T.kind == GFGPU_TERM_GRADGRAD) c1 += T.scale * val(T.c[1]);
+        else if (T.kind == GFGPU_TERM_MASS) cm += T.scale * val(T.c[0]);
+        else if (T.kind == GFGPU_TERM_SOURCE)
+          csrc += T.scale * (T.c[0].kind == GFGPU_COEF_NONE ? 1.0 : val(T.c[0]));
       }
-    const double a0 = K[4] * K[8] - K[5] * K[7];
-    const double a1 = K[5] * K[6] - K[3] * K[8];
-    const double a2 = K[3] * K[7] - K[4] * K[6];
-    const double det = K[0] * a0 + K[1] * a1 + K[2] * a2;
-    if (det == 0.0) set_err(err, ERR_JACOBIAN);
-    double B[9];  // B(d,m) = cofactor(d,m) / det = K^{-T}(d,m)
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) {
-        const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
-        B[i + 3 * j] = (K[i1 + 3 * j1] * K[i2 + 3 * j2] - K[i1 + 3 * j2] * K[i2 + 3 * j1]) / det;
-      }
-    const double J = det == 0.0 ? 0.0 : fabs(det);
-    double M[9];  // M = B^T B
-    for (int m = 0; m < 3; ++m)
-      for (int n = 0; n < 3; ++n) {
-        double s = 0.0;
-        for (int d = 0; d < 3; ++d) s += B[d + 3 * m] * B[d + 3 * n];
-        M[m + 3 * n] = s;
-      }
-    double c1 = 0.0, cm = 0.0, csrc = 0.0;
-    for (int t = 0; t < form.n_terms; ++t) {
-      const gfgpu_term &T = form.terms[t];
-      auto val = [&](const gfgpu_coef &c) {
-        if (c.kind == GFGPU_COEF_CONST) return c.value;
-        if (c.kind == GFGPU_COEF_ELEMENT) return c.value * slots.p[c.slot][e];
-        return 0.0;
-      };
-      if (T.kind == GFGPU_TERM_GRADGRAD) c1 += T.scale * val(T.c[1]);
-      else if (T.kind == GFGPU_TERM_MASS) cm += T.scale * val(T.c[0]);
-      else if (T.kind == GFGPU_TERM_SOURCE)
-        csrc += T.scale * (T.c[0].kind == GFGPU_COEF_NONE ? 1.0 : val(T.c[0]));
+      const double cJ = c1 * J;
+      for (int k = 0; k < 6; ++k) cp[k] = cJ * geo[18 + k];
+      cp[6] = cm * J;
+      cf = csrc * J;
     }
-    const double cJ = c1 * J;
-    cp[0] = cJ * M[0], cp[1] = cJ * M[4], cp[2] = cJ * M[8];
-    cp[3] = cJ * M[3], cp[4] = cJ * M[6], cp[5] = cJ * M[7];
-    cp[6] = cm * J;
-    cf = csrc * J;
   }
   __syncthreads();
   double c[kAffTables];
@@ -193,6 +214,7 @@ __global__ void __launch_bounds__(kSfThreads) affine_hex_apply_kernel(
   constexpr int M3 = (P1 > Q1 ? P1 : Q1) * (P1 > Q1 ? P1 : Q1) * (P1 > Q1 ? P1 : Q1);
   __shared__ double sN[Q1][P1], sD[Q1][P1], sw[Q1];
   __shared__ double cM[6], cJ;            // c1 |J| B^T B (upper), |J|
+  __shared__ double geo[25];              // K, B, B^T B, |J|
   __shared__ double U[M3], Hd[M3];        // u and h = c_m u + c_f f (tensor order)
   __shared__ double A0[M3], A1[M3], A2[M3], A3[M3];
   __shared__ double B0[M3], B1[M3], B2[M3], B3[M3];
@@ -228,33 +250,10 @@ __global__ void __launch_bounds__(kSfThreads) affine_hex_apply_kernel(
     U[p] = ui;
     if (HASV) Hd[p] = cm * ui + (src_slot >= 0 ? csrc * slots.p[src_slot][n] : 0.0);
   }
-  if (tid == 0) {
-    double K[9];
-    for (int d = 0; d < 3; ++d)
-      for (int m = 0; m < 3; ++m) {
-        double s = 0.0;
-        for (int v = 0; v < 8; ++v) s += pts[int64_t(cv[e * 8 + v]) * 3 + d] * ggrad0[v * 3 + m];
-        K[d + 3 * m] = s;
-      }
-    const double a0 = K[4] * K[8] - K[5] * K[7];
-    const double a1 = K[5] * K[6] - K[3] * K[8];
-    const double a2 = K[3] * K[7] - K[4] * K[6];
-    const double det = K[0] * a0 + K[1] * a1 + K[2] * a2;
-    if (det == 0.0) set_err(err, ERR_JACOBIAN);
-    double B[9];
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) {
-        const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
-        B[i + 3 * j] = (K[i1 + 3 * j1] * K[i2 + 3 * j2] - K[i1 + 3 * j2] * K[i2 + 3 * j1]) / det;
-      }
-    const double J = det == 0.0 ? 0.0 : fabs(det);
-    const int pm[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
-    for (int k = 0; k < 6; ++k) {
-      double s = 0.0;
-      for (int d = 0; d < 3; ++d) s += B[d + 3 * pm[k][0]] * B[d + 3 * pm[k][1]];
-      cM[k] = c1 * J * s;
-    }
-    cJ = J;
+  if (tid < 32) {
+    parallelepiped_geometry(tid, e, pts, cv, ggrad0, geo, err);
+    if (tid < 6) cM[tid] = c1 * geo[24] * geo[18 + tid];
+    if (tid == 0) cJ = geo[24];
   }
   __syncthreads();
   // ---- x: A0 = N_x u, A1 = D_x u, A2 = N_x h          [c][b][qx]

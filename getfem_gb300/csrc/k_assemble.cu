@@ -416,6 +416,38 @@ __global__ void __launch_bounds__(128) gather_kernel(
                      vals, want_K, want_R, vec, err, ncol, u);
 }
 
+// Vector-only gather (no matrix): one thread per DOF node adds the QD
+// components of its adjacent elements' vectors in adjacency order, the
+// order gather_node sums them in, so R is the same bit for bit; no shared
+// memory, so the launch runs at full occupancy.
+template <int QD>
+__global__ void __launch_bounds__(256) vector_gather_kernel(
+    int64_t n0, int64_t n1, KeLayout L, const int32_t *__restrict__ adj_ptr,
+    const int32_t *__restrict__ adj, const double *__restrict__ elem,
+    double *__restrict__ vec, int *__restrict__ err) {
+  const int64_t node = n0 + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (node >= n1) return;
+  const int a0 = adj_ptr[node], a1 = adj_ptr[node + 1];
+  const int nb = L.nb;
+  double r[QD];
+#pragma unroll
+  for (int a = 0; a < QD; ++a) r[a] = 0.0;
+  for (int k = a0; k < a1; ++k) {
+    const int code = adj[k];
+    const int e = code / nb;
+    const double *v = elem + int64_t(e) * L.stride + L.off_vec + (code - e * nb) * QD;
+#pragma unroll
+    for (int a = 0; a < QD; ++a) r[a] += v[a];
+  }
+  bool bad = false;
+#pragma unroll
+  for (int a = 0; a < QD; ++a) {
+    bad |= !isfinite(r[a]);
+    vec[node * QD + a] = r[a];
+  }
+  if (bad) set_err(err, ERR_NAN);
+}
+
 // Persistent row gather over the DOF nodes of every mesh of a batch (R = 1:
 // rows of at most 32 columns); warp w of the grid takes nodes w, w + warps, ...
 template <int QD>
@@ -494,6 +526,29 @@ cudaError_t launch_gather_q(Plan &P, bool want_K, bool want_R, int64_t i0, int64
     case 4: return launch_gather_t<QD, 4>(P, want_K, want_R, i0, i1, order, ms, mad);
     default: return cudaErrorInvalidValue;
   }
+}
+
+cudaError_t launch_vector_gather(Plan &P, int64_t n0, int64_t n1) {
+  if (n1 <= n0) return cudaSuccess;
+  constexpr int kThreads = 256;
+  const unsigned blocks = unsigned((n1 - n0 + kThreads - 1) / kThreads);
+  switch (P.qdim) {
+    case 1:
+      vector_gather_kernel<1><<<blocks, kThreads, 0, P.stream>>>(
+          n0, n1, P.lay, P.d_adj_ptr, P.d_adj, P.d_elem, P.d_vec, P.d_err);
+      break;
+    case 2:
+      vector_gather_kernel<2><<<blocks, kThreads, 0, P.stream>>>(
+          n0, n1, P.lay, P.d_adj_ptr, P.d_adj, P.d_elem, P.d_vec, P.d_err);
+      break;
+    case 3:
+      vector_gather_kernel<3><<<blocks, kThreads, 0, P.stream>>>(
+          n0, n1, P.lay, P.d_adj_ptr, P.d_adj, P.d_elem, P.d_vec, P.d_err);
+      break;
+    default: return cudaErrorInvalidValue;
+  }
+  P.launches++;
+  return cudaGetLastError();
 }
 
 cudaError_t launch_gather_list(Plan &P, bool want_K, bool want_R, int64_t i0, int64_t i1,
@@ -576,14 +631,16 @@ cudaError_t batch_gather_attr(size_t smem) {
 }
 
 cudaError_t launch_gather_range(Plan &P, bool want_K, bool want_R, int64_t n0, int64_t n1) {
+  if (!want_K) return want_R ? launch_vector_gather(P, n0, n1) : cudaSuccess;
   return launch_gather_list(P, want_K, want_R, n0, n1, nullptr, P.max_slots, P.max_adj);
 }
 
 // The whole gather: one launch per valence bucket (nodes with similar
 // element counts, so the 4 warps of a block finish together and each launch
 // reserves only its own bucket's shared memory), else one launch over all
-// nodes.
+// nodes; a vector-only gather is one thread per node.
 cudaError_t launch_gather(Plan &P, bool want_K, bool want_R) {
+  if (!want_K) return launch_gather_range(P, want_K, want_R, 0, P.n_nodes);
   if (P.d_order && P.bucket_ms.size() + 1 == P.h_bucket.size()) {
     for (size_t b = 0; b + 1 < P.h_bucket.size(); ++b) {
       cudaError_t ce = launch_gather_list(P, want_K, want_R, P.h_bucket[b], P.h_bucket[b + 1],
