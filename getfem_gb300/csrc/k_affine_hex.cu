@@ -17,8 +17,8 @@
 //
 // One CTA per element.  K_e is symmetric: each thread owns upper-triangle
 // entries (tables read coalesced from L2) and writes both (r,c) and (c,r).
-// V_e = K_e u_e + load is then formed by one warp per row from the rows just
-// written.
+// V_e = K_e u_e + load is then formed by one thread per row from the
+// (symmetric) columns just written.
 //
 // The vector-only pass (matrix-free R = K u + load) is sum-factorised: the
 // FEM_QK(3,K) basis is the tensor product of the FEM_PK(1,K) basis
@@ -157,32 +157,30 @@ __global__ void __launch_bounds__(kAffThreads) affine_hex_kernel(
     atomicMax(&smax, mx);
     __syncthreads();  // the rows of K_e are visible to the block
   }
-  // V_e[r] = sum_c K_e[r,c] u_c + c_f sum_c Mhat[r,c] f_c, one warp per row
-  for (int r = wid; r < NB; r += kAffThreads / 32) {
+  // V_e[r] = sum_c K_e[r,c] u_c + c_f sum_c Mhat[r,c] f_c, one thread per row.
+  // K_e and the tables are symmetric bit for bit (both halves of K_e are one
+  // value; the tables' (i,j) and (j,i) sums add the same products), so thread
+  // r walks column r instead: the loads coalesce across threads and no warp
+  // reduction is needed (one FMA per entry; the butterfly of a warp per row
+  // cost more FP64 instructions than the row's FMAs).
+  for (int r = tid; r < NB; r += kAffThreads) {
     double s = 0.0, sf = 0.0;
-    for (int col = lane; col < NB; col += 32) {
+    for (int col = 0; col < NB; ++col) {
+      const int idx = col * NB + r;
       double k;
       if constexpr (WANT_K) {
-        k = o[r * L.rowstride + col];
+        k = o[col * L.rowstride + r];
       } else {
-        const int idx = r * NB + col;
         k = c[0] * tabs[idx];
 #pragma unroll
         for (int p = 1; p < kAffTables; ++p) k = fma(c[p], tabs[p * NN + idx], k);
       }
       s = fma(k, us[col], s);
-      sf = fma(tabs[6 * NN + r * NB + col], fs[col], sf);
+      if (src_slot >= 0) sf = fma(tabs[6 * NN + idx], fs[col], sf);
     }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      s += __shfl_xor_sync(0xffffffffu, s, off);
-      sf += __shfl_xor_sync(0xffffffffu, sf, off);
-    }
-    if (lane == 0) {
-      const double v = fma(cf, sf, s);
-      if (!isfinite(v)) set_err(err, ERR_NAN);
-      o[L.off_vec + r] = v;
-    }
+    const double v = fma(cf, sf, s);
+    if (!isfinite(v)) set_err(err, ERR_NAN);
+    o[L.off_vec + r] = v;
   }
   if constexpr (WANT_K) {
     if (tid == 0) {
