@@ -304,6 +304,17 @@ int check_err(Plan &P, bool repair = false) {
   return status_from_err(herr);
 }
 
+// The parallelepiped kernels of a plan need parallelepipeds: after
+// gfgpu_set_points moved the vertices off them, orders 1 and 2 fail loudly.
+int check_geometry(const Plan &P) {
+  if (P.affine_hex && !P.parallelepiped) {
+    set_last_error("the mesh points set by gfgpu_set_points no longer form parallelepipeds, "
+                   "which this plan's element kernel requires: create a new plan");
+    return GFGPU_E_UNSUPPORTED;
+  }
+  return GFGPU_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -375,11 +386,15 @@ int gfgpu_plan_create(const gfgpu_space *space, const gfgpu_form *form, void *cu
       delete P;
       return rc;
     }
+    if (S.kind == GFGPU_HEX) {
+      P->parallelepiped = mesh_is_parallelepiped(S.points, S.cvpts, S.n_elements);
+      P->h_cvpts.assign(S.cvpts, S.cvpts + S.n_elements * 8);
+    }
     if (!P->affine_simplex) {
       // parallelepiped hexahedra with a scalar isotropic form take the
       // reference-tensor kernel; the rest the Gauss-point kernel
       if (S.kind == GFGPU_HEX && P->law == LAW_ISO && affine_hex_form_ok(P->form, S.qdim) &&
-          affine_hex_available(S.degree) && mesh_is_parallelepiped(S.points, S.cvpts, S.n_elements)) {
+          affine_hex_available(S.degree) && P->parallelepiped) {
         P->affine_hex = true;
         P->kmat = true;
         build_affine_hex_tables(*P);
@@ -705,6 +720,7 @@ int gfgpu_assemble(gfgpu_plan *P, int32_t order, int32_t flags, double *potentia
     set_last_error("orders 1 and 2 are not lowered for this element, integration method and form");
     return GFGPU_E_UNSUPPORTED;
   }
+  if (int grc = check_geometry(*P)) return grc;
   const bool condense = (flags & GFGPU_CONDENSATION) != 0;
   if (condense && (P->ip_term < 0 || order != 2)) {
     set_last_error("GFGPU_CONDENSATION: order 2 of a form with an internal variable only");
@@ -839,6 +855,17 @@ int gfgpu_set_points(gfgpu_plan *P, const double *points, int64_t n, int32_t on_
                           on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                           P->stream));
   GF_CUDA(cudaStreamSynchronize(P->stream));
+  if (P->kind == GFGPU_HEX) {
+    // hexahedra: are the elements still parallelepipeds (constant Jacobian)?
+    const double *hp = points;
+    std::vector<double> tmp;
+    if (on_device) {
+      tmp.resize(size_t(n));
+      GF_CUDA(cudaMemcpy(tmp.data(), points, size_t(n) * sizeof(double), cudaMemcpyDeviceToHost));
+      hp = tmp.data();
+    }
+    P->parallelepiped = mesh_is_parallelepiped(hp, P->h_cvpts.data(), P->n_elements);
+  }
   return GFGPU_OK;
 }
 
@@ -1065,6 +1092,7 @@ int gfgpu_assemble_host(gfgpu_plan *P, const double *u, double *vals, double *ve
     return check_err(*P);
   }
   if ((rc = check_slots(*P, true))) return rc;
+  if ((rc = check_geometry(*P))) return rc;
   // The element pass, then the row gather in chunks of DOF nodes; the rows
   // of each chunk (contiguous in the CSR) are copied to the host on a second
   // stream while the next chunk is gathered.  (Writing the values from the

@@ -95,9 +95,13 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-template <int DIM, int QD, int NB, int NBG, int LAW>
+// SHAPE: mode 2 (shape derivative), compiled apart so that modes 0 and 1 do
+// not carry its per-vertex partials in registers.  const_jac: the Jacobian
+// is the same at every Gauss point (affine simplices, parallelepipeds), so K,
+// det and B are formed once per element, from the first point's table.
+template <int DIM, int QD, int NB, int NBG, int LAW, bool SHAPE>
 __global__ void __launch_bounds__(kGpWarps * 32) gauss_potential_kernel(
-    int64_t E, int nq, int mode, int wslot, const double *__restrict__ pts,
+    int64_t E, int nq, int mode, int wslot, int const_jac, const double *__restrict__ pts,
     const int32_t *__restrict__ cv, const int32_t *__restrict__ enode,
     const double *__restrict__ hval, const double *__restrict__ hvalT,
     const double *__restrict__ hgradT, const double *__restrict__ ggrad,
@@ -131,29 +135,33 @@ __global__ void __launch_bounds__(kGpWarps * 32) gauss_potential_kernel(
   for (int t = 0; t < form.n_terms; ++t)
     need_val |= form.terms[t].kind == GFGPU_TERM_MASS || form.terms[t].kind == GFGPU_TERM_SOURCE;
   double acc = 0.0;                  // energy or element-coefficient derivative
-  double accx[NBG * DIM];            // shape derivative partials of this lane
+  constexpr int NX = SHAPE ? NBG * DIM : 1;
+  double accx[NX];                   // shape derivative partials of this lane
 #pragma unroll
-  for (int k = 0; k < NBG * DIM; ++k) accx[k] = 0.0;
+  for (int k = 0; k < NX; ++k) accx[k] = 0.0;
   double accn[(NB + 31) / 32];       // nodal partials, node j = lane + 32 r
 #pragma unroll
   for (int r = 0; r < (NB + 31) / 32; ++r) accn[r] = 0.0;
+  double B[DIM * DIM], det = 0.0;
   for (int q0 = 0; q0 < nq; q0 += 32) {
     const int q = q0 + lane;
     const bool act = q < nq;
     const int qq = act ? q : 0;
-    double K[DIM * DIM];
+    if (!const_jac || q0 == 0) {
+      const int qg = const_jac ? 0 : qq;
+      double K[DIM * DIM];
 #pragma unroll
-    for (int d = 0; d < DIM; ++d)
+      for (int d = 0; d < DIM; ++d)
 #pragma unroll
-      for (int m = 0; m < DIM; ++m) {
-        double s = 0.0;
+        for (int m = 0; m < DIM; ++m) {
+          double s = 0.0;
 #pragma unroll
-        for (int v = 0; v < NBG; ++v)
-          s = madd<kFuse>(xs[v * DIM + d], ggrad[(qq * NBG + v) * DIM + m], s);
-        K[d + DIM * m] = s;
-      }
-    double B[DIM * DIM], det;
-    geo_inverse<DIM>(K, B, det);
+          for (int v = 0; v < NBG; ++v)
+            s = madd<kFuse>(xs[v * DIM + d], ggrad[(qg * NBG + v) * DIM + m], s);
+          K[d + DIM * m] = s;
+        }
+      geo_inverse<DIM>(K, B, det);
+    }
     if (act && det == 0.0) set_err(err, ERR_JACOBIAN);
     const double wJ = (act && det != 0.0) ? fabs(det) * hw[qq] : 0.0;
     // Grad_u in reference coordinates, Gr(a,m) = sum_j u_ja dphi_j/dxi_m, then
@@ -233,7 +241,7 @@ __global__ void __launch_bounds__(kGpWarps * 32) gauss_potential_kernel(
         const double dW1 = sc * (j1 - 3.0), dW2 = sc * (r * r);
         de = dW1 * f1e + dW2 * f2e;
         dnq = dW1 * f1n + dW2 * f2n;
-        if (mode == 2) {
+        if constexpr (SHAPE) {
           // P = sc F S(E), S the law's second Piola-Kirchhoff stress
           const double dd = D1 - D1 / sqrt(fabs(i3));
           double Sm[9];
@@ -279,7 +287,7 @@ __global__ void __launch_bounds__(kGpWarps * 32) gauss_potential_kernel(
               v += Dk * Gu[a][k];
               gg += Gu[a][k] * Gu[a][k];
               if constexpr (QD > 1) gt += Gu[k < QD ? k : 0][a] * Gu[a][k];
-              P[a][k] += 2.0 * Dk;
+              if constexpr (SHAPE) P[a][k] += 2.0 * Dk;
             }
           psi += v;
           double fe, fn;
@@ -326,23 +334,25 @@ __global__ void __launch_bounds__(kGpWarps * 32) gauss_potential_kernel(
       }
     }
     if (!act) psi = de = dnq = 0.0;
-    if (mode == 0) {
-      acc += psi * wJ;
-    } else if (mode == 1) {
-      acc += de * wJ;
-      dn[lane] = dnq * wJ;
-      __syncwarp();
-      const int nlast = nq - q0 < 32 ? nq - q0 : 32;
+    if constexpr (!SHAPE) {
+      if (mode == 0) {
+        acc += psi * wJ;
+      } else if (mode == 1) {
+        acc += de * wJ;
+        dn[lane] = dnq * wJ;
+        __syncwarp();
+        const int nlast = nq - q0 < 32 ? nq - q0 : 32;
 #pragma unroll
-      for (int r = 0; r < (NB + 31) / 32; ++r) {
-        const int j = lane + 32 * r;
-        if (j < NB) {
-          double s = 0.0;
-          for (int l = 0; l < nlast; ++l) s += dn[l] * hval[(q0 + l) * NB + j];
-          accn[r] += s;
+        for (int r = 0; r < (NB + 31) / 32; ++r) {
+          const int j = lane + 32 * r;
+          if (j < NB) {
+            double s = 0.0;
+            for (int l = 0; l < nlast; ++l) s += dn[l] * hval[(q0 + l) * NB + j];
+            accn[r] += s;
+          }
         }
+        __syncwarp();
       }
-      __syncwarp();
     } else {
       // H(d,k) = psi d_dk - sum_a P(a,k) Grad_u(a,d); dE/dx_v[d] += wJ H(d,:).G_v
       double H[DIM][DIM];
@@ -376,7 +386,7 @@ __global__ void __launch_bounds__(kGpWarps * 32) gauss_potential_kernel(
       }
     }
   }
-  if (mode == 0 || mode == 1) {
+  if constexpr (!SHAPE) {
     const double tot = warp_sum(acc);
     if (lane == 0) {
       if (!isfinite(tot) && mode == 1) set_err(err, ERR_NAN);
@@ -433,10 +443,12 @@ template <int DIM, int QD, int NB, int NBG, int LAW>
 cudaError_t launch_gp(Plan &P, int mode, int wslot, const SlotPtrs &sp, double *oe, double *on,
                       double *ox) {
   const unsigned blocks = unsigned((P.n_elements + kGpWarps - 1) / kGpWarps);
-  gauss_potential_kernel<DIM, QD, NB, NBG, LAW><<<blocks, kGpWarps * 32, 0, P.stream>>>(
-      P.n_elements, P.nq, mode, wslot, P.d_points, P.d_cv, P.d_enode, P.d_hval, P.d_hvalT,
-      P.d_hgradT,
-      P.d_ggrad, P.d_hw, P.form, sp, oe, on, ox, P.d_err);
+  const int cj = P.kind == SIMPLEX || P.parallelepiped;
+  auto kern = mode == 2 ? gauss_potential_kernel<DIM, QD, NB, NBG, LAW, true>
+                        : gauss_potential_kernel<DIM, QD, NB, NBG, LAW, false>;
+  kern<<<blocks, kGpWarps * 32, 0, P.stream>>>(
+      P.n_elements, P.nq, mode, wslot, cj, P.d_points, P.d_cv, P.d_enode, P.d_hval, P.d_hvalT,
+      P.d_hgradT, P.d_ggrad, P.d_hw, P.form, sp, oe, on, ox, P.d_err);
   return cudaGetLastError();
 }
 

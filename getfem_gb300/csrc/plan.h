@@ -120,6 +120,11 @@ struct Plan {
   double *d_hvalT = nullptr, *d_hgradT = nullptr;
   std::vector<int32_t> h_tri;  // upper-triangle entries of K_e (Gauss kernel)
   int32_t *d_tri = nullptr;
+  // every element a parallelepiped (hexahedra; checked again by
+  // gfgpu_set_points): the Jacobian is constant, and the affine_hex kernels
+  // apply
+  bool parallelepiped = false;
+  std::vector<int64_t> h_cvpts;  // E x 8 vertex ids of the hexahedra, for that check
   // parallelepiped hexahedra: reference tensors (7 x nb x nb)
   bool affine_hex = false;
   std::vector<double> h_aff;

@@ -305,7 +305,10 @@ int gfgpu_potential_gradient(gfgpu_plan *plan, int32_t slot, double *grad, int64
 
 /* Replaces the mesh vertex coordinates (n = n_points * dim doubles, device
    memory if on_device); the DOF map and the CSR pattern are kept.  Waits for
-   the copy. */
+   the copy.  Hexahedra are checked again for parallelepipeds: a plan whose
+   order-1/2 kernel needs them (scalar isotropic forms on parallelepipeds)
+   then returns GFGPU_E_UNSUPPORTED from those assemblies until the points
+   form parallelepipeds again; potentials (order 0) stay available. */
 int gfgpu_set_points(gfgpu_plan *plan, const double *points, int64_t n, int32_t on_device);
 
 /* Dirichlet conditions by elimination on the plan's assembled K (after an

@@ -161,3 +161,55 @@ def test_nodal_coefficient_gradient_is_exact():
     grp = ws.groups[0]
     Eo = oracle_problem(mesh, mf, mim, grp.order0, slots_of(ws)).potential(2)
     assert abs(float(E) - Eo) <= RTOL * abs(Eo)
+
+
+def test_points_moved_off_parallelepipeds():
+    """kappa*Grad_u.Grad_u on Q2 hexahedra of a parallelepiped mesh: the
+    order-1/2 plan takes the parallelepiped kernel and the potential forms the
+    Jacobian once per element.  Moving an interior vertex (gfgpu_set_points)
+    keeps the potential exact (the Jacobian is formed per Gauss point again)
+    and makes orders 1 and 2 fail loudly; the original points restore them."""
+    import ctypes as C
+
+    from getfem_gb300 import _lib as L
+    from oracle import gfref
+    torch = _torch()
+    rng = np.random.default_rng(12)
+    mesh = g.Mesh.regular_unit(3, 2, "hex")
+    mf = g.MeshFem(mesh, 1, degree=2)
+    mim = g.MeshIm(mesh, "IM_GAUSS_PARALLELEPIPED(3,5)")
+    u0 = rng.standard_normal(mf.nb_dof())
+    k0 = np.exp(rng.normal(0, 0.5, mesh.nb_convex()))
+    ws = g.GaWorkspace()
+    ws.add_fem_variable("u", mf, U=u0)
+    ws.add_fem_constant("kappa", g.MeshFem(mesh, 1, degree=0), k0)
+    ws.add_expression("kappa*Grad_u.Grad_u", mim)
+    pot = g.Potential(ws)
+    dev = torch.device("cuda")
+    u = torch.tensor(u0, device=dev)
+    kappa = torch.tensor(k0, device=dev)
+    X0 = torch.tensor(mesh.points.ravel(), device=dev)
+    grp = ws.groups[0]
+
+    def e_oracle(pts):
+        return gfref.Problem(3, mesh.kind, 2, 1, mim.im, pts.reshape(mesh.points.shape),
+                             mesh.cvpts, mf.dofs, mf.nb_dof(), grp.order0,
+                             slots_of(ws)).potential(4)
+    E0 = float(pot(u, points=X0, kappa=kappa))
+    e0 = e_oracle(mesh.points.ravel())
+    assert abs(E0 - e0) <= RTOL * abs(e0), (E0, e0)
+    X1 = X0.clone()
+    centre = int(np.argmin(np.abs(mesh.points - 0.5).sum(axis=1)))
+    X1[3 * centre] += 0.05
+    E1 = float(pot(u, points=X1, kappa=kappa))
+    e1 = e_oracle(X1.cpu().numpy())
+    assert abs(E1 - e1) <= RTOL * abs(e1), (E1, e1)
+    assert abs(e1 - e0) > 1e-6 * abs(e0)
+    lib = L.lib()
+    h1 = pot.h1
+    L.check(lib.gfgpu_set_points(h1, C.c_void_p(X1.data_ptr()), X1.numel(), 1))
+    assert lib.gfgpu_assemble(h1, 1, 0, None) == L.E_UNSUPPORTED
+    assert b"parallelepipeds" in lib.gfgpu_last_error()
+    pot._bind(h1, u, X0, ["kappa"], [kappa])
+    L.check(lib.gfgpu_assemble(h1, 1, 0, None))
+    L.check(lib.gfgpu_sync(h1))
