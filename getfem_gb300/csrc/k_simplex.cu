@@ -72,21 +72,25 @@ __host__ __device__ constexpr int pk_sup_v(int dim, int nb, int i, int t) {
   }
 }
 
-// Shared memory of one 32-element tile of the simplex element pass.
-template <int DIM, int QD, int NB>
+// Shared memory of one 32-element tile of the simplex element pass (KU:
+// with the staging of u and of the warps' parts of K_e u_e, which a pass
+// leaving K u to the row gather does not reserve).
+template <int DIM, int QD, int NB, bool KU = true>
 struct EpShared {
   static constexpr int NV = DIM + 1, M = QD * NV, NTP = M * (M + 1) / 2;
   static constexpr int S = NB * QD;
-  static constexpr int NG = NV * DIM + 8;  // g, J c0, J c1, J c2, J cmass, J, flag
+  // rows: g (NV x DIM), J c1 g_v.g_w (v <= w), then J c0, J c1, J c2, J cmass, J
+  static constexpr int KC = NV * DIM, KX = KC + NV * (NV + 1) / 2;
+  static constexpr int NG = KX + 8;
   double s_gval[NB * NB * kMaxPairTerms];
   double s_mass[NB * NB];
   double Gs[NG][32];     // geometry of the tile's 32 elements
   union {
     struct {
-      double Tp[NTP][32];  // upper triangle of T per element
-      double Us[S][32];    // u at the element's DOFs
-    } a;                   // while the blocks of K_e are built
-    double Rs[kEpWarps][S][32];  // then: each warp's part of R_e
+      double Tp[NTP][32];         // upper triangle of T per element
+      double Us[KU ? S : 1][32];  // u at the element's DOFs
+    } a;                          // while the blocks of K_e are built
+    double Rs[KU ? kEpWarps : 1][KU ? S : 1][32];  // then: each warp's part of R_e
   } x;
   unsigned long long mxs[kEpWarps][32];
 };
@@ -97,12 +101,12 @@ struct EpShared {
 // assembly forms K u from the assembled rows in the row gather)
 template <int DIM, int QD, int NB, bool MASS, bool STORE_K, bool KU = true>
 __device__ __forceinline__ void simplex_element_tile(
-    EpShared<DIM, QD, NB> &sh, int64_t tile, int64_t E, const double *__restrict__ pts,
+    EpShared<DIM, QD, NB, KU> &sh, int64_t tile, int64_t E, const double *__restrict__ pts,
     const int32_t *__restrict__ cv, const int32_t *__restrict__ enode,
     const SimplexTables *__restrict__ tab, const KeLayout &L, const gfgpu_form &form,
     const SlotPtrs &slots, const double *__restrict__ fsrc, double fscale,
     const double *__restrict__ u, double *__restrict__ out, int *__restrict__ err) {
-  using SH = EpShared<DIM, QD, NB>;
+  using SH = EpShared<DIM, QD, NB, KU>;
   constexpr int NV = SH::NV, M = SH::M;
   constexpr int S = SH::S, RS = (S + 3) & ~3;
   auto &s_gval = sh.s_gval;
@@ -191,40 +195,56 @@ __device__ __forceinline__ void simplex_element_tile(
     for (int v = 0; v < NV; ++v)
 #pragma unroll
       for (int d = 0; d < DIM; ++d) Gs[v * DIM + d][lane] = bad ? 0.0 : g[v][d];
-    Gs[NV * DIM + 0][lane] = J * c0;
-    Gs[NV * DIM + 1][lane] = J * c1;
-    Gs[NV * DIM + 2][lane] = J * c2;
-    Gs[NV * DIM + 3][lane] = J * cmass;
-    Gs[NV * DIM + 4][lane] = J;
+    // J c1 g_v.g_w, shared by the QD diagonal blocks of T
+    int kvw = SH::KC;
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+#pragma unroll
+      for (int w = v; w < NV; ++w, ++kvw) {
+        double gg = 0;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) gg += g[v][d] * g[w][d];
+        Gs[kvw][lane] = bad ? 0.0 : (J * c1) * gg;
+      }
+    Gs[SH::KX + 0][lane] = J * c0;
+    Gs[SH::KX + 1][lane] = J * c1;
+    Gs[SH::KX + 2][lane] = J * c2;
+    Gs[SH::KX + 3][lane] = J * cmass;
+    Gs[SH::KX + 4][lane] = J;
   }
   __syncthreads();
-  // ---- all warps: T[(a,v),(b,w)] = J (c0 g_va g_wb + c1 d_ab g_v.g_w + c2 g_vb g_wa)
+  // ---- all warps: T[(a,v),(b,w)] = J (c0 g_va g_wb + c1 d_ab g_v.g_w + c2 g_vb g_wa),
+  // row p = (a,v) by one warp (rows dealt in snake order, which balances the
+  // rows' lengths M - p): J c0 g_va and J c2 g_vb are formed once per row,
+  // so an entry costs one multiply and one FMA (plus the c1 term on the
+  // diagonal blocks)
   {
-    const double Jc0 = Gs[NV * DIM + 0][lane], Jc1 = Gs[NV * DIM + 1][lane];
-    const double Jc2 = Gs[NV * DIM + 2][lane];
-    int k = 0;
+    const double Jc0 = Gs[SH::KX + 0][lane], Jc2 = Gs[SH::KX + 2][lane];
 #pragma unroll
-    for (int p = 0; p < M; ++p)
+    for (int p = 0; p < M; ++p) {
+      const int pos = p % kEpWarps;
+      if (((p / kEpWarps) & 1 ? kEpWarps - 1 - pos : pos) != wid) continue;  // warp-uniform
+      const int a = p / NV, v = p % NV;
+      double s0 = 0.0, ub[QD];
+      if constexpr (QD > 1) {
+        s0 = Jc0 * Gs[v * DIM + a][lane];
+#pragma unroll
+        for (int b = 0; b < QD; ++b) ub[b] = Jc2 * Gs[v * DIM + b][lane];
+      }
+      int k = p * M - (p * (p - 1)) / 2;
 #pragma unroll
       for (int q = p; q < M; ++q, ++k) {
-        if (k % kEpWarps != wid) continue;  // warp-uniform
-        const int a = p / NV, v = p % NV, b = q / NV, w = q % NV;
+        const int b = q / NV, w = q % NV;
         double val = 0.0;
-        if (a == b) {
-          double gg = 0;
-#pragma unroll
-          for (int d = 0; d < DIM; ++d) gg += Gs[v * DIM + d][lane] * Gs[w * DIM + d][lane];
-          val = Jc1 * gg;
-        }
-        if (QD > 1)
-          val += Jc0 * Gs[v * DIM + a][lane] * Gs[w * DIM + b][lane] +
-                 Jc2 * Gs[v * DIM + b][lane] * Gs[w * DIM + a][lane];
+        if constexpr (QD > 1) val = fma(ub[b], Gs[w * DIM + a][lane], s0 * Gs[w * DIM + b][lane]);
+        if (a == b) val += Gs[SH::KC + v * NV - (v * (v - 1)) / 2 + (w - v)][lane];
         Tp[k][lane] = val;
       }
+    }
   }
   __syncthreads();
   // ---- u at the element's DOFs
-  if (KU) {
+  if constexpr (KU) {
     for (int j = wid; j < NB; j += kEpWarps) {
       const int nd = active ? __ldg(enode + e * NB + j) : 0;
 #pragma unroll
@@ -233,7 +253,7 @@ __device__ __forceinline__ void simplex_element_tile(
     }
   }
   __syncthreads();
-  const double cm = Gs[NV * DIM + 3][lane], jf = Gs[NV * DIM + 4][lane] * fscale;
+  const double cm = Gs[SH::KX + 3][lane], jf = Gs[SH::KX + 4][lane] * fscale;
   double *o = out + e * L.stride;
   unsigned long long mx = 0ull;  // abs_key of the largest |entry|
   // load term of row r = (i,a): scale |J| sum_j M[i,j] f[(j,a)]
@@ -283,7 +303,7 @@ __device__ __forceinline__ void simplex_element_tile(
       double rv = load_of(i, 0);
 #pragma unroll
       for (int c = 0; c < S; ++c) {
-        if (KU) rv += row[c] * Us[c][lane];
+        if constexpr (KU) rv += row[c] * Us[c][lane];
         const unsigned long long kv = abs_key(row[c]);
         mx = kv > mx ? kv : mx;
       }
@@ -342,7 +362,7 @@ __device__ __forceinline__ void simplex_element_tile(
         for (int a = 0; a < QD; ++a)
 #pragma unroll
           for (int b = 0; b < QD; ++b) {
-            if (KU) {
+            if constexpr (KU) {
               Rp[i * QD + a] += B[a][b] * Us[j * QD + b][lane];
               if (i != j) Rp[j * QD + b] += B[a][b] * Us[i * QD + a][lane];
             }
@@ -370,14 +390,14 @@ __device__ __forceinline__ void simplex_element_tile(
     }
     mxs[wid][lane] = mx;
     __syncthreads();  // every warp is done with T and u
-    if (KU) {
+    if constexpr (KU) {
 #pragma unroll
       for (int c = 0; c < S; ++c) Rs[wid][c][lane] = Rp[c];
       __syncthreads();
     }
     for (int r = wid; r < S; r += kEpWarps) {
       double rv = load_of(r / QD, r % QD);
-      if (KU) {
+      if constexpr (KU) {
 #pragma unroll
         for (int k = 0; k < kEpWarps; ++k) rv += Rs[k][r][lane];
       }
@@ -405,7 +425,7 @@ __global__ void __launch_bounds__(kEpThreads) simplex_element_pass(
     gfgpu_form form, SlotPtrs slots, const double *__restrict__ fsrc, double fscale,
     const double *__restrict__ u, double *__restrict__ out, int *__restrict__ err,
     int64_t tile0) {
-  __shared__ EpShared<DIM, QD, NB> sh;
+  __shared__ EpShared<DIM, QD, NB, KU> sh;
   simplex_element_tile<DIM, QD, NB, MASS, STORE_K, KU>(sh, tile0 + blockIdx.x, E, pts, cv, enode,
                                                    tab, L, form, slots, fsrc, fscale, u, out, err);
 }
@@ -553,7 +573,7 @@ __global__ void __launch_bounds__(kEpThreads) batch_element_pass(
     const BatchItem *__restrict__ items, const int64_t *__restrict__ tile0, int nitems,
     int64_t ntiles) {
   using B = BatchType<T>;
-  __shared__ EpShared<B::DIM, B::QD, B::NB> sh;
+  __shared__ EpShared<B::DIM, B::QD, B::NB, false> sh;
   for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
     int lo = 0, hi = nitems - 1;
     while (lo < hi) {
