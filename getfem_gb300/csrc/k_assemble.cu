@@ -31,6 +31,7 @@
 //    with its own shared-memory footprint.
 #include <atomic>
 #include <cub/cub.cuh>
+#include <type_traits>
 
 #include "k_common.cuh"
 #include "plan.h"
@@ -302,24 +303,35 @@ __device__ __forceinline__ void gather_node(
     if (want_K) {
       const double *Kb = Kbuf + (k % kGatherBufs) * blk;
       const unsigned long long tb = abs_key(thr0);
+      // the node's first element stores into the zeroed accumulators (an
+      // element touches each accumulator once): no FP64 add for it
+      auto add_block = [&](auto first) {
 #pragma unroll
-      for (int r = 0; r < R; ++r) {
-        const int c = lane + 32 * r;
-        if (c < S) {
-          const int b = c % QD;
-          const unsigned sb = sl0[r] >= 0 ? bits[sl0[r]] : 0u;
-          const int c0 = L.blk ? (c / QD) * L.blk + b : c;
-          const int cstep = L.blk ? QD : L.rowstride;
+        for (int r = 0; r < R; ++r) {
+          const int c = lane + 32 * r;
+          if (c < S) {
+            const int b = c % QD;
+            const unsigned sb = sl0[r] >= 0 ? bits[sl0[r]] : 0u;
+            const int c0 = L.blk ? (c / QD) * L.blk + b : c;
+            const int cstep = L.blk ? QD : L.rowstride;
 #pragma unroll
-          for (int a = 0; a < QD; ++a) {
-            const double x = Kb[c0 + a * cstep];
-            if (abs_greater(x, tb)) {
-              if ((sb >> (a * QD + b)) & 1u) acc[(sl0[r] * QD + a) * QD + b] += x;
-              else miss = true;
+            for (int a = 0; a < QD; ++a) {
+              const double x = Kb[c0 + a * cstep];
+              if (abs_greater(x, tb)) {
+                if ((sb >> (a * QD + b)) & 1u) {
+                  double &dst = acc[(sl0[r] * QD + a) * QD + b];
+                  if constexpr (decltype(first)::value) dst = x;
+                  else dst += x;
+                } else {
+                  miss = true;
+                }
+              }
             }
           }
         }
-      }
+      };
+      if (k == 0) add_block(std::true_type{});
+      else add_block(std::false_type{});
     }
     __syncwarp();
 #pragma unroll
