@@ -609,15 +609,19 @@ def main():
     L.check(lib.gfgpu_fp64_peak(0, C.byref(fp64_peak)))
     # FP64 flops the element pass executes per element (from its loop
     # structure): the node-pair blocks i <= j of the symmetric K_e (2 per
-    # reference-tensor term per component pair), the load term, T and the
-    # geometry (K u is formed by the row gather from the assembled rows)
+    # reference-tensor term per component pair), the load term, T (a multiply
+    # and an FMA per upper entry, the c1 term on the diagonal blocks, 4
+    # multiplies per row, |J| c1 g_v.g_w per vertex pair) and the geometry
+    # (K u is formed by the row gather from the assembled rows)
     from getfem_gb300.tables import simplex_term_count, simplex_upper_term_count
     _, nb = simplex_term_count(3, 2)
     nterm_upper = simplex_upper_term_count(3, 2)
-    qd, M = 3, 3 * 4
+    qd, nv = 3, 4
+    M = qd * nv
     s_ = nb * qd
     ep_flops = (2.0 * nterm_upper * qd * qd + 2.0 * s_ * nb
-                + 6.0 * M * (M + 1) / 2 + 150.0)
+                + 3.0 * M * (M + 1) / 2 + qd * nv * (nv + 1) / 2 + 4.0 * M
+                + 6.0 * nv * (nv + 1) / 2 + 90.0)
     ep_tflops = E * ep_flops / (kt[0] * 1e-3) / 1e12
     # DRAM bytes per launch of the dominant kernel: from one ncu capture of
     # the same kernel on the 20^3 x 6 mesh, scaled by the element count
