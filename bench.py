@@ -41,19 +41,32 @@ EXPR = "(lambda*Div_u*Id(3)+2*mu*Sym(Grad_u)):Grad_Test_u - f.Test_u"
 METRIC = "elements/s assembled (K + residual), P2 tet elasticity"
 
 
-def make_problem(nx: int, seed: int = 2026):
-    import getfem_gb300 as g
+def p2tet_inputs(nx: int, seed: int = 2026):
+    """Seeded inputs of the P2-tet elasticity workload, made with numpy only
+    (the reference arm uses them without the package): interior-vertex
+    jitter U[-0.1h, 0.1h] in lattice order (x fastest), u N(0,1)*1e-3, the
+    per-element Lame scalings lambda, mu lognormal(0, 0.2) and the nodal load
+    f N(0,1).  Sizes of regular_unit_mesh(nx^3) split into 6 tetrahedra
+    with FEM_PK(3,2), qdim 3: E = 6 nx^3 elements, 3 (2 nx + 1)^3 DOFs."""
     rng = np.random.default_rng(seed)
     h = 1.0 / nx
+    E = 6 * nx ** 3
+    ndof = 3 * (2 * nx + 1) ** 3
     jit = rng.uniform(-0.1 * h, 0.1 * h, ((nx + 1) ** 3, 3))
+    data = dict(u=rng.standard_normal(ndof) * 1e-3,
+                lam=np.exp(rng.normal(0.0, 0.2, E)), mu=np.exp(rng.normal(0.0, 0.2, E)),
+                f=rng.standard_normal(ndof))
+    return jit, data
+
+
+def make_problem(nx: int, seed: int = 2026):
+    import getfem_gb300 as g
+    jit, data = p2tet_inputs(nx, seed)
     mesh = g.Mesh.regular_unit(3, nx, "simplex", jitter=jit)
     mf = g.MeshFem(mesh, 3, degree=2)
     mf0 = g.MeshFem(mesh, 1, degree=0)
     mim = g.MeshIm(mesh, "IM_TETRAHEDRON(5)")
-    E = mesh.nb_convex()
-    data = dict(u=rng.standard_normal(mf.nb_dof()) * 1e-3,
-                lam=np.exp(rng.normal(0.0, 0.2, E)), mu=np.exp(rng.normal(0.0, 0.2, E)),
-                f=rng.standard_normal(mf.nb_dof()))
+    assert mf.nb_dof() == data["u"].size and mesh.nb_convex() == data["lam"].size
     ws = g.GaWorkspace()
     ws.add_fem_variable("u", mf, U=data["u"])
     ws.add_fem_constant("lambda", mf0, data["lam"])
@@ -61,6 +74,39 @@ def make_problem(nx: int, seed: int = 2026):
     ws.add_fem_constant("f", mf, data["f"])
     ws.add_expression(EXPR, mim)
     return mesh, mf, mim, ws, data
+
+
+REF_DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
+
+
+def time_reference_model(nx, threads, warmup, steps, seed=2026):
+    """The reference itself (GetFEM built from its sources by
+    oracle/refbuild, with OpenMP): model::assembly(BUILD_ALL) of the
+    P2-tet elasticity workload (K and the right-hand side; one ga_workspace
+    per thread over its partition of the mesh, src/getfem_models.cc:2646-2730)
+    on the same seeded inputs, `warmup` untimed then `steps` timed calls with
+    steady_clock.  Returns (step seconds list, info dict) or None when the
+    reference build is absent."""
+    import tempfile
+    if not os.access(REF_DRIVER, os.X_OK):
+        return None
+    jit, data = p2tet_inputs(nx, seed)
+    with tempfile.TemporaryDirectory() as td:
+        ind, outd = os.path.join(td, "in"), os.path.join(td, "out")
+        os.makedirs(ind)
+        os.makedirs(outd)
+        jit.astype(np.float64).tofile(os.path.join(ind, "jitter.bin"))
+        for k, name in (("u", "u"), ("lam", "lambda"), ("mu", "mu"), ("f", "f")):
+            data[k].astype(np.float64).tofile(os.path.join(ind, name + ".bin"))
+        cmd = [REF_DRIVER, "dim=3", f"nx={nx}", "gt=PK", "fem=2", "qdim=3",
+               "im=IM_TETRAHEDRON(5)", f"in={ind}", f"out={outd}", f"expr={EXPR}", "jitter=1",
+               "consts=lambda:P0,mu:P0,f:V", "time=model", f"threads={threads}",
+               f"warmup={warmup}", f"steps={steps}", "dump=0"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("reference driver failed: " + (r.stderr or r.stdout)[-400:])
+        info = json.load(open(os.path.join(outd, "info.json")))
+    return info["t_steps"], info
 
 
 class ClockSampler:
@@ -144,33 +190,49 @@ def cpu_time_oracle(nx, nthreads, reps=1):
     return min(ts), mesh.nb_convex()
 
 
+def workload_config(nx, E, ndof, nnz):
+    return {"workload": f"3-D P2 tet linear elasticity, regular_unit_mesh {nx}^3 x 6 tets, "
+                        "IM_TETRAHEDRON(5), K + R value re-assembly, pattern cached",
+            "elements": E, "n_dof": ndof, "nnz": nnz}
+
+
 def run_reference(args, rank, world):
+    """The reference arm: GetFEM's own multi-threaded model::assembly of the
+    same workload (same mesh, seeds and expression) on all host cores."""
     if rank != 0:
         return
-    from oracle import gfref
-    gfref.build()
     nthreads = os.cpu_count() or 1
-    nx = args.ref_nx
-    _, E = cpu_time_oracle(nx, nthreads)  # warm-up (also builds tables)
-    for _ in range(max(args.warmup - 1, 0)):
-        cpu_time_oracle(nx, nthreads)
-    total_t, total_e = 0.0, 0
-    for _ in range(args.steps):
-        t, E = cpu_time_oracle(nx, nthreads)
-        total_t += t
-        total_e += E
-    v = total_e / total_t
-    sample = f"regular_unit_mesh 3-D P2 tet elasticity, nx={nx} ({E} elements) per step, K + R"
+    nx = args.nx
+    E, ndof = 6 * nx ** 3, 3 * (2 * nx + 1) ** 3
+    try:
+        res = time_reference_model(nx, nthreads, args.warmup, args.steps)
+    except RuntimeError as exc:
+        res = None
+        why = str(exc).splitlines()[-1] if str(exc) else "reference driver failed"
+    else:
+        why = "the reference build (oracle/_ref/ref_driver) is absent on this host"
+    if res is None:
+        print(json.dumps({"impl": "reference", "unavailable": why}), flush=True)
+        return
+    times, info = res
+    mean_s = float(np.mean(times))
+    v = E / mean_s
+    sample = (f"GetFEM built from its sources with OpenMP, model::assembly(BUILD_ALL) "
+              f"(K + right-hand side) of the full workload, {nthreads} threads, "
+              f"nx={nx} ({E} elements) per step")
+    cfg = workload_config(nx, E, ndof, int(info["nnz"]))
+    cfg["l2"] = "host memory (CPU run)"
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "elements/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * total_t / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-            "config": {"workload": "P2 tet elasticity sub-mesh (CPU sample)", "nx": nx,
-                       "elements_per_step": E},
-            "cpu_baseline": {"value": v, "unit": "elements/s", "cores": nthreads, "kind": "port",
-                             "sample": sample},
+            "ms_per_step": 1e3 * mean_s, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded jittered mesh, lognormal coefficients, N(0,1) load)",
+            "config": cfg,
+            "cpu_baseline": {"value": v, "unit": "elements/s", "cores": nthreads,
+                             "kind": "reference", "sample": sample},
             "e2e": {"value": v, "unit": "elements/s", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 0}}
+                    "d2h_bytes_per_step": 0},
+            "reference_steps_s": times}
     print(json.dumps(line), flush=True)
 
 
@@ -560,6 +622,20 @@ def main():
     L.check(lib.gfgpu_sync(h))
     ms = e0.elapsed_time(e1) / args.steps
 
+    # a longer run of the same step (about a second) with its own clock
+    # record, for the steadiness of the figure above
+    steady_steps = max(args.steps, 300)
+    steady = ClockSampler(local)
+    with steady:
+        barrier()
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record()
+        for _ in range(steady_steps):
+            L.check(lib.gfgpu_assemble(h, 2, flags, None))
+        s1.record()
+        barrier()
+    steady_ms = s0.elapsed_time(s1) / steady_steps
+
     # per-kernel durations (CUDA events on the plan's stream)
     kt = np.zeros(2)
     nprof = min(args.steps, 20)
@@ -598,6 +674,8 @@ def main():
     except (OSError, ValueError):
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_source = ("MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks
+                   else "6800 GB/s (of fallback: MEASURED_PEAKS.json absent)")
     ab = algorithmic_bytes(mesh, mf, nnz)
     step_bytes = sum(ab.values())
     # the dominant kernel of the step and its achieved rate on the step's
@@ -605,8 +683,9 @@ def main():
     names = ["element_pass", "row_gather"]
     dom = int(np.argmax(kt))
     dom_gbs = step_bytes / (kt[dom] * 1e-3) / 1e9
-    fp64_peak = C.c_double()
+    fp64_peak, dmma_peak = C.c_double(), C.c_double()
     L.check(lib.gfgpu_fp64_peak(0, C.byref(fp64_peak)))
+    L.check(lib.gfgpu_fp64_peak(1, C.byref(dmma_peak)))
     # FP64 flops the element pass executes per element (from its loop
     # structure): the node-pair blocks i <= j of the symmetric K_e (2 per
     # reference-tensor term per component pair), the load term, T (a multiply
@@ -635,30 +714,46 @@ def main():
     cpu = None
     if not args.no_cpu:
         nthreads = os.cpu_count() or 1
-        t, Es = cpu_time_oracle(args.cpu_nx, nthreads, reps=2)
-        cpu = {"value": Es / t, "unit": "elements/s", "cores": nthreads, "kind": "port",
-               "sample": f"oracle (CPU restatement of the reference exec loop), OpenMP "
-                         f"{nthreads} threads, K + R of the same problem at nx={args.cpu_nx} "
-                         f"({Es} elements), best of 2"}
+        res = None
+        try:
+            res = time_reference_model(args.nx, nthreads, 1, 3)
+        except RuntimeError as exc:
+            print(f"reference CPU baseline failed ({exc}); timing the oracle port", file=sys.stderr)
+        if res is not None:
+            tr = float(np.mean(res[0]))
+            cpu = {"value": E / tr, "unit": "elements/s", "cores": nthreads, "kind": "reference",
+                   "sample": f"GetFEM built from its sources with OpenMP, "
+                             f"model::assembly(BUILD_ALL) of the full workload ({E} elements), "
+                             f"{nthreads} threads, mean of 3 after 1 warm-up"}
+        else:
+            t, Es = cpu_time_oracle(args.cpu_nx, nthreads, reps=2)
+            cpu = {"value": Es / t, "unit": "elements/s", "cores": nthreads, "kind": "port",
+                   "sample": f"oracle (CPU restatement of the reference exec loop), OpenMP "
+                             f"{nthreads} threads, K + R of the same problem at nx={args.cpu_nx} "
+                             f"({Es} elements), best of 2"}
     line = {
         "metric": METRIC, "value": value, "unit": "elements/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded jittered mesh, lognormal coefficients, N(0,1) load)",
-        "config": {"workload": f"3-D P2 tet linear elasticity, regular_unit_mesh {args.nx}^3 x 6 tets, "
-                               "IM_TETRAHEDRON(5), K + R value re-assembly, pattern cached",
-                   "elements": E, "n_dof": mf.nb_dof(), "nnz": nnz,
-                   "l2": "inputs larger than L2 (K values, scratch and DOF data >> 129 MB)",
-                   "dofs_per_s": value * mf.nb_dof() / E},
+        "config": dict(workload_config(args.nx, E, mf.nb_dof(), nnz),
+                       l2="inputs larger than L2 (K values, scratch and DOF data >> 129 MB)",
+                       dofs_per_s=value * mf.nb_dof() / E),
         "kernels_ms": {"element_pass": float(kt[0]), "row_gather": float(kt[1])},
         "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": dom_gbs,
                      "peak": hbm_peak, "unit": "GB/s", "frac": dom_gbs / hbm_peak,
                      "traffic": traffic, "algorithmic_bytes": step_bytes,
-                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
+                     "peak_source": peak_source,
+                     "limiter": "FP64 pipe and issue latency, not HBM: measured FP64 FMA "
+                                f"{fp64_peak.value:.2f} TFLOP/s is 0.19 flop per HBM byte; "
+                                "the fp64 object gives the element pass's FP64 fraction"},
         "fp64": {"kernel": "element_pass", "achieved_tflops": ep_tflops,
                  "peak_tflops": fp64_peak.value, "frac": ep_tflops / fp64_peak.value,
                  "flops_per_element": ep_flops,
-                 "peak_source": "gfgpu_fp64_peak FMA microbenchmark, this run"},
+                 "peak_source": "gfgpu_fp64_peak FMA microbenchmark, this run",
+                 "dmma_peak_tflops": dmma_peak.value},
+        "steady": {"steps": steady_steps, "ms_per_step": steady_ms,
+                   "elements_per_s": E / (steady_ms * 1e-3), "clocks": steady.summary()},
         "step_hbm_frac": step_bytes / (ms * 1e-3) / 1e9 / hbm_peak,
         "e2e": {"value": e2e, "unit": "elements/s", "h2d_bytes_per_step": 8 * mf.nb_dof(),
                 "d2h_bytes_per_step": 8 * nnz + 8 * mf.nb_dof(), "ms_per_step": e2e_ms},

@@ -73,6 +73,9 @@ void dfree(T *&p) {
   p = nullptr;
 }
 
+}  // namespace
+
+namespace gfgpu {
 // The forms the affine-simplex element pass lowers: GRADGRAD / MASS with
 // constant or per-element coefficients, SOURCE with a field on the
 // variable's mesh_fem and a constant factor.
@@ -120,7 +123,9 @@ bool simplex_form_supported(const gfgpu_form &f, int qdim, int dim, std::string 
   }
   return true;
 }
+}  // namespace gfgpu
 
+namespace {
 // The forms of the Gauss-point kernels: GRADGRAD / MASS / SOURCE terms
 // with constant, per-element or nodal coefficients and at most one internal
 // pressure term (LAW_ISO), or one compressible neo-Hookean term on a 3-D

@@ -249,6 +249,8 @@ cudaError_t launch_gather_range(Plan &P, bool want_K, bool want_R, int64_t n0, i
 int build_simplex_tables(Plan &P, std::string &err);
 int fill_simplex_tables(int dim, int degree, int qdim, const std::string &im, SimplexTables &t,
                         KeLayout &lay, int &nq, std::string &err);
+// whether the affine-simplex element pass lowers the form (why: the reason if not)
+bool simplex_form_supported(const gfgpu_form &f, int qdim, int dim, std::string &why);
 // potentials and adjoint gradients (k_gauss.cu)
 bool gauss_potential_available(int dim, int kind, int degree, int qdim, int law);
 int build_gauss_tables(Plan &P, std::string &err);

@@ -377,28 +377,40 @@ int gfgpu_fp64_peak(int32_t kind, double *tflops);
 
 /* Some callers cannot allocate device memory: code that works inside a
    memory budget owned by another allocator (a framework's caching
-   allocator, an arena sized at start-up) must not call cudaMalloc behind
-   that allocator's back, and cudaMalloc/cudaFree synchronise the device,
-   which a caller assembling in a tight loop cannot afford.  For them,
-   gfgpu_assemble_vector_noalloc assembles the vector (order 1) of an
-   affine-simplex form -- the same result as a plan's gfgpu_assemble(plan, 1)
-   -- from the caller's device arrays into the caller's device output, and
-   calls no cudaMalloc, cudaFree or other allocating routine.
+   allocator, an arena sized at start-up, a solver embedded in a host
+   program that hands it a fixed pool) must not call cudaMalloc behind that
+   allocator's back.  For them, gfgpu_assemble_vector_noalloc assembles the
+   vector (order 1) of an affine-simplex form -- the same result as a plan's
+   gfgpu_assemble(plan, 1) -- from the caller's device arrays into the
+   caller's device output, and calls no cudaMalloc, cudaFree or other
+   allocating routine.
 
    Its scratch (one vector of rowstride doubles per element, rowstride = the
    element's DOF count rounded up to 4) lives in a static device array of
    GFGPU_NOALLOC_SCRATCH_BYTES that every GPU which loads the library holds
-   until the process exits; larger meshes are rejected with GFGPU_E_INVALID
-   (about 560 000 P2 tetrahedra with 3 components, 1.4 million with one).
+   until the process exits.  The largest mesh is
+   GFGPU_NOALLOC_SCRATCH_BYTES / (8 * rowstride) elements: 524 288 P2
+   tetrahedra with 3 components (rowstride 32), 1 398 101 with one
+   (rowstride 12); larger meshes are rejected with GFGPU_E_INVALID.
 
    - The first call on a device looks up the device addresses of the static
-     arrays (cudaGetSymbolAddress, with that device current); make that first
-     call before any stream capture.
+     arrays (cudaGetSymbolAddress, with that device current) and keeps them
+     for the life of the process; make that first call before any stream
+     capture, and do not use the entry point across a cudaDeviceReset (the
+     kept addresses belong to the context that was reset).
    - Every call shares the arrays, which keep the last call's contents: each
      call writes every element's slot before reading it and overwrites the
      output, so nothing has to be cleared, but calls that overlap on the GPU
      race: issue them on one stream, one after another.
-   - The call waits for its stream before returning the status.
+   - Each call waits for its stream (cudaStreamSynchronize) to read the
+     device error word before returning the status, so it is not an
+     asynchronous call.
+   - Every pointer the kernels read is checked on the host first: null
+     arrays, per-element coefficient or load slots that are missing or out
+     of range, and forms of more than GFGPU_MAX_TERMS terms return
+     GFGPU_E_INVALID without a launch; an adjacency entry outside
+     [0, n_elements * nb) is skipped on the device and reported as
+     GFGPU_E_INVALID.
 
    Inputs (device memory): points (n_points x dim), cvpts (n_elements x
    (dim+1) vertex ids), enode (n_elements x nb: DOF node of each local node,

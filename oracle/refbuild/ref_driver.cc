@@ -27,11 +27,22 @@
 //       as the assembled vector, assembly(2, true) and writes the condensed K
 //       (K_*.bin), the vector Rc.bin and the internal coupling matrix
 //       (C_rowptr/C_colidx/C_vals.bin), workspace.cc:791-860)
+//   time=model threads=T warmup=W steps=S   (timing of the reference's
+//       multi-threaded assembly: u a variable of a getfem::model, the data
+//       initialized fem data, the expression a nonlinear term brick
+//       (getfem::add_nonlinear_term, re-assembled at every call), and
+//       model::assembly(BUILD_ALL) (K and the right-hand side,
+//       src/getfem_models.cc:2646-2730: one ga_workspace per OpenMP thread
+//       over that thread's partition of the region) run W + S times with T
+//       threads; writes the S step times, nnz(K) and the norms of K and of
+//       the right-hand side to info.json)
+//   dump=0   (skip the mesh / DOF map / reference-element dumps)
 // The variable is always "u" (file in/u.bin, zeros when absent).
 // Jitter: when jitter=1, in/jitter.bin holds (nx+1)^dim x dim doubles in
 // lattice order (x index fastest); interior vertices are moved by it.
 #include "getfem/getfem_generic_assembly.h"
 #include "getfem/getfem_models.h"
+#include "getfem/getfem_omp.h"
 #include "getfem/getfem_im_data.h"
 #include "getfem/getfem_regular_meshes.h"
 #include "getfem/getfem_mesh_fem.h"
@@ -42,6 +53,7 @@
 #include <fstream>
 #include <map>
 #include <algorithm>
+#include <cmath>
 
 using bgeot::size_type;
 using bgeot::scalar_type;
@@ -114,6 +126,11 @@ int main(int argc, char **argv) {
     size_t p = a.find('=');
     if (p != std::string::npos) args[a.substr(0, p)] = a.substr(p + 1);
   }
+  // the thread count is fixed before any GetFEM object exists: the
+  // per-thread storage of GetFEM's singletons is sized at creation
+  const int threads = std::stoi(arg("threads", "1"));
+  getfem::set_num_threads(threads);
+  if (arg("time", "") == "model") gmm::set_traces_level(0);
   int dim = std::stoi(arg("dim", "2"));
   size_type nx = std::stoul(arg("nx", "4"));
   std::string gt = arg("gt", "PK");
@@ -167,9 +184,10 @@ int main(int argc, char **argv) {
   size_type ndof = mf.nb_dof();
   size_type E = m.nb_convex();
 
+  const bool dump = arg("dump", "1") != "0";
   // reference-element tables: integration points, weights, and the FEM's
   // base values / reference gradients at those points
-  {
+  if (dump) {
     getfem::pintegration_method pim = getfem::int_method_descriptor(imname);
     const getfem::papprox_integration pai = pim->approx_method();
     std::vector<double> ipts, iw, bval, bgrad;
@@ -194,7 +212,7 @@ int main(int argc, char **argv) {
   }
 
   // mesh and DOF maps
-  {
+  if (dump) {
     std::vector<double> pts;
     for (size_type ip = 0; ip < m.points().size(); ++ip)
       for (int d = 0; d < dim; ++d) pts.push_back(m.points()[ip][d]);
@@ -214,6 +232,45 @@ int main(int argc, char **argv) {
   std::vector<double> U(ndof, 0.0);
   read_file(in + "/u.bin", U);
   if (U.size() != ndof) { fprintf(stderr, "u.bin has %zu values, need %zu\n", U.size(), size_t(ndof)); return 2; }
+
+  if (arg("time", "") == "model") {
+    getfem::model md;
+    md.add_fem_variable("u", mf);
+    gmm::copy(U, md.set_real_variable("u"));
+    for (const std::string &c : split(arg("consts", ""), ',')) {
+      std::vector<std::string> kv = split(c, ':');
+      std::vector<double> v;
+      if (!read_file(in + "/" + kv[0] + ".bin", v)) { fprintf(stderr, "missing %s\n", kv[0].c_str()); return 2; }
+      const std::string &k = kv[1];
+      if (k == "P0") md.add_initialized_fem_data(kv[0], mf0, v);
+      else if (k == "S") md.add_initialized_fem_data(kv[0], mfs, v);
+      else if (k == "V") md.add_initialized_fem_data(kv[0], mf, v);
+      else md.add_initialized_fixed_size_data(kv[0], v);
+    }
+    getfem::add_nonlinear_term(md, mim, expr);
+    const int warm = std::stoi(arg("warmup", "1")), steps = std::stoi(arg("steps", "3"));
+    std::vector<double> times;
+    for (int r = 0; r < warm + steps; ++r) {
+      auto t0 = std::chrono::steady_clock::now();
+      md.assembly(getfem::model::BUILD_ALL);
+      auto t1 = std::chrono::steady_clock::now();
+      if (r >= warm) times.push_back(std::chrono::duration<double>(t1 - t0).count());
+    }
+    const auto &K = md.real_tangent_matrix();
+    size_type nnz = 0;
+    double knorm = 0.0;
+    for (size_type j = 0; j < gmm::mat_ncols(K); ++j)
+      for (const auto &e : K.col(j)) { ++nnz; knorm += e.e * e.e; }
+    const auto &rhs = md.real_rhs();
+    FILE *info = fopen((out + "/info.json").c_str(), "w");
+    fprintf(info, "{\"n_dof\": %zu, \"n_elements\": %zu, \"threads\": %d, \"nnz\": %zu, "
+            "\"K_frobenius\": %.17g, \"rhs_norm\": %.17g, \"t_steps\": [",
+            size_t(ndof), size_t(E), threads, size_t(nnz), std::sqrt(knorm), gmm::vect_norm2(rhs));
+    for (size_t i = 0; i < times.size(); ++i) fprintf(info, "%s%.6e", i ? ", " : "", times[i]);
+    fprintf(info, "]}\n");
+    fclose(info);
+    return 0;
+  }
 
   const std::string internal = arg("internal", "");
   if (!internal.empty()) {

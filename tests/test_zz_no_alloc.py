@@ -1,6 +1,9 @@
 """The allocation-free vector assembly (gfgpu_assemble_vector_noalloc), for
-callers that must not allocate device memory themselves, against the plan
-entry point: same vector within the suite's tolerance, on two calls in a row.
+callers that must not allocate device memory themselves (their device memory
+belongs to another allocator or to a fixed arena), against the plan entry
+point and the oracle: same vector within the suite's tolerance, on two calls
+in a row.  The argument checks run on the CPU: a caller's mistake must come
+back as GFGPU_E_INVALID before anything is launched.
 
 Collected last so that a run stopping at the first failure has run every
 other test first; it also passes alone in a fresh process."""
@@ -13,9 +16,7 @@ import getfem_gb300 as g
 from getfem_gb300 import _lib as L
 from getfem_gb300 import gwfl
 
-from common import RTOL, vec_errors
-
-pytestmark = pytest.mark.gpu
+from common import RTOL, oracle_problem, slots_of, vec_errors
 
 
 def _problem(nx=5, seed=21):
@@ -46,6 +47,7 @@ def _adjacency(enode, n_nodes):
     return np.cumsum(ptr).astype(np.int32), order.astype(np.int32)
 
 
+@pytest.mark.gpu
 def test_noalloc_vector_matches_plan_vector_twice():
     torch = pytest.importorskip("torch")
     mesh, mf, mim, ws = _problem()
@@ -86,19 +88,87 @@ def test_noalloc_vector_matches_plan_vector_twice():
         torch.cuda.synchronize()
         L.check(lib.gfgpu_assemble_vector_noalloc(C.byref(args), C.byref(form), None))
         results.append(out.cpu().numpy().copy())
+    R_oracle = oracle_problem(mesh, mf, mim, ws.groups[0].order1, slots_of(ws)).vector(nthreads=1)
     for R in results:
         assert vec_errors(R, R_plan).max() <= RTOL
+        assert vec_errors(R, R_oracle).max() <= RTOL
     assert np.array_equal(results[0], results[1])
 
 
-def test_noalloc_rejects_meshes_beyond_its_scratch():
+def _valid_args(n_elements=10, n_nodes=10):
+    """Arguments that pass every host check; the pointers are dummies that no
+    test lets reach a launch."""
     args = L.NoallocArgs()
     args.dim, args.degree, args.qdim = 3, 2, 3
     args.im = b"IM_TETRAHEDRON(5)"
-    args.n_elements = L.NOALLOC_SCRATCH_BYTES // (32 * 8) + 1
-    args.n_nodes = 10
+    args.n_elements, args.n_nodes = n_elements, n_nodes
     args.points = args.cvpts = args.enode = args.adj_ptr = args.adj = args.vec = 1
+    args.slots[0] = 1
+    return args
+
+
+def _elasticity_form(coef_slot=1, source_slot=3):
     form = L.Form()
-    status = L.lib().gfgpu_assemble_vector_noalloc(C.byref(args), C.byref(form), None)
-    assert status == L.E_INVALID
+    form.n_terms = 2
+    t = form.terms[0]
+    t.kind, t.scale = 1, 1.0  # GRADGRAD
+    t.c[0].kind, t.c[0].slot, t.c[0].value = 2, coef_slot, 1.0  # ELEMENT
+    t.c[1].kind, t.c[1].value = 1, 1.0  # CONST
+    t.c[2].kind, t.c[2].value = 1, 1.0
+    s = form.terms[1]
+    s.kind, s.scale, s.field_slot = 3, -1.0, source_slot  # SOURCE
+    return form
+
+
+def _status(args, form):
+    return L.lib().gfgpu_assemble_vector_noalloc(C.byref(args), C.byref(form), None)
+
+
+def test_noalloc_rejects_meshes_beyond_its_scratch():
+    args = _valid_args()
+    args.n_elements = L.NOALLOC_SCRATCH_BYTES // (32 * 8) + 1
+    args.slots[1] = args.slots[3] = 1
+    assert _status(args, _elasticity_form()) == L.E_INVALID
     assert b"GFGPU_NOALLOC_SCRATCH_BYTES" in L.lib().gfgpu_last_error()
+
+
+def test_noalloc_rejects_a_missing_coefficient_slot():
+    args = _valid_args()
+    args.slots[3] = 1  # the load is there, the per-element coefficient (slot 1) is not
+    assert _status(args, _elasticity_form()) == L.E_INVALID
+    assert b"coefficient slot" in L.lib().gfgpu_last_error()
+
+
+def test_noalloc_rejects_a_coefficient_slot_out_of_range():
+    args = _valid_args()
+    args.slots[3] = 1
+    assert _status(args, _elasticity_form(coef_slot=L.MAX_SLOTS)) == L.E_INVALID
+
+
+def test_noalloc_rejects_a_missing_source_field():
+    args = _valid_args()
+    args.slots[1] = 1
+    assert _status(args, _elasticity_form()) == L.E_INVALID
+    assert b"source field" in L.lib().gfgpu_last_error()
+
+
+def test_noalloc_rejects_too_many_terms():
+    args = _valid_args()
+    args.slots[1] = args.slots[3] = 1
+    form = _elasticity_form()
+    form.n_terms = 9
+    assert _status(args, form) == L.E_INVALID
+    assert b"terms" in L.lib().gfgpu_last_error()
+
+
+def test_noalloc_rejects_null_adjacency_without_elements():
+    """No elements but nodes to write: the adjacency and the output must
+    still be real pointers."""
+    args = _valid_args(n_elements=0, n_nodes=4)
+    args.adj_ptr = None
+    assert _status(args, _elasticity_form()) == L.E_INVALID
+    args = _valid_args(n_elements=0, n_nodes=4)
+    args.vec = None
+    assert _status(args, _elasticity_form()) == L.E_INVALID
+
+
