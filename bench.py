@@ -59,6 +59,34 @@ def p2tet_inputs(nx: int, seed: int = 2026):
     return jit, data
 
 
+def neohookean_inputs(xyz: np.ndarray, E: int, seed: int = 3):
+    """Inputs of the Q2 neo-Hookean workload: u = the sum of 8 sinusoid modes
+    0.05 sin(k.x + phi) per component (k ~ U[-pi, pi]^3, phi ~ U[0, 2 pi]) at
+    the DOF nodes xyz, and the per-element shear modulus lognormal(0, 0.3)."""
+    rng = np.random.default_rng(seed)
+    u = np.zeros((xyz.shape[0], 3))
+    for a in range(3):
+        for _ in range(8):
+            k = rng.uniform(-np.pi, np.pi, 3)
+            u[:, a] += 0.05 * np.sin(xyz @ k + rng.uniform(0, 2 * np.pi))
+    mu = np.exp(rng.normal(0, 0.3, E))
+    return u.ravel(), mu
+
+
+def q4_inputs(E: int, ndof: int, seed: int = 5):
+    """Inputs of the Q4 Laplacian workload: per-element diffusivity
+    lognormal(0, 0.5) and u i.i.d. N(0, 1)."""
+    rng = np.random.default_rng(seed)
+    kappa = np.exp(rng.normal(0, 0.5, E))
+    u = rng.standard_normal(ndof)
+    return kappa, u
+
+
+def poisson_inputs(ndof: int, seed: int = 1):
+    """Nodal load of the 2-D Poisson workload, U[-1, 1]."""
+    return np.random.default_rng(seed).uniform(-1, 1, ndof)
+
+
 def make_problem(nx: int, seed: int = 2026):
     import getfem_gb300 as g
     jit, data = p2tet_inputs(nx, seed)
@@ -273,21 +301,15 @@ def bench_neohookean(steps, nx=32):
     import getfem_gb300 as g
     from getfem_gb300 import _lib as L
     lib = L.lib()
-    rng = np.random.default_rng(3)
     mesh = g.Mesh.regular_unit(3, nx, "hex")
     mf = g.MeshFem(mesh, 3, degree=2)
     mim = g.MeshIm(mesh, "IM_GAUSS_PARALLELEPIPED(3,5)")
-    xyz = mf.basic_dof_nodes()
-    u = np.zeros((xyz.shape[0], 3))
-    for a in range(3):
-        for _ in range(8):
-            k = rng.uniform(-np.pi, np.pi, 3)
-            u[:, a] += 0.05 * np.sin(xyz @ k + rng.uniform(0, 2 * np.pi))
     E = mesh.nb_convex()
+    u, mu_np = neohookean_inputs(mf.basic_dof_nodes(), E)
     dev = "cuda"
-    mu = torch.tensor(np.exp(rng.normal(0, 0.3, E)), device=dev)
+    mu = torch.tensor(mu_np, device=dev)
     ws = g.GaWorkspace()
-    ws.add_fem_variable("u", mf, U=torch.tensor(u.ravel(), device=dev))
+    ws.add_fem_variable("u", mf, U=torch.tensor(u, device=dev))
     ws.add_fem_constant("mu", g.MeshFem(mesh, 1, degree=0), mu)
     ws.add_fixed_size_constant("D1", np.array([1.5]))
     ws.add_expression("Compressible_Neo_Hookean_potential(Grad_u,[0.5*mu;D1])", mim)
@@ -443,15 +465,15 @@ def bench_q4(steps, nx=64):
     import getfem_gb300 as g
     from getfem_gb300 import _lib as L
     lib = L.lib()
-    rng = np.random.default_rng(5)
     t0 = time.perf_counter()
     mesh = g.Mesh.regular_unit(3, nx, "hex")
     mf = g.MeshFem(mesh, 1, degree=4)
     mim = g.MeshIm(mesh, "IM_GAUSS_PARALLELEPIPED(3,9)")
     E = mesh.nb_convex()
     dev = "cuda"
-    kappa = torch.tensor(np.exp(rng.normal(0, 0.5, E)), device=dev)
-    u = torch.tensor(rng.standard_normal(mf.nb_dof()), device=dev)
+    kappa_np, u_np = q4_inputs(E, mf.nb_dof())
+    kappa = torch.tensor(kappa_np, device=dev)
+    u = torch.tensor(u_np, device=dev)
     ws = g.GaWorkspace()
     ws.add_fem_variable("u", mf, U=u)
     ws.add_fem_constant("kappa", g.MeshFem(mesh, 1, degree=0), kappa)
@@ -525,12 +547,11 @@ def bench_poisson_cg():
     import torch
     import getfem_gb300 as g
     from getfem_gb300 import solvers
-    rng = np.random.default_rng(1)
     mesh = g.Mesh.regular_unit(2, 64, "simplex")
     mf = g.MeshFem(mesh, 1, degree=1)
     ws = g.GaWorkspace()
     ws.add_fem_variable("u", mf, U=np.zeros(mf.nb_dof()))
-    ws.add_fem_constant("f", mf, rng.uniform(-1, 1, mf.nb_dof()))
+    ws.add_fem_constant("f", mf, poisson_inputs(mf.nb_dof()))
     ws.add_expression("Grad_u.Grad_Test_u - f*Test_u", g.MeshIm(mesh, "IM_TRIANGLE(2)"))
     dofs = solvers.boundary_dofs(mf)
     solvers.solve_linear(ws, dofs)
@@ -646,21 +667,34 @@ def main():
         kt += np.array([t[0], t[1]])
     kt /= nprof
 
-    # end to end through the C ABI with pinned host buffers
+    # end to end through the C ABI with pinned host buffers: u in, the
+    # upper triangle of the symmetric K (gfgpu_assemble_host_upper; the
+    # full K is its mirror, bit for bit) and R out every step; the same with
+    # all nnz values (gfgpu_assemble_host) as a second figure
     u_h = torch.from_numpy(np.ascontiguousarray(data["u"])).pin_memory()
-    vals_h = torch.empty(nnz, dtype=torch.float64).pin_memory()
     vec_h = torch.empty(mf.nb_dof(), dtype=torch.float64).pin_memory()
+    nnz_u = C.c_int64()
+    L.check(lib.gfgpu_pattern_upper(h, C.byref(nnz_u), None, None))
+    nnz_u = nnz_u.value
     e2e_steps = max(3, min(args.steps, 20))
-    for _ in range(2):
-        L.check(lib.gfgpu_assemble_host(h, C.c_void_p(u_h.data_ptr()), C.c_void_p(vals_h.data_ptr()),
-                                        C.c_void_p(vec_h.data_ptr())))
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        L.check(lib.gfgpu_assemble_host(h, C.c_void_p(u_h.data_ptr()), C.c_void_p(vals_h.data_ptr()),
-                                        C.c_void_p(vec_h.data_ptr())))
-    barrier()
-    e2e_ms = 1e3 * (time.perf_counter() - t0) / e2e_steps
+
+    def host_loop(fn, out_h):
+        for _ in range(2):
+            L.check(fn(h, C.c_void_p(u_h.data_ptr()), C.c_void_p(out_h.data_ptr()),
+                       C.c_void_p(vec_h.data_ptr())))
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            L.check(fn(h, C.c_void_p(u_h.data_ptr()), C.c_void_p(out_h.data_ptr()),
+                       C.c_void_p(vec_h.data_ptr())))
+        barrier()
+        return 1e3 * (time.perf_counter() - t0) / e2e_steps
+    vals_h = torch.empty(nnz, dtype=torch.float64).pin_memory()
+    e2e_full_ms = host_loop(lib.gfgpu_assemble_host, vals_h)
+    del vals_h
+    uvals_h = torch.empty(nnz_u, dtype=torch.float64).pin_memory()
+    e2e_ms = host_loop(lib.gfgpu_assemble_host_upper, uvals_h)
+    del uvals_h
 
     ms, e2e_ms, value, e2e = combine_ranks(dist, world, E, ms, e2e_ms, "cuda")
     if rank != 0:
@@ -756,7 +790,13 @@ def main():
                    "elements_per_s": E / (steady_ms * 1e-3), "clocks": steady.summary()},
         "step_hbm_frac": step_bytes / (ms * 1e-3) / 1e9 / hbm_peak,
         "e2e": {"value": e2e, "unit": "elements/s", "h2d_bytes_per_step": 8 * mf.nb_dof(),
-                "d2h_bytes_per_step": 8 * nnz + 8 * mf.nb_dof(), "ms_per_step": e2e_ms},
+                "d2h_bytes_per_step": 8 * nnz_u + 8 * mf.nb_dof(), "ms_per_step": e2e_ms,
+                "api": "gfgpu_assemble_host_upper (u in; the upper triangle of the "
+                       "bit-symmetric K, nnz_upper values, and R out)", "nnz_upper": nnz_u},
+        "e2e_full_values": {"value": world * E / (e2e_full_ms * 1e-3), "unit": "elements/s",
+                            "h2d_bytes_per_step": 8 * mf.nb_dof(),
+                            "d2h_bytes_per_step": 8 * nnz + 8 * mf.nb_dof(),
+                            "ms_per_step": e2e_full_ms, "api": "gfgpu_assemble_host"},
         "gpu_launches": int(launches), "cpu_baseline": cpu, "clocks": sampler.summary(),
     }
     if not args.no_extra and world == 1:

@@ -109,6 +109,9 @@ _PROTOS = {
     "gfgpu_device_vector": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "gfgpu_assemble": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_double)]),
     "gfgpu_assemble_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "gfgpu_assemble_host_upper": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "gfgpu_pattern_upper": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.c_void_p,
+                                      C.c_void_p]),
     "gfgpu_sync": (C.c_int, [C.c_void_p]),
     "gfgpu_launch_count": (C.c_int64, [C.c_void_p]),
     "gfgpu_copy_result": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),

@@ -320,6 +320,40 @@ int check_geometry(const Plan &P) {
   return GFGPU_OK;
 }
 
+// The upper triangle of the current pattern (entries with column >= row):
+// per-row skips, row pointers (device and host) and the value buffer.
+int build_upper(Plan &P) {
+  if (P.upper_build == P.pattern_builds && P.d_urowptr) return GFGPU_OK;
+  dfree(P.d_urowptr);
+  dfree(P.d_uskip);
+  dfree(P.d_uvals);
+  P.upper_build = -1;
+  int rc;
+  if ((rc = dalloc(&P.d_urowptr, size_t(P.n_dof + 1)))) return rc;
+  if ((rc = dalloc(&P.d_uskip, size_t(P.n_dof)))) return rc;
+  // row lengths into d_count (scratch of n_dof + 1, free after a pattern build)
+  GF_CUDA(cudaMemsetAsync(P.d_count, 0, size_t(P.n_dof + 1) * sizeof(int64_t), P.stream));
+  GF_CUDA(launch_upper_count(P, P.d_count));
+  size_t need = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, need, P.d_count, P.d_urowptr, P.n_dof + 1);
+  if (need > P.cub_bytes) {
+    dfree(P.d_cub);
+    GF_CUDA(cudaMalloc(&P.d_cub, need));
+    P.cub_bytes = need;
+  }
+  GF_CUDA(cub::DeviceScan::ExclusiveSum(P.d_cub, P.cub_bytes, P.d_count, P.d_urowptr,
+                                        P.n_dof + 1, P.stream));
+  P.launches++;
+  P.h_urowptr.resize(size_t(P.n_dof + 1));
+  GF_CUDA(cudaMemcpyAsync(P.h_urowptr.data(), P.d_urowptr, size_t(P.n_dof + 1) * sizeof(int64_t),
+                          cudaMemcpyDeviceToHost, P.stream));
+  GF_CUDA(cudaStreamSynchronize(P.stream));
+  P.nnz_upper = P.h_urowptr.back();
+  if ((rc = dalloc(&P.d_uvals, size_t(P.nnz_upper)))) return rc;
+  P.upper_build = P.pattern_builds;
+  return GFGPU_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -411,6 +445,10 @@ int gfgpu_plan_create(const gfgpu_space *space, const gfgpu_form *form, void *cu
     }
     for (int t = 0; t < P->form.n_terms; ++t)
       if (P->form.terms[t].kind == GFGPU_TERM_INTERNAL_P) P->ip_term = t;
+    // every other lowered term has a symmetric element matrix, which every
+    // element kernel computes once per pair and mirrors: K is symmetric bit
+    // for bit
+    P->symmetric = P->ip_term < 0;
     // potentials of forms with an internal variable are not lowered
     P->kpot = P->ip_term < 0 && gauss_potential_available(S.dim, S.kind, S.degree, S.qdim, P->law);
     if (!P->kmat && !P->kpot) {
@@ -477,14 +515,35 @@ int gfgpu_plan_create(const gfgpu_space *space, const gfgpu_form *form, void *cu
       P->h_bucket.assign(1, 0);
       P->bucket_mad.clear();
       int32_t carry = 0;
+      std::vector<int> merged_of(33, 0), pending;
       for (int b = 0; b < 33; ++b) {
         if (cnt[b + 1] == cnt[b]) continue;
         carry = std::max(carry, mad[b]);
+        pending.push_back(b);
         const bool last = cnt[b + 1] == cnt[33];
         if (cnt[b + 1] - P->h_bucket.back() < small && !last) continue;
         P->h_bucket.push_back(cnt[b + 1]);
         P->bucket_mad.push_back(carry);
+        for (int q : pending) merged_of[q] = int(P->h_bucket.size()) - 2;
+        pending.clear();
         carry = 0;
+      }
+      // the same buckets within each chunk of gfgpu_assemble_host: chunk c
+      // keeps its nodes [n0, n1) in positions [n0, n1) of h_corder, ordered
+      // by bucket; h_cbucket[c * (nmb + 1) + m] starts bucket m
+      const int nmb = int(P->h_bucket.size()) - 1;
+      P->h_corder.assign(size_t(P->n_nodes), 0);
+      P->h_cbucket.assign(size_t(kHostChunks) * (nmb + 1), 0);
+      for (int c = 0; c < kHostChunks && nmb > 0; ++c) {
+        const int64_t n0 = P->n_nodes * c / kHostChunks, n1 = P->n_nodes * (c + 1) / kHostChunks;
+        int64_t *cb = P->h_cbucket.data() + size_t(c) * (nmb + 1);
+        std::vector<int64_t> ccnt(size_t(nmb + 1), 0);
+        for (int64_t i = n0; i < n1; ++i) ccnt[merged_of[bucket_of(aptr[i + 1] - aptr[i])] + 1]++;
+        cb[0] = n0;
+        for (int m = 0; m < nmb; ++m) cb[m + 1] = cb[m] + ccnt[m + 1];
+        std::vector<int64_t> cfill(cb, cb + nmb);
+        for (int64_t i = n0; i < n1; ++i)
+          P->h_corder[size_t(cfill[merged_of[bucket_of(aptr[i + 1] - aptr[i])]]++)] = int32_t(i);
       }
     }
     // host-buffer assembly: for each gather chunk of DOF nodes, one past the
@@ -541,6 +600,10 @@ int gfgpu_plan_create(const gfgpu_space *space, const gfgpu_form *form, void *cu
     if (!P->h_tri.empty()) {
       CHK(dalloc(&P->d_tri, P->h_tri.size()));
       CHK(up(P->d_tri, P->h_tri.data(), P->h_tri.size() * sizeof(int32_t)));
+    }
+    if (!P->h_corder.empty()) {
+      CHK(dalloc(&P->d_corder, P->h_corder.size()));
+      CHK(up(P->d_corder, P->h_corder.data(), P->h_corder.size() * sizeof(int32_t)));
     }
     if (!P->h_order.empty()) {
       CHK(dalloc(&P->d_order, P->h_order.size()));
@@ -610,10 +673,14 @@ void gfgpu_plan_destroy(gfgpu_plan *P) {
   dfree(P->d_int);
   dfree(P->d_kqj);
   dfree(P->d_order);
+  dfree(P->d_corder);
   dfree(P->d_elem);
   dfree(P->d_rowptr);
   dfree(P->d_colidx);
   dfree(P->d_vals);
+  dfree(P->d_urowptr);
+  dfree(P->d_uskip);
+  dfree(P->d_uvals);
   dfree(P->d_nptr);
   dfree(P->d_ncol);
   dfree(P->d_nbits);
@@ -1083,21 +1150,41 @@ int gfgpu_sync(gfgpu_plan *P) {
   return check_err(*P, true);
 }
 
-int gfgpu_assemble_host(gfgpu_plan *P, const double *u, double *vals, double *vec) {
-  if (!P) return GFGPU_E_INVALID;
+}  // extern "C"
+
+namespace {
+
+// The host-buffer assembly of gfgpu_assemble_host (upper = false: the full
+// CSR values) and gfgpu_assemble_host_upper (upper = true: the values of
+// the entries with column >= row, in the order of gfgpu_pattern_upper).
+int assemble_host(gfgpu_plan *P, const double *u, double *vals, double *vec, bool upper) {
   int rc;
   if (u && (rc = gfgpu_set_data(P, GFGPU_SLOT_U, u, P->n_dof, 0))) return rc;
   if (P->nnz < 0 || !vals || !P->kmat || P->h_rowptr.empty()) {
     // first assembly (the pattern is built) or no matrix wanted
     if ((rc = gfgpu_assemble(P, 2, vec ? GFGPU_WITH_VECTOR : 0, nullptr))) return rc;
-    if (vals) GF_CUDA(cudaMemcpyAsync(vals, P->d_vals, size_t(P->nnz) * sizeof(double),
-                                      cudaMemcpyDeviceToHost, P->stream));
+    if (vals && !upper)
+      GF_CUDA(cudaMemcpyAsync(vals, P->d_vals, size_t(P->nnz) * sizeof(double),
+                              cudaMemcpyDeviceToHost, P->stream));
     if (vec) GF_CUDA(cudaMemcpyAsync(vec, P->d_vec, size_t(P->n_dof) * sizeof(double),
                                      cudaMemcpyDeviceToHost, P->stream));
+    if ((rc = check_err(*P))) return rc;
+    if (!vals || !upper) return GFGPU_OK;
+    // the upper values of the first call: the gather once more in upper mode
+    if ((rc = build_upper(*P))) return rc;
+    P->upper_out = true;
+    cudaError_t ce = launch_gather(*P, true, false);
+    P->upper_out = false;
+    GF_CUDA(ce);
+    GF_CUDA(cudaMemcpyAsync(vals, P->d_uvals, size_t(P->nnz_upper) * sizeof(double),
+                            cudaMemcpyDeviceToHost, P->stream));
     return check_err(*P);
   }
   if ((rc = check_slots(*P, true))) return rc;
   if ((rc = check_geometry(*P))) return rc;
+  if (upper && (rc = build_upper(*P))) return rc;
+  const std::vector<int64_t> &hptr = upper ? P->h_urowptr : P->h_rowptr;
+  double *dvals = upper ? P->d_uvals : P->d_vals;
   // The element pass, then the row gather in chunks of DOF nodes; the rows
   // of each chunk (contiguous in the CSR) are copied to the host on a second
   // stream while the next chunk is gathered.  (Writing the values from the
@@ -1119,29 +1206,35 @@ int gfgpu_assemble_host(gfgpu_plan *P, const double *u, double *vals, double *ve
   if (P->affine_hex) GF_CUDA(launch_affine_hex_pass(*P, true));
   else if (!P->affine_simplex) GF_CUDA(launch_hex_element_pass(*P, true));
   const int qd = P->qdim;
+  P->upper_out = upper;
   for (int c = 0; c < kHostChunks; ++c) {
     const int64_t n0 = P->n_nodes * c / kHostChunks, n1 = P->n_nodes * (c + 1) / kHostChunks;
     if (P->affine_simplex) {
       const int64_t need = c == kHostChunks - 1 ? (P->n_elements + 31) / 32
                                                 : (P->h_chunk_eend[c] + 31) / 32;
       if (need > tiles_done) {
-        GF_CUDA(launch_simplex_element_pass(*P, true, tiles_done, need, false));
+        cudaError_t ce = launch_simplex_element_pass(*P, true, tiles_done, need, false);
+        if (ce != cudaSuccess) P->upper_out = false;
+        GF_CUDA(ce);
         tiles_done = need;
       }
     }
-    GF_CUDA(launch_gather_range(*P, true, vec != nullptr, n0, n1));
+    cudaError_t ce = launch_gather_chunk(*P, vec != nullptr, c);
+    if (ce != cudaSuccess) P->upper_out = false;
+    GF_CUDA(ce);
     cudaStream_t cs = P->copy_stream[c & 1];
     GF_CUDA(cudaEventRecord(P->chunk_ev[c], P->stream));
     GF_CUDA(cudaStreamWaitEvent(cs, P->chunk_ev[c], 0));
-    const int64_t r0 = P->h_rowptr[size_t(n0 * qd)], r1 = P->h_rowptr[size_t(n1 * qd)];
+    const int64_t r0 = hptr[size_t(n0 * qd)], r1 = hptr[size_t(n1 * qd)];
     if (r1 > r0)
-      GF_CUDA(cudaMemcpyAsync(vals + r0, P->d_vals + r0, size_t(r1 - r0) * sizeof(double),
+      GF_CUDA(cudaMemcpyAsync(vals + r0, dvals + r0, size_t(r1 - r0) * sizeof(double),
                               cudaMemcpyDeviceToHost, cs));
     if (vec && n1 > n0)
       GF_CUDA(cudaMemcpyAsync(vec + n0 * qd, P->d_vec + n0 * qd,
                               size_t((n1 - n0) * qd) * sizeof(double), cudaMemcpyDeviceToHost,
                               cs));
   }
+  P->upper_out = false;
   GF_CUDA(cudaStreamSynchronize(P->copy_stream[0]));
   GF_CUDA(cudaStreamSynchronize(P->copy_stream[1]));
   P->last_want_R = vec != nullptr;
@@ -1154,14 +1247,66 @@ int gfgpu_assemble_host(gfgpu_plan *P, const double *u, double *vals, double *ve
                    "nonzero now): read gfgpu_pattern_size / the new pattern and call again");
     return GFGPU_E_STATE;
   }
-  if (vals) {
+  if (vals && !upper) {
     // rebuilt with the same size: copy the repaired values again
     GF_CUDA(cudaMemcpy(vals, P->d_vals, size_t(P->nnz) * sizeof(double),
                        cudaMemcpyDeviceToHost));
-    if (vec) GF_CUDA(cudaMemcpy(vec, P->d_vec, size_t(P->n_dof) * sizeof(double),
-                                cudaMemcpyDeviceToHost));
+  } else if (vals) {
+    // the repair gathered the full CSR: the upper values once more
+    if ((rc = build_upper(*P))) return rc;
+    P->upper_out = true;
+    cudaError_t ce = launch_gather(*P, true, false);
+    P->upper_out = false;
+    GF_CUDA(ce);
+    GF_CUDA(cudaMemcpyAsync(vals, P->d_uvals, size_t(P->nnz_upper) * sizeof(double),
+                            cudaMemcpyDeviceToHost, P->stream));
+    if ((rc = check_err(*P))) return rc;
   }
+  if (vec) GF_CUDA(cudaMemcpy(vec, P->d_vec, size_t(P->n_dof) * sizeof(double),
+                              cudaMemcpyDeviceToHost));
   return rc2;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gfgpu_assemble_host(gfgpu_plan *P, const double *u, double *vals, double *vec) {
+  if (!P) return GFGPU_E_INVALID;
+  return assemble_host(P, u, vals, vec, false);
+}
+
+int gfgpu_assemble_host_upper(gfgpu_plan *P, const double *u, double *upper_vals, double *vec) {
+  if (!P) return GFGPU_E_INVALID;
+  if (!P->symmetric) {
+    set_last_error("gfgpu_assemble_host_upper: the form's matrix is not symmetric");
+    return GFGPU_E_UNSUPPORTED;
+  }
+  return assemble_host(P, u, upper_vals, vec, true);
+}
+
+int gfgpu_pattern_upper(gfgpu_plan *P, int64_t *nnz_upper, int64_t *rowptr, int32_t *colidx) {
+  if (!P || !nnz_upper) return GFGPU_E_INVALID;
+  if (P->nnz < 0) {
+    set_last_error("no pattern yet: assemble order 2 first");
+    return GFGPU_E_STATE;
+  }
+  int rc;
+  if ((rc = build_upper(*P))) return rc;
+  *nnz_upper = P->nnz_upper;
+  if (rowptr) std::copy(P->h_urowptr.begin(), P->h_urowptr.end(), rowptr);
+  if (colidx && P->nnz_upper > 0) {
+    int32_t *d_ucol = nullptr;
+    if ((rc = dalloc(&d_ucol, size_t(P->nnz_upper)))) return rc;
+    cudaError_t ce = launch_upper_fill(*P, d_ucol);
+    if (ce == cudaSuccess)
+      ce = cudaMemcpyAsync(colidx, d_ucol, size_t(P->nnz_upper) * sizeof(int32_t),
+                           cudaMemcpyDeviceToHost, P->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(P->stream);
+    dfree(d_ucol);
+    GF_CUDA(ce);
+  }
+  return GFGPU_OK;
 }
 
 int gfgpu_pattern_size(gfgpu_plan *P, int64_t *n_rows, int64_t *nnz) {

@@ -220,7 +220,7 @@ __device__ __forceinline__ void gather_node(
     const int16_t *__restrict__ slotmap, const int64_t *__restrict__ rowptr,
     double *__restrict__ vals, bool want_K, bool want_R, double *__restrict__ vec,
     int *__restrict__ err, const int32_t *__restrict__ ncol = nullptr,
-    const double *__restrict__ u = nullptr) {
+    const double *__restrict__ u = nullptr, UpperOut up = UpperOut{}) {
   constexpr int QQ = QD * QD;
   const int lane = threadIdx.x & 31;
   const int nb = L.nb, S = L.s, blk = L.rowblk;
@@ -375,8 +375,18 @@ __device__ __forceinline__ void gather_node(
 #pragma unroll
     for (int a = 0; a < QD; ++a) {
       const unsigned am = ((1u << QD) - 1u) << (a * QD);
-      int64_t p = rowptr[node * QD + a];
-      const int64_t pend = rowptr[node * QD + a + 1];
+      const int64_t row = node * QD + a;
+      const int64_t p0 = rowptr[row];
+      int64_t p = p0;
+      const int64_t pend = rowptr[row + 1];
+      // upper-triangle output: entry k of the row (k >= skip[row], the
+      // first column >= row) goes to up.vals[up.rowptr[row] + k - skip]
+      int64_t ub = 0, ustart = 0, uend = 0;
+      if (up.vals) {
+        ustart = up.rowptr[row];
+        ub = ustart - up.skip[row];
+        uend = up.rowptr[row + 1];
+      }
       for (int j0 = 0; j0 < ns; j0 += kWarp) {
         const int j = j0 + lane;
         const unsigned m = j < ns ? (unsigned(bits[j]) & am) : 0u;
@@ -391,8 +401,17 @@ __device__ __forceinline__ void gather_node(
 #pragma unroll
           for (int b = 0; b < QD; ++b)
             if (m & (1u << (a * QD + b))) {
-              if (q < pend) vals[q] = acc[(j * QD + a) * QD + b];
-              else set_err(err, ERR_CAPACITY);
+              const double x = acc[(j * QD + a) * QD + b];
+              if (!up.vals) {
+                if (q < pend) vals[q] = x;
+                else set_err(err, ERR_CAPACITY);
+              } else {
+                const int64_t t = ub + (q - p0);
+                if (t >= ustart) {
+                  if (t < uend) up.vals[t] = x;
+                  else set_err(err, ERR_CAPACITY);
+                }
+              }
               ++q;
             }
         }
@@ -417,7 +436,7 @@ __global__ void __launch_bounds__(128) gather_kernel(
     const uint16_t *__restrict__ nbits, const int16_t *__restrict__ slotmap,
     const int64_t *__restrict__ rowptr, double *__restrict__ vals, bool want_K, bool want_R,
     double *__restrict__ vec, int *__restrict__ err, const int32_t *__restrict__ ncol,
-    const double *__restrict__ u) {
+    const double *__restrict__ u, UpperOut up) {
   extern __shared__ __align__(16) double dsm[];
   const int wib = threadIdx.x >> 5;
   char *base = reinterpret_cast<char *>(dsm) + wib * gather_warp_bytes(ms, QD, L.rowblk, mad);
@@ -425,7 +444,37 @@ __global__ void __launch_bounds__(128) gather_kernel(
   if (i >= i1) return;
   const int64_t node = order ? int64_t(order[i]) : i;
   gather_node<QD, R>(base, node, L, adj_ptr, adj, elem, ms, mad, nptr, nbits, slotmap, rowptr,
-                     vals, want_K, want_R, vec, err, ncol, u);
+                     vals, want_K, want_R, vec, err, ncol, u, up);
+}
+
+// Upper-triangle pattern of a CSR with sorted columns: skip[r] = number of
+// entries of row r with a column < r; ulen[r] = the others.
+__global__ void upper_count_kernel(int64_t n, const int64_t *__restrict__ rowptr,
+                                   const int32_t *__restrict__ colidx, int32_t *__restrict__ skip,
+                                   int64_t *__restrict__ ulen) {
+  const int64_t r = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (r >= n) return;
+  int64_t lo = rowptr[r], hi = rowptr[r + 1];
+  const int64_t start = lo, end = hi;
+  while (lo < hi) {  // first column >= r
+    const int64_t mid = (lo + hi) >> 1;
+    if (int64_t(colidx[mid]) < r) lo = mid + 1;
+    else hi = mid;
+  }
+  skip[r] = int32_t(lo - start);
+  ulen[r] = end - lo;
+}
+
+// Upper-triangle column indices (entries k >= skip[r] of every row).
+__global__ void upper_fill_kernel(int64_t n, const int64_t *__restrict__ rowptr,
+                                  const int32_t *__restrict__ colidx,
+                                  const int32_t *__restrict__ skip,
+                                  const int64_t *__restrict__ urowptr,
+                                  int32_t *__restrict__ ucol) {
+  const int64_t r = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (r >= n) return;
+  const int64_t s = rowptr[r] + skip[r], len = urowptr[r + 1] - urowptr[r];
+  for (int64_t k = 0; k < len; ++k) ucol[urowptr[r] + k] = colidx[s + k];
 }
 
 // Vector-only gather (no matrix): one thread per DOF node adds the QD
@@ -522,7 +571,8 @@ cudaError_t launch_gather_t(Plan &P, bool want_K, bool want_R, int64_t i0, int64
   gather_kernel<QD, R><<<blocks, kWarpsPerBlock * 32, smem, P.stream>>>(
       i0, i1, order, P.lay, P.d_adj_ptr, P.d_adj, P.d_elem, ms, mad, P.d_nptr, P.d_nbits,
       P.d_slotmap, P.d_rowptr, P.d_vals, want_K, want_R, P.d_vec, P.d_err,
-      P.r_from_rows ? P.d_ncol : nullptr, P.slot_ptr[GFGPU_SLOT_U]);
+      P.r_from_rows ? P.d_ncol : nullptr, P.slot_ptr[GFGPU_SLOT_U],
+      P.upper_out ? UpperOut{P.d_uvals, P.d_urowptr, P.d_uskip} : UpperOut{});
   P.launches++;
   return cudaGetLastError();
 }
@@ -603,6 +653,24 @@ cudaError_t launch_pattern_fill(Plan &P) {
   return cudaGetLastError();
 }
 
+cudaError_t launch_upper_count(Plan &P, int64_t *d_ulen) {
+  if (P.n_dof == 0) return cudaSuccess;
+  const unsigned blocks = unsigned((P.n_dof + 255) / 256);
+  upper_count_kernel<<<blocks, 256, 0, P.stream>>>(P.n_dof, P.d_rowptr, P.d_colidx, P.d_uskip,
+                                                   d_ulen);
+  P.launches++;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_upper_fill(Plan &P, int32_t *d_ucol) {
+  if (P.n_dof == 0) return cudaSuccess;
+  const unsigned blocks = unsigned((P.n_dof + 255) / 256);
+  upper_fill_kernel<<<blocks, 256, 0, P.stream>>>(P.n_dof, P.d_rowptr, P.d_colidx, P.d_uskip,
+                                                  P.d_urowptr, d_ucol);
+  P.launches++;
+  return cudaGetLastError();
+}
+
 size_t batch_gather_warp_bytes(const BatchItem &it) {
   return gather_warp_bytes(it.ms, it.qd, it.L.rowblk, it.mad);
 }
@@ -645,6 +713,23 @@ cudaError_t batch_gather_attr(size_t smem) {
 cudaError_t launch_gather_range(Plan &P, bool want_K, bool want_R, int64_t n0, int64_t n1) {
   if (!want_K) return want_R ? launch_vector_gather(P, n0, n1) : cudaSuccess;
   return launch_gather_list(P, want_K, want_R, n0, n1, nullptr, P.max_slots, P.max_adj);
+}
+
+cudaError_t launch_gather_chunk(Plan &P, bool want_R, int c) {
+  const int nmb = int(P.h_bucket.size()) - 1;
+  if (P.d_corder && nmb > 0 && P.bucket_ms.size() == size_t(nmb) &&
+      P.h_cbucket.size() == size_t(kHostChunks) * (nmb + 1)) {
+    const int64_t *cb = P.h_cbucket.data() + size_t(c) * (nmb + 1);
+    for (int m = 0; m < nmb; ++m) {
+      if (cb[m + 1] <= cb[m]) continue;
+      cudaError_t ce = launch_gather_list(P, true, want_R, cb[m], cb[m + 1], P.d_corder,
+                                          P.bucket_ms[m], P.bucket_mad[m]);
+      if (ce != cudaSuccess) return ce;
+    }
+    return cudaSuccess;
+  }
+  const int64_t n0 = P.n_nodes * c / kHostChunks, n1 = P.n_nodes * (c + 1) / kHostChunks;
+  return launch_gather_range(P, true, want_R, n0, n1);
 }
 
 // The whole gather: one launch per valence bucket (nodes with similar

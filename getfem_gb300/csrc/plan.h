@@ -37,6 +37,15 @@ struct SimplexTables {
   double mass[kMaxNb * kMaxNb];  // reference mass matrix sum_q w_q phi_i phi_j
 };
 
+// Upper-triangle output of the row gather (gfgpu_assemble_host_upper):
+// entries with column >= row, row r at vals[rowptr[r] ..), skip[r] = the
+// entries of row r left of its diagonal.  vals == nullptr: the full CSR.
+struct UpperOut {
+  double *vals = nullptr;
+  const int64_t *rowptr = nullptr;
+  const int32_t *skip = nullptr;
+};
+
 // Per-element scratch written by every element kernel and read by the
 // pattern build and the row gather (doubles):
 //   K_e   s x s, row (li,a) = li*qd + a at offset row*rowstride (rowstride even)
@@ -192,8 +201,25 @@ struct Plan {
   int32_t *d_order = nullptr;
   std::vector<int64_t> h_bucket;
   std::vector<int32_t> h_order, bucket_ms, bucket_mad;
+  // the same buckets within each gather chunk of gfgpu_assemble_host
+  // (chunk c: nodes [n0, n1) of the chunk, ordered by bucket, in positions
+  // [n0, n1) of d_corder; bucket m of chunk c starts at
+  // h_cbucket[c * (buckets + 1) + m])
+  int32_t *d_corder = nullptr;
+  std::vector<int32_t> h_corder;
+  std::vector<int64_t> h_cbucket;
   cudaStream_t copy_stream[2] = {nullptr, nullptr};
   cudaEvent_t chunk_ev[kHostChunks] = {};
+  // upper triangle of a symmetric K (gfgpu_assemble_host_upper): row
+  // pointers (device and host), the entries of each row left of its
+  // diagonal, the values; built for the pattern of build number upper_build
+  bool symmetric = false;       // the form's K is symmetric bit for bit
+  bool upper_out = false;       // the current gather writes d_uvals only
+  int64_t *d_urowptr = nullptr;
+  int32_t *d_uskip = nullptr;
+  double *d_uvals = nullptr;
+  int64_t nnz_upper = -1, upper_build = -1;
+  std::vector<int64_t> h_urowptr;
 };
 
 // One mesh of a batched launch: everything the element pass and the row
@@ -246,6 +272,12 @@ cudaError_t launch_pattern_fill(Plan &P);
 cudaError_t launch_gather(Plan &P, bool want_K, bool want_R);
 // the gather of DOF nodes [n0, n1) (their rows of the CSR and of R)
 cudaError_t launch_gather_range(Plan &P, bool want_K, bool want_R, int64_t n0, int64_t n1);
+// the K (+ R) gather of host chunk c (of kHostChunks), per valence bucket
+cudaError_t launch_gather_chunk(Plan &P, bool want_R, int c);
+// upper-triangle pattern: per-row counts into d_ulen (and P.d_uskip), then
+// the column indices into d_ucol (after P.d_urowptr is scanned)
+cudaError_t launch_upper_count(Plan &P, int64_t *d_ulen);
+cudaError_t launch_upper_fill(Plan &P, int32_t *d_ucol);
 int build_simplex_tables(Plan &P, std::string &err);
 int fill_simplex_tables(int dim, int degree, int qdim, const std::string &im, SimplexTables &t,
                         KeLayout &lay, int &nq, std::string &err);

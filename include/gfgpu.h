@@ -263,6 +263,27 @@ int gfgpu_assemble(gfgpu_plan *plan, int32_t order, int32_t flags, double *poten
    Any of u / vals / vec may be NULL to skip that copy. */
 int gfgpu_assemble_host(gfgpu_plan *plan, const double *u, double *vals, double *vec);
 
+/* The same for a symmetric K, delivering only its upper triangle: the values
+   of the entries with column >= row, row by row in the order of
+   gfgpu_pattern_upper (about half of nnz), so that half the bytes cross the
+   host link.  K is symmetric bit for bit for every form without an
+   INTERNAL_P term (each element kernel computes a symmetric element matrix
+   once per entry pair and mirrors it; GetFEM's own K is symmetric for these
+   forms too), so mirroring the upper values gives the full K exactly.  A
+   GetFEM-side caller adds each value at (i, j) and, off the diagonal, at
+   (j, i) when it copies the result into its col_matrix (the add of
+   workspace.cc:803-845).  GFGPU_E_UNSUPPORTED for a form with an INTERNAL_P
+   term.  The plan's device CSR values (gfgpu_device_csr) are not updated by
+   this call. */
+int gfgpu_assemble_host_upper(gfgpu_plan *plan, const double *u, double *upper_vals,
+                              double *vec);
+
+/* Upper triangle of the plan's pattern (entries with column >= row):
+   *nnz_upper, and when non-NULL the row pointers (n_dof + 1 int64) and the
+   column indices (nnz_upper int32), host memory. */
+int gfgpu_pattern_upper(gfgpu_plan *plan, int64_t *nnz_upper, int64_t *rowptr,
+                        int32_t *colidx);
+
 /* Copies a result of the plan into caller memory (host or device; the
    copy direction is inferred from the pointer):
    which = 0: row pointers (n_dof+1 int64), 1: column indices (nnz int32),
