@@ -26,6 +26,7 @@ from __future__ import annotations
 import argparse
 import ctypes as C
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -41,6 +42,50 @@ EXPR = "(lambda*Div_u*Id(3)+2*mu*Sym(Grad_u)):Grad_Test_u - f.Test_u"
 METRIC = "elements/s assembled (K + residual), P2 tet elasticity"
 
 
+# --------------------------------------------------- synthetic inputs
+# The inputs are drawn with numpy's Generator (its uniform and normal
+# variates are the same bits on every host) and shaped with the two
+# functions below instead of np.exp / np.sin, whose last bit differs
+# between x86-64 and aarch64 builds of numpy: the fixtures made on one host
+# then describe the inputs of the other exactly.  Both use separate IEEE
+# multiplies and adds only (numpy ufuncs, never fused), so every host gives
+# the same bits; their accuracy is a few units in the last place.
+
+_LN2_HI, _LN2_LO = 0.6931471803691238, 1.9082149292705877e-10  # ln 2 = HI + LO, HI 32 bits
+_PIO2 = (1.5707963267341256, 6.077100506303966e-11, 2.0222662487959506e-21)  # pi/2, 3 parts
+_INV_FACT = [1.0 / math.factorial(n) for n in range(22)]
+
+
+def det_exp(x):
+    """e^x: x = k ln2 + r, |r| <= ln2/2, e^r by its Taylor series to r^17/17!
+    (Horner), scaled by 2^k."""
+    x = np.asarray(x, dtype=np.float64)
+    k = np.rint(x * (1.0 / 0.6931471805599453))
+    r = (x - k * _LN2_HI) - k * _LN2_LO
+    p = np.full_like(r, _INV_FACT[17])
+    for n in range(16, -1, -1):
+        p = p * r + _INV_FACT[n]
+    return np.ldexp(p, k.astype(np.int64))
+
+
+def det_sin(t):
+    """sin t: t = n pi/2 + r, |r| <= pi/4, then +-sin r or +-cos r by their
+    Taylor series (to r^21/21! and r^20/20!)."""
+    t = np.asarray(t, dtype=np.float64)
+    n = np.rint(t * (2.0 / math.pi))
+    r = ((t - n * _PIO2[0]) - n * _PIO2[1]) - n * _PIO2[2]
+    r2 = r * r
+    s = np.full_like(r, _INV_FACT[21])
+    for k in range(19, 0, -2):
+        s = s * r2 * (-1.0) + _INV_FACT[k]
+    s = s * r
+    c = np.full_like(r, _INV_FACT[20])
+    for k in range(18, -1, -2):
+        c = c * r2 * (-1.0) + _INV_FACT[k]
+    q = n.astype(np.int64) % 4
+    return np.where(q == 0, s, np.where(q == 1, c, np.where(q == 2, -s, -c)))
+
+
 def p2tet_inputs(nx: int, seed: int = 2026):
     """Seeded inputs of the P2-tet elasticity workload, made with numpy only
     (the reference arm uses them without the package): interior-vertex
@@ -54,7 +99,7 @@ def p2tet_inputs(nx: int, seed: int = 2026):
     ndof = 3 * (2 * nx + 1) ** 3
     jit = rng.uniform(-0.1 * h, 0.1 * h, ((nx + 1) ** 3, 3))
     data = dict(u=rng.standard_normal(ndof) * 1e-3,
-                lam=np.exp(rng.normal(0.0, 0.2, E)), mu=np.exp(rng.normal(0.0, 0.2, E)),
+                lam=det_exp(rng.normal(0.0, 0.2, E)), mu=det_exp(rng.normal(0.0, 0.2, E)),
                 f=rng.standard_normal(ndof))
     return jit, data
 
@@ -68,8 +113,9 @@ def neohookean_inputs(xyz: np.ndarray, E: int, seed: int = 3):
     for a in range(3):
         for _ in range(8):
             k = rng.uniform(-np.pi, np.pi, 3)
-            u[:, a] += 0.05 * np.sin(xyz @ k + rng.uniform(0, 2 * np.pi))
-    mu = np.exp(rng.normal(0, 0.3, E))
+            t = ((xyz[:, 0] * k[0] + xyz[:, 1] * k[1]) + xyz[:, 2] * k[2]) + rng.uniform(0, 2 * np.pi)
+            u[:, a] += 0.05 * det_sin(t)
+    mu = det_exp(rng.normal(0, 0.3, E))
     return u.ravel(), mu
 
 
@@ -77,7 +123,7 @@ def q4_inputs(E: int, ndof: int, seed: int = 5):
     """Inputs of the Q4 Laplacian workload: per-element diffusivity
     lognormal(0, 0.5) and u i.i.d. N(0, 1)."""
     rng = np.random.default_rng(seed)
-    kappa = np.exp(rng.normal(0, 0.5, E))
+    kappa = det_exp(rng.normal(0, 0.5, E))
     u = rng.standard_normal(ndof)
     return kappa, u
 

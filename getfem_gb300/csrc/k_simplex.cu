@@ -286,16 +286,19 @@ __device__ __forceinline__ void simplex_element_tile(
       double row[RS];
 #pragma unroll
       for (int j = 0; j < NB; ++j) {
-        const int pij = i * NB + j;
-        double x = MASS ? cm * s_mass[pij] : 0.0;
-        const int ni = pk_sup_n(DIM, NB, i), nj = pk_sup_n(DIM, NB, j);
+        // entry (i, j) is computed as entry (min, max): the same terms in the
+        // same order as its mirror (j, i), so K_e is symmetric bit for bit
+        const int p = i < j ? i : j, q = i < j ? j : i;
+        const int ppq = p * NB + q;
+        double x = MASS ? cm * s_mass[ppq] : 0.0;
+        const int np_ = pk_sup_n(DIM, NB, p), nq_ = pk_sup_n(DIM, NB, q);
 #pragma unroll
-        for (int ti = 0; ti < 2; ++ti)
+        for (int tp_ = 0; tp_ < 2; ++tp_)
 #pragma unroll
-          for (int tj = 0; tj < 2; ++tj)
-            if (ti < ni && tj < nj)
-              x += s_gval[pij * kMaxPairTerms + ti * nj + tj] *
-                 tp(0, pk_sup_v(DIM, NB, i, ti), 0, pk_sup_v(DIM, NB, j, tj));
+          for (int tq = 0; tq < 2; ++tq)
+            if (tp_ < np_ && tq < nq_)
+              x += s_gval[ppq * kMaxPairTerms + tp_ * nq_ + tq] *
+                 tp(0, pk_sup_v(DIM, NB, p, tp_), 0, pk_sup_v(DIM, NB, q, tq));
         row[j] = x;
       }
 #pragma unroll
@@ -357,6 +360,15 @@ __device__ __forceinline__ void simplex_element_tile(
 #pragma unroll
               for (int b = 0; b < QD; ++b) B[a][b] += gv * tp(a, v, b, w);
           }
+        }
+        // a diagonal block holds the same terms in another order below its
+        // diagonal: take the mirror of the upper entries (K_e symmetric bit
+        // for bit)
+        if (i == j) {
+#pragma unroll
+          for (int a = 0; a < QD; ++a)
+#pragma unroll
+            for (int b = 0; b < a; ++b) B[a][b] = B[b][a];
         }
 #pragma unroll
         for (int a = 0; a < QD; ++a)

@@ -35,8 +35,12 @@
 //       src/getfem_models.cc:2646-2730: one ga_workspace per OpenMP thread
 //       over that thread's partition of the region) run W + S times with T
 //       threads; writes the S step times, nnz(K) and the norms of K and of
-//       the right-hand side to info.json)
+//       the right-hand side to info.json; model_out=1 also writes the
+//       tangent matrix K_*.bin and rhs.bin)
 //   dump=0   (skip the mesh / DOF map / reference-element dumps)
+//   vars=name:KIND,...   (data declared as variables after u, KIND as for
+//       consts but P0 / S / V only: the order-1 vector of a potential then
+//       holds dE/d(name) after the u rows)
 // The variable is always "u" (file in/u.bin, zeros when absent).
 // Jitter: when jitter=1, in/jitter.bin holds (nx+1)^dim x dim doubles in
 // lattice order (x index fastest); interior vertices are moved by it.
@@ -257,6 +261,12 @@ int main(int argc, char **argv) {
       if (r >= warm) times.push_back(std::chrono::duration<double>(t1 - t0).count());
     }
     const auto &K = md.real_tangent_matrix();
+    if (arg("model_out", "0") == "1") {
+      // the model's tangent matrix and right-hand side (rhs = -residual)
+      write_csr(out + "/K", K);
+      std::vector<double> rhs(md.real_rhs().begin(), md.real_rhs().end());
+      write_file(out + "/rhs.bin", rhs);
+    }
     size_type nnz = 0;
     double knorm = 0.0;
     for (size_type j = 0; j < gmm::mat_ncols(K); ++j)
@@ -335,6 +345,21 @@ int main(int argc, char **argv) {
     else if (k == "S") ws.add_fem_constant(kv[0], mfs, v);
     else if (k == "V") ws.add_fem_constant(kv[0], mf, v);
     else ws.add_fixed_size_constant(kv[0], v);
+  }
+  // data declared as variables (vars=name:P0|S|V,...), placed after u in
+  // the order given: the order-1 assembly of a potential then holds its
+  // derivative in each of them too (the derivative loop of add_tree,
+  // workspace.cc:520-535, GWFL's Diff), in R.bin after the n_dof u rows
+  size_type voff = ndof;
+  for (const std::string &c : split(arg("vars", ""), ',')) {
+    std::vector<std::string> kv = split(c, ':');
+    std::vector<double> &v = cst[kv[0]];
+    if (!read_file(in + "/" + kv[0] + ".bin", v)) { fprintf(stderr, "missing %s\n", kv[0].c_str()); return 2; }
+    const std::string &k = kv[1];
+    const getfem::mesh_fem &vmf = k == "P0" ? mf0 : k == "S" ? mfs : mf;
+    if (v.size() != vmf.nb_dof()) { fprintf(stderr, "%s has %zu values, need %zu\n", kv[0].c_str(), v.size(), size_t(vmf.nb_dof())); return 2; }
+    ws.add_fem_variable(kv[0], vmf, gmm::sub_interval(voff, v.size()), v);
+    voff += v.size();
   }
   ws.add_expression(expr, mim);
 

@@ -24,8 +24,9 @@ def golden_names(condensed=False):
     internal-variable condensation cases (they carry R_full / Rc)."""
     out = []
     for p in sorted(glob.glob(os.path.join(GOLDEN, "*.npz"))):
-        if os.path.basename(p).startswith("full_"):
-            continue  # the full-size fixtures (compact records, test_fullsize.py)
+        if os.path.basename(p).startswith("full_") or p.endswith("_diff.npz"):
+            continue  # full-size records (test_fullsize.py), parameter gradients
+            # (test_adjoint_diff.py)
         with np.load(p) as z:
             if ("Rc" in z.files) == condensed:
                 out.append(os.path.basename(p)[:-4])

@@ -60,6 +60,10 @@ def sha256_i64(a: np.ndarray) -> str:
     return hashlib.sha256(np.ascontiguousarray(a, dtype="<i8").tobytes()).hexdigest()
 
 
+def sha256_f8(a) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a, dtype="<f8").tobytes()).hexdigest()
+
+
 def probe_vectors(n: int, k: int, seed: int = PROBE_SEED):
     """The probe vectors w_k, v_k (N(0,1)), regenerated by the tests."""
     rng = np.random.default_rng(seed)
@@ -179,6 +183,12 @@ def make(name, seed):
                                                   args["deg"], args["qdim"], args["im"],
                                                   args["expr"], inputs, consts, jit)
     rec = compact_record(rowptr, colidx, vals, R, seed)
+    # the generated inputs, so that a host whose generator gives other bits
+    # is told so before any value is compared
+    hashes = {k: sha256_f8(v) for k, v in inputs.items()}
+    if jit is not None:
+        hashes["jitter"] = sha256_f8(jit)
+    meta.update(input_sha256=hashes)
     meta.update(name=name, dim=args["dim"], nx=args["nx"], gt=args["gt"], degree=args["deg"],
                 qdim=args["qdim"], im=args["im"], expr=args["expr"], consts=consts,
                 n_dof=info["n_dof"], n_elements=info["n_elements"], nnz=info["nnz"],

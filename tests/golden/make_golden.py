@@ -93,6 +93,33 @@ ORDERS = {"q2hex_nh_potential": "0,1,2", "p2tet_nh_potential": "0,1,2",
           "q2hex_kappa_potential": "0,1,2", "p2tri_energy_potential": "0,1,2"}
 
 
+# Parameter gradients of potentials from GWFL's own symbolic derivative: the
+# coefficient is declared as a variable (ref_driver vars=...), so the
+# reference's order-1 assembly of the potential holds dE/du and dE/dcoef.
+# The neo-Hookean energy is written out in GWFL (the law's potential
+# operator has no parameter derivative, getfem_nonlinear_elasticity.cc:1812):
+# W = C1 (j1 - 3) + D1 (sqrt(i3) - 1)^2, C = F'F, j1 = tr(C) det(C)^(-1/3)
+# (the law's strain_energy, getfem_nonlinear_elasticity.cc:503-523), with
+# C1 = mu/2; `gpu_expr` is the built-in potential the GPU path lowers, whose
+# energy must equal the explicit one.
+_F = "(Id(3)+Grad_u)"
+NH_EXPLICIT = (f"0.5*mu*(Trace({_F}'*{_F})*pow(Det({_F}'*{_F}),-1/3) - 3)"
+               f" + D1*sqr(sqrt(Det({_F}'*{_F})) - 1)")
+# name, dim, gt, degree, qdim, im, nx, expr, gpu_expr, consts, vars, jitter, u kind
+DIFF_CASES = [
+    ("q2hex_kappa_diff", 3, "QK", 2, 1, "IM_GAUSS_PARALLELEPIPED(3,5)", 3,
+     "kappa*Grad_u.Grad_u", "kappa*Grad_u.Grad_u", {}, {"kappa": "P0"}, False, "normal"),
+    ("q4hex_kappa_diff", 3, "QK", 4, 1, "IM_GAUSS_PARALLELEPIPED(3,9)", 2,
+     "kappa*Grad_u.Grad_u", "kappa*Grad_u.Grad_u", {}, {"kappa": "P0"}, False, "normal"),
+    ("q1hex_kappa_nodal_diff", 3, "QK", 1, 1, "IM_GAUSS_PARALLELEPIPED(3,3)", 3,
+     "kappa*Grad_u.Grad_u", "kappa*Grad_u.Grad_u", {}, {"kappa": "S"}, True, "normal"),
+    ("q2hex_nh_mu_diff", 3, "QK", 2, 3, "IM_GAUSS_PARALLELEPIPED(3,5)", 3,
+     NH_EXPLICIT, NH_POT, {"D1": "C"}, {"mu": "P0"}, True, "modes"),
+    ("p2tet_nh_mu_diff", 3, "PK", 2, 3, "IM_TETRAHEDRON(5)", 2,
+     NH_EXPLICIT, NH_POT, {"D1": "C"}, {"mu": "P0"}, True, "modes"),
+]
+
+
 def sinusoid_modes(xyz: np.ndarray, qdim: int, rng) -> np.ndarray:
     """u_a(x) = sum of 8 modes 0.05 sin(k.x + phi), k ~ U[-pi,pi]^3."""
     u = np.zeros((xyz.shape[0], qdim))
@@ -185,6 +212,68 @@ def make_case(case, seed):
     print(name, "ndof", info["n_dof"], "nnz", info["nnz"])
 
 
+def make_diff_case(case, seed):
+    """Energy and first derivatives (u and the coefficient declared as a
+    variable) of a potential, from the reference's own symbolic derivative."""
+    name, dim, gt, deg, qdim, im, nx, expr, gpu_expr, consts, varsd, jitter, ukind = case
+    import getfem_gb300 as g
+    rng = np.random.default_rng(seed)
+    kind = "simplex" if gt == "PK" else "hex"
+    h = 1.0 / nx
+    jit = rng.uniform(-0.1 * h, 0.1 * h, ((nx + 1) ** dim, dim)) if jitter else None
+    mesh = g.Mesh.regular_unit(dim, nx, kind, jitter=jit)
+    mf = g.MeshFem(mesh, qdim, degree=deg)
+    ndof, E = mf.nb_dof(), mesh.nb_convex()
+    inputs = {"u": (sinusoid_modes(mf.basic_dof_nodes(), qdim, rng) if ukind == "modes"
+                    else rng.standard_normal(ndof) * 0.1)}
+    for cname, ck in consts.items():
+        inputs[cname] = np.array([1.5])
+    for vname, vk in varsd.items():
+        n = E if vk == "P0" else ndof // qdim
+        sigma = 0.3 if vname == "mu" else 0.5
+        inputs[vname] = np.exp(rng.normal(0.0, sigma, n))
+    out = {}
+    for tag, ex, vars_, orders in (("ref", expr, varsd, "0,1"), ("builtin", gpu_expr, {}, "0")):
+        with tempfile.TemporaryDirectory() as td:
+            ind, outd = os.path.join(td, "in"), os.path.join(td, "out")
+            os.makedirs(ind)
+            os.makedirs(outd)
+            for k, v in inputs.items():
+                np.asarray(v, dtype=np.float64).tofile(os.path.join(ind, k + ".bin"))
+            if jit is not None:
+                jit.astype(np.float64).tofile(os.path.join(ind, "jitter.bin"))
+            cs = dict(consts)
+            if tag == "builtin":
+                cs.update(varsd)  # the coefficient as a constant
+            cmd = [DRIVER, f"dim={dim}", f"nx={nx}", f"gt={gt}", f"fem={deg}", f"qdim={qdim}",
+                   f"im={im}", f"in={ind}", f"out={outd}", f"expr={ex}", f"orders={orders}",
+                   f"jitter={1 if jit is not None else 0}",
+                   "consts=" + ",".join(f"{k}:{v}" for k, v in cs.items()),
+                   "vars=" + ",".join(f"{k}:{v}" for k, v in vars_.items())]
+            subprocess.run(cmd, check=True)
+            out[tag] = {fn[:-4]: np.fromfile(os.path.join(outd, fn))
+                        for fn in ("E.bin", "R.bin") if os.path.exists(os.path.join(outd, fn))}
+    E_ref, E_bi = float(out["ref"]["E"][0]), float(out["builtin"]["E"][0])
+    assert abs(E_ref - E_bi) <= 1e-13 * abs(E_bi), (name, E_ref, E_bi)
+    V = out["ref"]["R"]
+    rec = {"E": np.array([E_ref]), "E_builtin": np.array([E_bi]), "dE_du": V[:ndof]}
+    off = ndof
+    for vname in varsd:
+        n = inputs[vname].size
+        rec["dE_d" + vname] = V[off:off + n]
+        off += n
+    assert off == V.size
+    for k, v in inputs.items():
+        rec["in_" + k] = np.asarray(v, dtype=np.float64)
+    if jit is not None:
+        rec["jitter"] = jit
+    meta = dict(name=name, dim=dim, gt=gt, degree=deg, qdim=qdim, im=im, nx=nx, expr=expr,
+                gpu_expr=gpu_expr, consts=consts, vars=varsd, n_dof=ndof, seed=seed)
+    rec["meta"] = np.array(json.dumps(meta))
+    np.savez_compressed(os.path.join(OUT, name + ".npz"), **rec)
+    print(name, "E", E_ref, "vars", list(varsd))
+
+
 def make_condensed_case(case, seed):
     """The reference's assembly(1, true) and assembly(2, true) over a model
     holding u and the internal variable p (ref_driver internal=p)."""
@@ -246,7 +335,7 @@ def make_condensed_case(case, seed):
 
 def main():
     if not os.path.exists(DRIVER):
-        sys.exit(f"{DRIVER} missing: make -C oracle/refbuild REF=/root/reference")
+        sys.exit(f"{DRIVER} missing: build it with make -C oracle/refbuild")
     only = set(sys.argv[1:])  # optional: names of the fixtures to (re)make
     for i, case in enumerate(CASES):
         if not only or case[0] in only:
@@ -254,6 +343,9 @@ def main():
     for i, case in enumerate(CONDENSE_CASES):
         if not only or case[0] in only:
             make_condensed_case(case, 2000 + i)
+    for i, case in enumerate(DIFF_CASES):
+        if not only or case[0] in only:
+            make_diff_case(case, 4000 + i)
 
 
 if __name__ == "__main__":

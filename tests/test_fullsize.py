@@ -28,26 +28,32 @@ from common import (RTOL, assert_fullsize, assert_same_pattern, fullsize_report,
 NH = "((Id(meshdim)+Grad_u)*(Compressible_Neo_Hookean_PK2(Grad_u,[0.5*mu;D1]))):Grad_Test_u"
 
 
-def build_full(name):
+def build_full(name, inputs=None):
     """Mesh, MeshFem, MeshIm and GaWorkspace of a full-size case with the
-    benchmark's inputs (the generators of bench.py)."""
+    benchmark's inputs (the generators of bench.py); `inputs`, when given,
+    receives the generated arrays under the fixture's names."""
+    inputs = {} if inputs is None else inputs
     if name == "full_p1tri_poisson_64":
         mesh = g.Mesh.regular_unit(2, 64, "simplex")
         mf = g.MeshFem(mesh, 1, degree=1)
         mim = g.MeshIm(mesh, "IM_TRIANGLE(2)")
+        inputs.update(u=np.zeros(mf.nb_dof()), f=bench.poisson_inputs(mf.nb_dof()))
         ws = g.GaWorkspace()
-        ws.add_fem_variable("u", mf, U=np.zeros(mf.nb_dof()))
-        ws.add_fem_constant("f", mf, bench.poisson_inputs(mf.nb_dof()))
+        ws.add_fem_variable("u", mf, U=inputs["u"])
+        ws.add_fem_constant("f", mf, inputs["f"])
         ws.add_expression("Grad_u.Grad_Test_u - f*Test_u", mim)
         return mesh, mf, mim, ws
     if name == "full_p2tet_elastic_40":
-        mesh, mf, mim, ws, _ = bench.make_problem(40)
+        mesh, mf, mim, ws, d = bench.make_problem(40)
+        jit, _ = bench.p2tet_inputs(40)
+        inputs.update(u=d["u"], **{"lambda": d["lam"]}, mu=d["mu"], f=d["f"], jitter=jit)
         return mesh, mf, mim, ws
     if name == "full_q2hex_neohookean_32":
         mesh = g.Mesh.regular_unit(3, 32, "hex")
         mf = g.MeshFem(mesh, 3, degree=2)
         mim = g.MeshIm(mesh, "IM_GAUSS_PARALLELEPIPED(3,5)")
         u, mu = bench.neohookean_inputs(mf.basic_dof_nodes(), mesh.nb_convex())
+        inputs.update(u=u, mu=mu, D1=np.array([1.5]))
         ws = g.GaWorkspace()
         ws.add_fem_variable("u", mf, U=u)
         ws.add_fem_constant("mu", g.MeshFem(mesh, 1, degree=0), mu)
@@ -59,12 +65,21 @@ def build_full(name):
         mf = g.MeshFem(mesh, 1, degree=4)
         mim = g.MeshIm(mesh, "IM_GAUSS_PARALLELEPIPED(3,9)")
         kappa, u = bench.q4_inputs(mesh.nb_convex(), mf.nb_dof())
+        inputs.update(u=u, kappa=kappa)
         ws = g.GaWorkspace()
         ws.add_fem_variable("u", mf, U=u)
         ws.add_fem_constant("kappa", g.MeshFem(mesh, 1, degree=0), kappa)
         ws.add_expression("kappa*Grad_u.Grad_Test_u", mim)
         return mesh, mf, mim, ws
     raise KeyError(name)
+
+
+def assert_same_inputs(rec, inputs):
+    """The generated inputs are those the reference assembled (same bits)."""
+    import hashlib
+    for k, h in rec["meta"]["input_sha256"].items():
+        got = hashlib.sha256(np.ascontiguousarray(inputs[k], dtype="<f8").tobytes()).hexdigest()
+        assert got == h, f"input {k} differs from the fixture's (the generator gave other bits)"
 
 
 NAMES = ["full_p1tri_poisson_64", "full_q4hex_laplace_8", "full_q2hex_neohookean_32",
@@ -83,7 +98,9 @@ def _oracle(mesh, mf, mim, ws, nthreads):
 def test_oracle_matches_reference_at_full_size(name):
     """The oracle is pinned at the configurations' sizes too."""
     rec = load(name)
-    mesh, mf, mim, ws = build_full(name)
+    inputs = {}
+    mesh, mf, mim, ws = build_full(name, inputs)
+    assert_same_inputs(rec, inputs)
     assert mf.nb_dof() == rec["meta"]["n_dof"]
     K, R = _oracle(mesh, mf, mim, ws, os.cpu_count() or 1)
     assert_fullsize(fullsize_report(rec, K.indptr, K.indices, K.data, R))
@@ -93,7 +110,9 @@ def test_oracle_matches_reference_at_full_size(name):
 @pytest.mark.parametrize("name", NAMES)
 def test_gpu_matches_reference_and_oracle_at_full_size(name):
     rec = load(name)
-    mesh, mf, mim, ws = build_full(name)
+    inputs = {}
+    mesh, mf, mim, ws = build_full(name, inputs)
+    assert_same_inputs(rec, inputs)
     ws.assembly(2)
     K = ws.assembled_matrix()
     ws.assembly(1)
