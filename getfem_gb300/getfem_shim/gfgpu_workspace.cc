@@ -29,13 +29,17 @@
 // and the coefficients) are copied to the plan at every call.  GPU calls are
 // serialised by a mutex (OpenMP threads of model::assembly each hold their
 // own plan).
+#include <array>
+#include <cmath>
 #include <cstring>
+#include <iostream>
 #include <map>
 #include <memory>
 #include <mutex>
 #include <sstream>
 
 #include "getfem/getfem_generic_assembly.h"
+#include "getfem/getfem_integration.h"
 #include "getfem/getfem_models.h"
 #include "gfgpu_getfem.h"
 
@@ -58,14 +62,82 @@ void check(int rc, const char *what) {
     throw gmm::gmm_error(std::string("gfgpu: ") + what + ": " + gfgpu_last_error());
 }
 
-// "FEM_PK(3,2)" -> kind, degree
-void fem_kind(const std::string &name, int &kind, int &degree, int dim) {
-  int d = 0, k = 0;
-  if (std::sscanf(name.c_str(), "FEM_PK(%d,%d)", &d, &k) == 2) kind = GFGPU_SIMPLEX;
-  else if (std::sscanf(name.c_str(), "FEM_QK(%d,%d)", &d, &k) == 2) kind = GFGPU_HEX;
-  else throw gmm::gmm_error("gfgpu: finite element " + name + " not lowered");
-  if (d != dim) throw gmm::gmm_error("gfgpu: finite element " + name + " of another dimension");
-  degree = k;
+// Element types are identified by structure, not by name: GetFEM's names of
+// finite elements and integration methods live in per-thread naming
+// systems, and inside model::assembly's OpenMP section a worker thread sees
+// FEM_QK(3,2) as FEM_PRODUCT(FEM_PRODUCT(FEM_PK(1,2),...)).
+
+// The Lagrange nodes of FEM_PK(dim,K) / FEM_QK(dim,K) in GetFEM's order
+// (lattice points, first coordinate fastest; for PK those of sum <= K).
+std::vector<std::array<double, 3>> lattice_nodes(int dim, int kind, int K) {
+  std::vector<std::array<double, 3>> out;
+  const int n2 = dim == 3 ? K : 0;
+  for (int k = 0; k <= n2; ++k)
+    for (int j = 0; j <= K; ++j)
+      for (int i = 0; i <= K; ++i) {
+        if (kind == GFGPU_SIMPLEX && i + j + k > K) continue;
+        out.push_back({double(i) / K, double(j) / K, dim == 3 ? double(k) / K : 0.0});
+      }
+  return out;
+}
+
+// kind and degree of a Lagrange FEM_PK / FEM_QK element, by its node count
+// and node positions
+void fem_kind(getfem::pfem pf, bgeot::size_type cv, int dim, int &kind, int &degree) {
+  GMM_ASSERT1(int(pf->dim()) == dim && pf->target_dim() == 1 && pf->is_lagrange() &&
+                  pf->is_equivalent() && pf->is_polynomial(),
+              "gfgpu: finite element not lowered (a scalar Lagrange FEM_PK / FEM_QK is needed)");
+  const size_t nb = pf->nb_dof(cv), nv = pf->basic_structure(cv)->nb_points();
+  kind = nv == size_t(dim + 1) ? GFGPU_SIMPLEX : nv == (size_t(1) << dim) ? GFGPU_HEX : -1;
+  GMM_ASSERT1(kind >= 0, "gfgpu: element shape not lowered");
+  degree = -1;
+  for (int K = 1; K <= 6 && degree < 0; ++K) {
+    const auto nodes = lattice_nodes(dim, kind, K);
+    if (nodes.size() != nb) continue;
+    bool same = true;
+    for (size_t i = 0; i < nb && same; ++i) {
+      const bgeot::base_node &x = pf->node_of_dof(cv, i);
+      for (int d = 0; d < dim; ++d) same &= std::fabs(x[d] - nodes[i][d]) < 1e-12;
+    }
+    GMM_ASSERT1(same, "gfgpu: finite element with another node order");
+    degree = K;
+  }
+  GMM_ASSERT1(degree > 0, "gfgpu: finite element degree not lowered");
+}
+
+// the name of the integration method for the C ABI: the candidate whose
+// points and weights (gfgpu_quadrature) are those of the method
+std::string im_name(getfem::pintegration_method pim, int dim, int kind) {
+  GMM_ASSERT1(pim->type() == getfem::IM_APPROX, "gfgpu: exact integration is not lowered");
+  const getfem::papprox_integration pai = pim->approx_method();
+  const size_t nq = pai->nb_points_on_convex();
+  std::vector<std::string> cands;
+  char buf[64];
+  if (kind == GFGPU_HEX) {
+    for (int k = 1; k <= 31; k += 2) {
+      std::snprintf(buf, sizeof buf, "IM_GAUSS_PARALLELEPIPED(%d,%d)", dim, k);
+      cands.push_back(buf);
+    }
+  } else {
+    for (int k = 1; k <= 20; ++k) {
+      std::snprintf(buf, sizeof buf, dim == 2 ? "IM_TRIANGLE(%d)" : "IM_TETRAHEDRON(%d)", k);
+      cands.push_back(buf);
+    }
+  }
+  for (const std::string &c : cands) {
+    int32_t d = 0, n = 0;
+    if (gfgpu_quadrature(c.c_str(), &d, &n, nullptr, nullptr) != GFGPU_OK) continue;
+    if (d != dim || size_t(n) != nq) continue;
+    std::vector<double> pts(static_cast<size_t>(n) * dim), w(static_cast<size_t>(n));
+    if (gfgpu_quadrature(c.c_str(), &d, &n, pts.data(), w.data()) != GFGPU_OK) continue;
+    bool same = true;
+    for (size_t q = 0; q < nq && same; ++q) {
+      same &= std::fabs(w[q] - pai->coeff(q)) < 1e-14;
+      for (int k = 0; k < dim; ++k) same &= std::fabs(pts[q * dim + k] - pai->point(q)[k]) < 1e-14;
+    }
+    if (same) return c;
+  }
+  throw gmm::gmm_error("gfgpu: integration method not lowered");
 }
 
 uint64_t fnv(const void *p, size_t n, uint64_t h = 1469598103934665603ull) {
@@ -103,21 +175,28 @@ PlanEntry &plan_for(const getfem::ga_workspace &ws, const Lowered &L) {
   std::string im;
   std::vector<int64_t> cvpts, dofs;
   size_t nbg = 0, nb = 0;
+  getfem::pfem pf0 = nullptr;
+  getfem::pintegration_method pim0 = nullptr;
+  bgeot::pgeometric_trans pgt0 = nullptr;
   for (bgeot::size_type cv : cvs) {
-    int k, deg;
-    fem_kind(getfem::name_of_fem(mf.fem_of_element(cv)), k, deg, dim);
-    const std::string imn = getfem::name_of_int_method(L.mim->int_method_of_element(cv));
-    if (kind < 0) {
-      kind = k;
-      degree = deg;
-      im = imn;
+    // one finite element, integration method and geometric transformation
+    // per region (identified once, compared by pointer afterwards)
+    getfem::pfem pf = mf.fem_of_element(cv);
+    getfem::pintegration_method pim = L.mim->int_method_of_element(cv);
+    bgeot::pgeometric_trans pgt = m.trans_of_convex(cv);
+    if (!pf0) {
+      pf0 = pf;
+      pim0 = pim;
+      pgt0 = pgt;
+      fem_kind(pf, cv, dim, kind, degree);
+      im = im_name(pim, dim, kind);
+      // the geometric transformation of a degree-1 simplex or hexahedron
+      GMM_ASSERT1(pgt->nb_points() == (kind == GFGPU_SIMPLEX ? size_t(dim + 1) : size_t(1) << dim) &&
+                      pgt->dim() == bgeot::dim_type(dim),
+                  "gfgpu: geometric transformation not lowered (GT_PK(dim,1) / GT_QK(dim,1))");
     }
-    GMM_ASSERT1(k == kind && deg == degree && imn == im,
+    GMM_ASSERT1(pf == pf0 && pim == pim0 && pgt == pgt0,
                 "gfgpu: one element type, finite element and integration method per region");
-    const std::string gt = bgeot::name_of_geometric_trans(m.trans_of_convex(cv));
-    char want[64];
-    std::snprintf(want, sizeof want, "GT_%s(%d,1)", kind == GFGPU_SIMPLEX ? "PK" : "QK", dim);
-    GMM_ASSERT1(gt == want, "gfgpu: geometric transformation " << gt << " not lowered");
     const auto &P = m.ind_points_of_convex(cv);
     const auto &D = mf.ind_scalar_basic_dof_of_element(cv);
     if (!nbg) nbg = P.size(), nb = D.size();
@@ -271,8 +350,16 @@ void ga_workspace::assembly(size_type order, bool condensation) {
   if (order == 0) assemb_t.adjust_sizes(bgeot::multi_index());
   gmm::clear(assemb_t.as_vector());
   double pot = 0.0;
-  gfgpu_getfem::assemble(*this, order, order == 2 ? K.get() : nullptr,
-                         order == 1 ? V.get() : nullptr, &pot);
+  try {
+    gfgpu_getfem::assemble(*this, order, order == 2 ? K.get() : nullptr,
+                           order == 1 ? V.get() : nullptr, &pot);
+  } catch (const std::exception &e) {
+    // inside model::assembly's OpenMP section GetFEM rethrows a thread's
+    // exception from a destructor, which ends the program without the
+    // message: say it here first
+    std::cerr << "ga_workspace::assembly(" << order << "): " << e.what() << std::endl;
+    throw;
+  }
   if (order == 0) assemb_t[0] += pot;
 }
 

@@ -230,7 +230,8 @@ def test_dropin_workspace_assembly_matches_reference(name):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["p2tet_elastic", "q2hex_neohookean"])
+@pytest.mark.parametrize("name", ["p2tet_elastic", "q2hex_neohookean", "q4hex_laplace",
+                                  "q1hex_nodal_kappa"])
 def test_dropin_model_assembly_with_threads_matches_reference(name):
     """model::assembly(BUILD_ALL) with 4 OpenMP threads: each thread's
     workspace assembles its partition of the mesh on the GPU; the model sums
