@@ -621,6 +621,8 @@ def main():
     ap.add_argument("--ref-nx", type=int, default=12)
     ap.add_argument("--cpu-nx", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="keep the default launch configuration (no gfgpu_tune)")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the secondary workloads (neo-Hookean, batched, Q4, CG)")
     ap.add_argument("--secondary", choices=["neohookean", "q4", "batched", "cg"],
@@ -666,6 +668,13 @@ def main():
     nr, nnz = C.c_int64(), C.c_int64()
     L.check(lib.gfgpu_pattern_size(h, C.byref(nr), C.byref(nnz)))
     nnz = nnz.value
+    # launch configuration: the autotuner's choice for this element family
+    # (same bits for every candidate), picked before the warm-up
+    launch = L.Launch()
+    if args.no_tune:
+        L.check(lib.gfgpu_get_launch(h, C.byref(launch)))
+    else:
+        L.check(lib.gfgpu_tune(h, 3, C.byref(launch)))
     for _ in range(args.warmup):
         L.check(lib.gfgpu_assemble(h, 2, flags, None))
     L.check(lib.gfgpu_sync(h))
@@ -818,7 +827,10 @@ def main():
         "data": "synthetic (seeded jittered mesh, lognormal coefficients, N(0,1) load)",
         "config": dict(workload_config(args.nx, E, mf.nb_dof(), nnz),
                        l2="inputs larger than L2 (K values, scratch and DOF data >> 129 MB)",
-                       dofs_per_s=value * mf.nb_dof() / E),
+                       dofs_per_s=value * mf.nb_dof() / E,
+                       launch={"ep_threads_per_element": launch.ep_threads,
+                               "gather_warps_per_block": launch.gather_warps,
+                               "autotuned": not args.no_tune}),
         "kernels_ms": {"element_pass": float(kt[0]), "row_gather": float(kt[1])},
         "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": dom_gbs,
                      "peak": hbm_peak, "unit": "GB/s", "frac": dom_gbs / hbm_peak,

@@ -68,6 +68,12 @@ class Space(C.Structure):
                 ("dofs", C.POINTER(C.c_int64))]
 
 
+class Launch(C.Structure):
+    """gfgpu_launch: threads per element of the element pass, warps per
+    block of the row gather."""
+    _fields_ = [("ep_threads", C.c_int32), ("gather_warps", C.c_int32)]
+
+
 class NoallocArgs(C.Structure):
     _fields_ = [("dim", C.c_int32), ("degree", C.c_int32), ("qdim", C.c_int32),
                 ("im", C.c_char_p), ("n_elements", C.c_int64), ("n_nodes", C.c_int64),
@@ -110,6 +116,11 @@ _PROTOS = {
     "gfgpu_assemble": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_double)]),
     "gfgpu_assemble_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "gfgpu_assemble_host_upper": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "gfgpu_get_launch": (C.c_int, [C.c_void_p, C.POINTER(Launch)]),
+    "gfgpu_set_launch": (C.c_int, [C.c_void_p, C.POINTER(Launch)]),
+    "gfgpu_tune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(Launch)]),
+    "gfgpu_tune_save": (C.c_int, [C.c_char_p]),
+    "gfgpu_tune_load": (C.c_int, [C.c_char_p]),
     "gfgpu_pattern_upper": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.c_void_p,
                                       C.c_void_p]),
     "gfgpu_sync": (C.c_int, [C.c_void_p]),

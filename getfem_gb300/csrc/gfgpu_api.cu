@@ -1,6 +1,9 @@
 // C ABI of the device plans: creation (upload of the discretisation,
 // node adjacency, tables), data slots, assembly and result access.
 #include <cub/cub.cuh>
+#include <cstdio>
+#include <mutex>
+#include <map>
 
 #include <algorithm>
 #include <cstring>
@@ -311,6 +314,43 @@ int check_err(Plan &P, bool repair = false) {
 
 // The parallelepiped kernels of a plan need parallelepipeds: after
 // gfgpu_set_points moved the vertices off them, orders 1 and 2 fail loudly.
+// ------------------------------------------------- launch configurations
+
+std::mutex g_tune_mutex;
+std::map<std::string, LaunchConfig> g_tuned;  // family|GPU -> configuration
+
+std::string gpu_name() {
+  int dev = 0;
+  cudaDeviceProp prop;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&prop, dev) != cudaSuccess)
+    return "unknown";
+  std::string n(prop.name);
+  for (char &c : n)
+    if (c == ' ' || c == '|') c = '_';
+  return n;
+}
+
+// the kernels a plan's K pass runs: element kind and degree, components,
+// Gauss points, which element kernel
+std::string family_key(const Plan &P) {
+  std::string k = P.affine_simplex ? "simplex" : P.affine_hex ? "parallelepiped" : "gauss";
+  k += "-d" + std::to_string(P.dim) + "-k" + std::to_string(P.kind) + "-p" +
+       std::to_string(P.degree) + "-q" + std::to_string(P.qdim) + "-nq" + std::to_string(P.nq) +
+       "-law" + std::to_string(P.law);
+  return k + "|" + gpu_name();
+}
+
+std::vector<int> ep_candidates(const Plan &P) {
+  if (P.affine_simplex) return {2, 4, 8};
+  return {128, 256, 512};
+}
+
+void recorded_launch(Plan &P) {
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  auto it = g_tuned.find(family_key(P));
+  if (it != g_tuned.end()) P.tune = it->second;
+}
+
 int check_geometry(const Plan &P) {
   if (P.affine_hex && !P.parallelepiped) {
     set_last_error("the mesh points set by gfgpu_set_points no longer form parallelepipeds, "
@@ -456,6 +496,11 @@ int gfgpu_plan_create(const gfgpu_space *space, const gfgpu_form *form, void *cu
       delete P;
       return GFGPU_E_UNSUPPORTED;
     }
+    // launch configuration: the family's default, or the one recorded by
+    // gfgpu_tune / gfgpu_tune_load for this family on this GPU model
+    P->tune.ep_threads = P->affine_simplex ? 4 : 256;
+    P->tune.gather_warps = 4;
+    recorded_launch(*P);
     const int64_t E = S.n_elements, nb = P->nb, nbg = P->nbg;
     // validate and convert indices
     std::vector<int32_t> cv(size_t(E * nbg)), en(size_t(E * nb));
@@ -1354,6 +1399,130 @@ int gfgpu_device_vector(gfgpu_plan *P, double **vec) {
 }
 
 int64_t gfgpu_launch_count(gfgpu_plan *P) { return P ? P->launches : -1; }
+
+int gfgpu_get_launch(gfgpu_plan *P, gfgpu_launch *l) {
+  if (!P || !l) return GFGPU_E_INVALID;
+  l->ep_threads = P->tune.ep_threads;
+  l->gather_warps = P->tune.gather_warps;
+  return GFGPU_OK;
+}
+
+int gfgpu_set_launch(gfgpu_plan *P, const gfgpu_launch *l) {
+  if (!P || !l) return GFGPU_E_INVALID;
+  const auto eps = ep_candidates(*P);
+  const bool ep_ok = std::find(eps.begin(), eps.end(), l->ep_threads) != eps.end();
+  const bool gw_ok = l->gather_warps == 2 || l->gather_warps == 4 || l->gather_warps == 8;
+  if (!ep_ok || !gw_ok) {
+    set_last_error("gfgpu_set_launch: ep_threads " + std::to_string(l->ep_threads) +
+                   " / gather_warps " + std::to_string(l->gather_warps) +
+                   " is not a candidate of this plan's kernels");
+    return GFGPU_E_INVALID;
+  }
+  P->tune.ep_threads = l->ep_threads;
+  P->tune.gather_warps = l->gather_warps;
+  return GFGPU_OK;
+}
+
+int gfgpu_tune(gfgpu_plan *P, int32_t reps, gfgpu_launch *best) {
+  if (!P || reps < 1) return GFGPU_E_INVALID;
+  if (!P->kmat) {
+    set_last_error("gfgpu_tune: the plan has no element-matrix kernel");
+    return GFGPU_E_UNSUPPORTED;
+  }
+  int rc;
+  const int flags = GFGPU_WITH_VECTOR | (P->ip_term >= 0 ? GFGPU_CONDENSATION : 0);
+  if (P->nnz < 0 && (rc = gfgpu_assemble(P, 2, flags, nullptr))) return rc;
+  if ((rc = check_err(*P, true))) return rc;
+  // median over reps of the element-pass (w = 0) or gather (w = 1) time
+  auto time_of = [&](int w, float &med) -> int {
+    std::vector<float> t;
+    for (int r = 0; r <= reps; ++r) {  // the first run warms up
+      int rc2 = gfgpu_assemble(P, 2, flags | GFGPU_PROFILE, nullptr);
+      if (rc2) return rc2;
+      float k[2];
+      if ((rc2 = gfgpu_kernel_times(P, k, 2))) return rc2;
+      if (r) t.push_back(k[w]);
+    }
+    if ((rc = check_err(*P, true))) return rc;
+    std::sort(t.begin(), t.end());
+    med = t[t.size() / 2];
+    return GFGPU_OK;
+  };
+  float bt = 0.0f;
+  int be = P->tune.ep_threads;
+  for (int ep : ep_candidates(*P)) {
+    P->tune.ep_threads = ep;
+    float m;
+    if ((rc = time_of(0, m))) return rc;
+    if (ep == ep_candidates(*P)[0] || m < bt) bt = m, be = ep;
+  }
+  P->tune.ep_threads = be;
+  int bg = P->tune.gather_warps;
+  for (int gw : {2, 4, 8}) {
+    P->tune.gather_warps = gw;
+    float m;
+    if ((rc = time_of(1, m))) return rc;
+    if (gw == 2 || m < bt) bt = m, bg = gw;
+  }
+  P->tune.gather_warps = bg;
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    g_tuned[family_key(*P)] = P->tune;
+  }
+  if (best) {
+    best->ep_threads = P->tune.ep_threads;
+    best->gather_warps = P->tune.gather_warps;
+  }
+  return GFGPU_OK;
+}
+
+int gfgpu_tune_save(const char *path) {
+  if (!path) return GFGPU_E_INVALID;
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  FILE *f = std::fopen(path, "w");
+  if (!f) {
+    set_last_error(std::string("gfgpu_tune_save: cannot write ") + path);
+    return GFGPU_E_INVALID;
+  }
+  for (const auto &kv : g_tuned)
+    std::fprintf(f, "%s %d %d\n", kv.first.c_str(), kv.second.ep_threads, kv.second.gather_warps);
+  std::fclose(f);
+  return GFGPU_OK;
+}
+
+int gfgpu_tune_load(const char *path) {
+  if (!path) return GFGPU_E_INVALID;
+  FILE *f = std::fopen(path, "r");
+  if (!f) {
+    set_last_error(std::string("gfgpu_tune_load: cannot read ") + path);
+    return GFGPU_E_INVALID;
+  }
+  std::map<std::string, LaunchConfig> got;
+  char key[512];
+  int ep = 0, gw = 0, n = 0;
+  while ((n = std::fscanf(f, "%511s %d %d", key, &ep, &gw)) == 3) {
+    const bool ok = (ep == 2 || ep == 4 || ep == 8 || ep == 128 || ep == 256 || ep == 512) &&
+                    (gw == 2 || gw == 4 || gw == 8);
+    if (!ok) {
+      std::fclose(f);
+      set_last_error(std::string("gfgpu_tune_load: bad configuration for ") + key);
+      return GFGPU_E_INVALID;
+    }
+    LaunchConfig c;
+    c.ep_threads = ep;
+    c.gather_warps = gw;
+    got[key] = c;
+  }
+  const bool bad = n != EOF;
+  std::fclose(f);
+  if (bad) {
+    set_last_error(std::string("gfgpu_tune_load: malformed line in ") + path);
+    return GFGPU_E_INVALID;
+  }
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  for (const auto &kv : got) g_tuned[kv.first] = kv.second;
+  return GFGPU_OK;
+}
 
 int gfgpu_kernel_times(gfgpu_plan *P, float *times, int32_t n) {
   if (!P || !times || n < 2) return GFGPU_E_INVALID;

@@ -87,8 +87,10 @@ __device__ __forceinline__ void parallelepiped_geometry(int lane, int64_t e,
   __syncwarp();
 }
 
-template <int NB, bool WANT_K>
-__global__ void __launch_bounds__(kAffThreads) affine_hex_kernel(
+// T threads per element (the CTA of the element); every entry and row is
+// computed by one thread in the same order whatever T is (same bits).
+template <int NB, bool WANT_K, int T = kAffThreads>
+__global__ void __launch_bounds__(T) affine_hex_kernel(
     int64_t E, const double *__restrict__ pts, const int32_t *__restrict__ cv,
     const int32_t *__restrict__ enode, const double *__restrict__ tabs,
     const int32_t *__restrict__ tri, const double *__restrict__ ggrad0, KeLayout L,
@@ -106,7 +108,7 @@ __global__ void __launch_bounds__(kAffThreads) affine_hex_kernel(
   int src_slot = -1;
   for (int t = 0; t < form.n_terms; ++t)
     if (form.terms[t].kind == GFGPU_TERM_SOURCE) src_slot = form.terms[t].field_slot;
-  for (int j = tid; j < NB; j += kAffThreads) {
+  for (int j = tid; j < NB; j += T) {
     const int32_t n = enode[e * NB + j];
     us[j] = u ? u[n] : 0.0;
     fs[j] = src_slot >= 0 ? slots.p[src_slot][n] : 0.0;
@@ -118,16 +120,16 @@ __global__ void __launch_bounds__(kAffThreads) affine_hex_kernel(
       const double J = geo[24];
       double c1 = 0.0, cm = 0.0, csrc = 0.0;
       for (int t = 0; t < form.n_terms; ++t) {
-        const gfgpu_term &T = form.terms[t];
+        const gfgpu_term &Tm = form.terms[t];
         auto val = [&](const gfgpu_coef &c) {
           if (c.kind == GFGPU_COEF_CONST) return c.value;
           if (c.kind == GFGPU_COEF_ELEMENT) return c.value * slots.p[c.slot][e];
           return 0.0;
         };
-        if (T.kind == GFGPU_TERM_GRADGRAD) c1 += T.scale * val(T.c[1]);
-        else if (T.kind == GFGPU_TERM_MASS) cm += T.scale * val(T.c[0]);
-        else if (T.kind == GFGPU_TERM_SOURCE)
-          csrc += T.scale * (T.c[0].kind == GFGPU_COEF_NONE ? 1.0 : val(T.c[0]));
+        if (Tm.kind == GFGPU_TERM_GRADGRAD) c1 += Tm.scale * val(Tm.c[1]);
+        else if (Tm.kind == GFGPU_TERM_MASS) cm += Tm.scale * val(Tm.c[0]);
+        else if (Tm.kind == GFGPU_TERM_SOURCE)
+          csrc += Tm.scale * (Tm.c[0].kind == GFGPU_COEF_NONE ? 1.0 : val(Tm.c[0]));
       }
       const double cJ = c1 * J;
       for (int k = 0; k < 6; ++k) cp[k] = cJ * geo[18 + k];
@@ -142,7 +144,7 @@ __global__ void __launch_bounds__(kAffThreads) affine_hex_kernel(
   double *o = out + e * L.stride;
   if constexpr (WANT_K) {
     unsigned long long mx = 0ull;
-    for (int ent = tid; ent < NT; ent += kAffThreads) {
+    for (int ent = tid; ent < NT; ent += T) {
       const int rc = tri[ent];
       const int r = rc >> 16, col = rc & 0xffff;
       const int idx = r * NB + col;
@@ -163,7 +165,7 @@ __global__ void __launch_bounds__(kAffThreads) affine_hex_kernel(
   // r walks column r instead: the loads coalesce across threads and no warp
   // reduction is needed (one FMA per entry; the butterfly of a warp per row
   // cost more FP64 instructions than the row's FMAs).
-  for (int r = tid; r < NB; r += kAffThreads) {
+  for (int r = tid; r < NB; r += T) {
     double s = 0.0, sf = 0.0;
     for (int col = 0; col < NB; ++col) {
       const int idx = col * NB + r;
@@ -540,12 +542,17 @@ cudaError_t launch_affine_hex_pass(Plan &P, bool want_K) {
     P.launches++;
     return cudaGetLastError();
   }
+  // the K pass with the plan's threads per element (autotuned)
+  const int tk = P.tune.ep_threads;
+#define AFFK(NB, TT)                                                                           \
+  affine_hex_kernel<NB, true, TT><<<grid, TT, 0, P.stream>>>(                                  \
+      P.n_elements, P.d_points, P.d_cv, P.d_enode, P.d_aff, P.d_tri, P.d_ggrad, P.lay, P.form, \
+      sp, P.d_elem, P.d_err)
 #define AFF(NB)                                                                                \
   do {                                                                                         \
-    if (want_K)                                                                                \
-      affine_hex_kernel<NB, true><<<grid, kAffThreads, 0, P.stream>>>(                          \
-          P.n_elements, P.d_points, P.d_cv, P.d_enode, P.d_aff, P.d_tri, P.d_ggrad, P.lay,     \
-          P.form, sp, P.d_elem, P.d_err);                                                      \
+    if (want_K && tk == 128) AFFK(NB, 128);                                                    \
+    else if (want_K && tk == 512) AFFK(NB, 512);                                               \
+    else if (want_K) AFFK(NB, 256);                                                            \
     else                                                                                       \
       affine_hex_kernel<NB, false><<<grid, kAffThreads, 0, P.stream>>>(                         \
           P.n_elements, P.d_points, P.d_cv, P.d_enode, P.d_aff, P.d_tri, P.d_ggrad, P.lay,     \
@@ -559,6 +566,7 @@ cudaError_t launch_affine_hex_pass(Plan &P, bool want_K) {
     default: return cudaErrorInvalidValue;
   }
 #undef AFF
+#undef AFFK
   P.launches++;
   return cudaGetLastError();
 }

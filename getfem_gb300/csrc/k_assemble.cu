@@ -212,7 +212,7 @@ __host__ __device__ __forceinline__ size_t gather_warp_bytes(int ms, int qd, int
 // The row gather of one DOF node by one warp (QD components, R =
 // ceil(nb*qd/32) lane rounds over the columns of a row); `base` is the
 // warp's shared-memory area of gather_warp_bytes(ms, QD, rowblk, mad).
-template <int QD, int R>
+template <int QD, int R, bool UP = false>
 __device__ __forceinline__ void gather_node(
     char *base, int64_t node, const KeLayout &L, const int32_t *__restrict__ adj_ptr,
     const int32_t *__restrict__ adj, const double *__restrict__ elem, int ms, int mad,
@@ -382,7 +382,7 @@ __device__ __forceinline__ void gather_node(
       // upper-triangle output: entry k of the row (k >= skip[row], the
       // first column >= row) goes to up.vals[up.rowptr[row] + k - skip]
       int64_t ub = 0, ustart = 0, uend = 0;
-      if (up.vals) {
+      if constexpr (UP) {
         ustart = up.rowptr[row];
         ub = ustart - up.skip[row];
         uend = up.rowptr[row + 1];
@@ -402,7 +402,7 @@ __device__ __forceinline__ void gather_node(
           for (int b = 0; b < QD; ++b)
             if (m & (1u << (a * QD + b))) {
               const double x = acc[(j * QD + a) * QD + b];
-              if (!up.vals) {
+              if constexpr (!UP) {
                 if (q < pend) vals[q] = x;
                 else set_err(err, ERR_CAPACITY);
               } else {
@@ -428,8 +428,11 @@ __device__ __forceinline__ void gather_node(
 
 // Warps take the nodes i0, i0 + 1, ... < i1 of `order` (or the nodes i
 // themselves when order is null).
-template <int QD, int R>
-__global__ void __launch_bounds__(128) gather_kernel(
+// BW: the largest block (warps) the instance is compiled for; the register
+// budget follows it (a 4-warp instance keeps the budget that lets 10
+// blocks of the common buckets share an SM)
+template <int QD, int R, bool UP = false, int BW = 4>
+__global__ void __launch_bounds__(32 * BW) gather_kernel(
     int64_t i0, int64_t i1, const int32_t *__restrict__ order, KeLayout L,
     const int32_t *__restrict__ adj_ptr, const int32_t *__restrict__ adj,
     const double *__restrict__ elem, int ms, int mad, const int64_t *__restrict__ nptr,
@@ -443,8 +446,8 @@ __global__ void __launch_bounds__(128) gather_kernel(
   const int64_t i = i0 + blockIdx.x * int64_t(blockDim.x >> 5) + wib;
   if (i >= i1) return;
   const int64_t node = order ? int64_t(order[i]) : i;
-  gather_node<QD, R>(base, node, L, adj_ptr, adj, elem, ms, mad, nptr, nbits, slotmap, rowptr,
-                     vals, want_K, want_R, vec, err, ncol, u, up);
+  gather_node<QD, R, UP>(base, node, L, adj_ptr, adj, elem, ms, mad, nptr, nbits, slotmap, rowptr,
+                         vals, want_K, want_R, vec, err, ncol, u, up);
 }
 
 // Upper-triangle pattern of a CSR with sorted columns: skip[r] = number of
@@ -544,12 +547,25 @@ int pattern_cap(const Plan &P) {
   return np;
 }
 
-template <int QD, int R>
-cudaError_t launch_gather_t(Plan &P, bool want_K, bool want_R, int64_t i0, int64_t i1,
-                            const int32_t *order, int ms, int mad) {
+template <int QD, int R, bool UP>
+cudaError_t launch_gather_tu(Plan &P, bool want_K, bool want_R, int64_t i0, int64_t i1,
+                             const int32_t *order, int ms, int mad) {
   ms = ms < 1 ? 1 : ms;
   mad = mad < 1 ? 1 : mad;
-  const size_t smem = size_t(kWarpsPerBlock) * gather_warp_bytes(ms, QD, P.lay.rowblk, mad);
+  // warps per block: the plan's (autotuned), fewer when the block would
+  // exceed the shared memory of an SM
+  static int smem_max = 0;
+  if (!smem_max) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) !=
+        cudaSuccess)
+      smem_max = 48 * 1024;
+  }
+  const size_t wb = gather_warp_bytes(ms, QD, P.lay.rowblk, mad);
+  int warps = P.tune.gather_warps;
+  while (warps > 1 && size_t(warps) * wb > size_t(smem_max)) warps /= 2;
+  const size_t smem = size_t(warps) * wb;
   // the dynamic shared-memory limit of this instantiation, raised only when
   // a launch needs more (per device; a host call between launches otherwise)
   static std::atomic<int> limit[16];
@@ -557,8 +573,11 @@ cudaError_t launch_gather_t(Plan &P, bool want_K, bool want_R, int64_t i0, int64
   cudaError_t ce = cudaGetDevice(&dev);
   if (ce != cudaSuccess) return ce;
   if (dev < 0 || dev >= 16 || int(smem) > limit[dev].load()) {
-    ce = cudaFuncSetAttribute(gather_kernel<QD, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              int(smem));
+    ce = cudaFuncSetAttribute(gather_kernel<QD, R, UP, 4>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (ce != cudaSuccess) return ce;
+    ce = cudaFuncSetAttribute(gather_kernel<QD, R, UP, 8>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (ce != cudaSuccess) return ce;
     if (dev >= 0 && dev < 16) {
       int cur = limit[dev].load();
@@ -567,14 +586,24 @@ cudaError_t launch_gather_t(Plan &P, bool want_K, bool want_R, int64_t i0, int64
     }
   }
   if (i1 <= i0) return cudaSuccess;
-  const unsigned blocks = unsigned((i1 - i0 + kWarpsPerBlock - 1) / kWarpsPerBlock);
-  gather_kernel<QD, R><<<blocks, kWarpsPerBlock * 32, smem, P.stream>>>(
+  const unsigned blocks = unsigned((i1 - i0 + warps - 1) / warps);
+  auto kern = warps > 4 ? gather_kernel<QD, R, UP, 8> : gather_kernel<QD, R, UP, 4>;
+  kern<<<blocks, warps * 32, smem, P.stream>>>(
       i0, i1, order, P.lay, P.d_adj_ptr, P.d_adj, P.d_elem, ms, mad, P.d_nptr, P.d_nbits,
       P.d_slotmap, P.d_rowptr, P.d_vals, want_K, want_R, P.d_vec, P.d_err,
       P.r_from_rows ? P.d_ncol : nullptr, P.slot_ptr[GFGPU_SLOT_U],
-      P.upper_out ? UpperOut{P.d_uvals, P.d_urowptr, P.d_uskip} : UpperOut{});
+      UP ? UpperOut{P.d_uvals, P.d_urowptr, P.d_uskip} : UpperOut{});
   P.launches++;
   return cudaGetLastError();
+}
+
+template <int QD, int R>
+cudaError_t launch_gather_t(Plan &P, bool want_K, bool want_R, int64_t i0, int64_t i1,
+                            const int32_t *order, int ms, int mad) {
+  // the upper-triangle output is a separate instance: the plain gather
+  // carries none of its work
+  if (P.upper_out) return launch_gather_tu<QD, R, true>(P, want_K, want_R, i0, i1, order, ms, mad);
+  return launch_gather_tu<QD, R, false>(P, want_K, want_R, i0, i1, order, ms, mad);
 }
 
 template <int QD>

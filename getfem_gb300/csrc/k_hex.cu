@@ -128,11 +128,13 @@ struct HexSmem {
   static constexpr size_t bytes = size_t(total) * 8;
   // phase B: the upper triangle of K_e (r <= c), entries dealt round-robin
   static constexpr int NT = S * (S + 1) / 2;
-  static constexpr int NE = (NT + kHexThreads - 1) / kHexThreads;
 };
 
-template <int QD, int NB, int NBG, int NQ, int LAW, bool WANT_K>
-__global__ void __launch_bounds__(kHexThreads, 2) hex_element_kernel(
+// T threads per element (the CTA of the element): every entry of K_e, every
+// Z product and every row of the residual is computed by one thread in the
+// same order whatever T is, so the results are the same bits for every T.
+template <int QD, int NB, int NBG, int NQ, int LAW, bool WANT_K, int T = kHexThreads>
+__global__ void __launch_bounds__(T, 512 / T) hex_element_kernel(
     int64_t E, const double *__restrict__ pts, const int32_t *__restrict__ cv,
     const int32_t *__restrict__ enode, const double *__restrict__ hval,
     const double *__restrict__ hgrad, const double *__restrict__ ggrad,
@@ -160,11 +162,11 @@ __global__ void __launch_bounds__(kHexThreads, 2) hex_element_kernel(
   if (tid == 0) smax = 0ull;
   __syncthreads();
   const double *u = slots.p[GFGPU_SLOT_U];
-  for (int c = tid; c < S; c += kHexThreads)
+  for (int c = tid; c < S; c += T)
     us[c] = u ? u[int64_t(ens[c / QD]) * QD + c % QD] : 0.0;
   __syncthreads();
   // ---------------------------------------------------------------- A1
-  for (int q = tid; q < NQ; q += kHexThreads) {
+  for (int q = tid; q < NQ; q += T) {
     double K[9];
 #pragma unroll
     for (int d = 0; d < 3; ++d)
@@ -275,17 +277,17 @@ __global__ void __launch_bounds__(kHexThreads, 2) hex_element_kernel(
       for (int a = 0; a < QD; ++a) div += Gu[a][a < 3 ? a : 0];
       rs[RDIV] = div;
       for (int t = 0; t < form.n_terms; ++t) {
-        const gfgpu_term &T = form.terms[t];
+        const gfgpu_term &Tm = form.terms[t];
         double *tv = rs + RTERM + 3 * t;
-        const double sc = T.scale;
-        if (T.kind == GFGPU_TERM_GRADGRAD) {
-          const double a0 = coef_at(T.c[0], slots, e, ens, phi, NB) * sc;
-          const double a1 = coef_at(T.c[1], slots, e, ens, phi, NB) * sc;
-          const double a2 = coef_at(T.c[2], slots, e, ens, phi, NB) * sc;
+        const double sc = Tm.scale;
+        if (Tm.kind == GFGPU_TERM_GRADGRAD) {
+          const double a0 = coef_at(Tm.c[0], slots, e, ens, phi, NB) * sc;
+          const double a1 = coef_at(Tm.c[1], slots, e, ens, phi, NB) * sc;
+          const double a2 = coef_at(Tm.c[2], slots, e, ens, phi, NB) * sc;
           tv[0] = a0, tv[1] = a1, tv[2] = a2;
           c0 += a0, c1 += a1, c2 += a2;
-        } else if (T.kind == GFGPU_TERM_MASS) {
-          const double a0 = coef_at(T.c[0], slots, e, ens, phi, NB) * sc;
+        } else if (Tm.kind == GFGPU_TERM_MASS) {
+          const double a0 = coef_at(Tm.c[0], slots, e, ens, phi, NB) * sc;
           cm += a0;
           double uq[QD];
 #pragma unroll
@@ -295,19 +297,19 @@ __global__ void __launch_bounds__(kHexThreads, 2) hex_element_kernel(
             for (int b = 0; b < QD; ++b) uq[b] += phi[j] * us[j * QD + b];
 #pragma unroll
           for (int b = 0; b < QD; ++b) tv[b] = a0 * uq[b];
-        } else if (T.kind == GFGPU_TERM_INTERNAL_P) {
+        } else if (Tm.kind == GFGPU_TERM_INTERNAL_P) {
           // the internal pressure at this Gauss point (im_data index e*NQ+q)
-          const double sp = coef_at(T.c[0], slots, e, ens, phi, NB);
-          const double kb = coef_at(T.c[1], slots, e, ens, phi, NB);
-          const double c3 = coef_at(T.c[2], slots, e, ens, phi, NB);
+          const double sp = coef_at(Tm.c[0], slots, e, ens, phi, NB);
+          const double kb = coef_at(Tm.c[1], slots, e, ens, phi, NB);
+          const double c3 = coef_at(Tm.c[2], slots, e, ens, phi, NB);
           const int64_t iq = e * NQ + q;
-          const double p = slots.p[T.field_slot][iq];
+          const double p = slots.p[Tm.field_slot][iq];
           if (cmode == 2) {
             // K_pp^-1, then KQJpr and RQpr as the reference forms them
             const double inv = 1.0 / (sc * (1.0 + c3 * (3.0 * (p * p))));
             if (!isfinite(inv)) set_err(err, ERR_NAN);
             const double kq = inv * (sc * kb);
-            const double rqpr = bad ? 0.0 : (inv * slots.p[T.aux_slot][iq]) / wJ;
+            const double rqpr = bad ? 0.0 : (inv * slots.p[Tm.aux_slot][iq]) / wJ;
             c0 += -(sp * kq);
             tv[0] = -(sp * rqpr);
             tv[1] = kq;
@@ -317,10 +319,10 @@ __global__ void __launch_bounds__(kHexThreads, 2) hex_element_kernel(
             tv[1] = 0.0;
             out_int[iq] = wJ * (sc * ((p + c3 * (p * p * p)) + kb * div));
           }
-        } else if (T.kind == GFGPU_TERM_SOURCE) {
+        } else if (Tm.kind == GFGPU_TERM_SOURCE) {
           const double a0 =
-              (T.c[0].kind == GFGPU_COEF_NONE ? 1.0 : coef_at(T.c[0], slots, e, ens, phi, NB)) * sc;
-          const double *f = slots.p[T.field_slot];
+              (Tm.c[0].kind == GFGPU_COEF_NONE ? 1.0 : coef_at(Tm.c[0], slots, e, ens, phi, NB)) * sc;
+          const double *f = slots.p[Tm.field_slot];
           double fv[QD];
 #pragma unroll
           for (int b = 0; b < QD; ++b) fv[b] = 0.0;
@@ -353,19 +355,19 @@ __global__ void __launch_bounds__(kHexThreads, 2) hex_element_kernel(
     // row entry (j, b) of point q is gq[q*S + j*3 + b]
     if (cmode == 2 && ipt >= 0) {
       double *ok = out_kqj + e * (NQ * S);
-      for (int z = tid; z < NQ * S; z += kHexThreads)
+      for (int z = tid; z < NQ * S; z += T)
         ok[z] = rq[(z / S) * kRes + RTERM + 3 * ipt + 1] * gq[z];
     }
   }
   if constexpr (LAW == LAW_NH && WANT_K) {
     // ---------------------------------------------------------------- A2
-    for (int z = tid; z < NQ * 81; z += kHexThreads) {
+    for (int z = tid; z < NQ * 81; z += T) {
       const int q = z / 81, r = z % 81;
       W[z] = nh_dsde(law + q * kLaw, r % 3, (r / 3) % 3, (r / 9) % 3, r / 27);
     }
     __syncthreads();
     // ---------------------------------------------------------------- A3
-    for (int z = tid; z < NQ * 81; z += kHexThreads) {
+    for (int z = tid; z < NQ * 81; z += T) {
       const int q = z / 81, r = z % 81, ak = r / 9, bl = r % 9;
       const int a = ak / 3, k = ak % 3, b = bl / 3, l = bl % 3;
       const double *st = law + q * kLaw;
@@ -388,12 +390,12 @@ __global__ void __launch_bounds__(kHexThreads, 2) hex_element_kernel(
     // K_e is symmetric (isotropic tangent; hyperelastic tangent): each thread
     // owns upper-triangle entries (r, c), r = i*QD + a <= c = j*QD + b, and
     // accumulates sum_k g_ik Z[(a,k), c] with Z = A g_j per Gauss point.
-    constexpr int NE = M::NE;
+    constexpr int NE = (M::NT + T - 1) / T;
     int goff[NE], zoff[NE];
     bool own[NE], dg[NE];
 #pragma unroll
     for (int k = 0; k < NE; ++k) {
-      const int ent = tid + kHexThreads * k;
+      const int ent = tid + T * k;
       own[k] = ent < M::NT;
       const int rc = own[k] ? tri[ent] : 0;
       const int r = rc >> 16, c = rc & 0xffff;
@@ -407,7 +409,7 @@ __global__ void __launch_bounds__(kHexThreads, 2) hex_element_kernel(
     constexpr int QG = M::kQG, NZ = NA * S;
     for (int q0 = 0; q0 < NQ; q0 += QG) {
       const int nqg = NQ - q0 < QG ? NQ - q0 : QG;
-      for (int z = tid; z < nqg * NZ; z += kHexThreads) {
+      for (int z = tid; z < nqg * NZ; z += T) {
         const int t = z / NZ, zz = z - t * NZ, q = q0 + t;
         const int ak = zz / S, cz = zz % S, j = cz / QD, b = cz % QD;
         const double *A = Aq + (q * NA + ak) * NA + b * 3;
@@ -435,7 +437,7 @@ __global__ void __launch_bounds__(kHexThreads, 2) hex_element_kernel(
 #pragma unroll
           for (int k = 0; k < NE; ++k) {
             if (own[k] && dg[k]) {
-              const int ent = tid + kHexThreads * k;
+              const int ent = tid + T * k;
               const int rc = tri[ent];
               acc[k] = fma(mqq * phi[(rc >> 16) / QD], phi[(rc & 0xffff) / QD], acc[k]);
             }
@@ -449,7 +451,7 @@ __global__ void __launch_bounds__(kHexThreads, 2) hex_element_kernel(
 #pragma unroll
     for (int k = 0; k < NE; ++k) {
       if (own[k]) {
-        const int rc = tri[tid + kHexThreads * k];
+        const int rc = tri[tid + T * k];
         const int r = rc >> 16, c = rc & 0xffff;
         o[r * L.rowstride + c] = acc[k];
         if (r != c) o[c * L.rowstride + r] = acc[k];
@@ -462,7 +464,7 @@ __global__ void __launch_bounds__(kHexThreads, 2) hex_element_kernel(
   // ---------------------------------------------------------------- C
   // R_e(i,a) = sum_q wJ_q t_q(i,a), t_q as the reference's exec loop forms
   // it (term by term, products and sums in its order)
-  for (int r = tid; r < S; r += kHexThreads) {
+  for (int r = tid; r < S; r += T) {
     const int i = r / QD, ra = r % QD;
     double s = 0.0;
     for (int q = 0; q < NQ; ++q) {
@@ -517,12 +519,18 @@ __global__ void __launch_bounds__(kHexThreads, 2) hex_element_kernel(
 template <int QD, int NB, int NBG, int NQ, int LAW>
 cudaError_t launch_hex_t(Plan &P, const SlotPtrs &sp, bool want_K) {
   using M = HexSmem<QD, NB, NBG, NQ, LAW>;
-  auto kern = want_K ? hex_element_kernel<QD, NB, NBG, NQ, LAW, true>
-                     : hex_element_kernel<QD, NB, NBG, NQ, LAW, false>;
+  // threads per element: the plan's (autotuned) for the K pass, the
+  // default for a vector-only pass
+  const int T = want_K ? P.tune.ep_threads : kHexThreads;
+  auto kern = !want_K ? hex_element_kernel<QD, NB, NBG, NQ, LAW, false>
+              : T == 128 ? hex_element_kernel<QD, NB, NBG, NQ, LAW, true, 128>
+              : T == 512 ? hex_element_kernel<QD, NB, NBG, NQ, LAW, true, 512>
+                         : hex_element_kernel<QD, NB, NBG, NQ, LAW, true, 256>;
+  const int threads = !want_K ? kHexThreads : (T == 128 || T == 512) ? T : 256;
   cudaError_t ce = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         int(M::bytes));
   if (ce != cudaSuccess) return ce;
-  kern<<<unsigned(P.n_elements), kHexThreads, M::bytes, P.stream>>>(
+  kern<<<unsigned(P.n_elements), threads, M::bytes, P.stream>>>(
       P.n_elements, P.d_points, P.d_cv, P.d_enode, P.d_hval, P.d_hgrad, P.d_ggrad, P.d_hw,
       P.d_tri, P.lay, P.form, sp, P.d_elem, P.d_err, P.ip_term, P.cmode, P.d_int, P.d_kqj);
   return cudaGetLastError();

@@ -75,7 +75,7 @@ __host__ __device__ constexpr int pk_sup_v(int dim, int nb, int i, int t) {
 // Shared memory of one 32-element tile of the simplex element pass (KU:
 // with the staging of u and of the warps' parts of K_e u_e, which a pass
 // leaving K u to the row gather does not reserve).
-template <int DIM, int QD, int NB, bool KU = true>
+template <int DIM, int QD, int NB, bool KU = true, int W = kEpWarps>
 struct EpShared {
   static constexpr int NV = DIM + 1, M = QD * NV, NTP = M * (M + 1) / 2;
   static constexpr int S = NB * QD;
@@ -90,23 +90,23 @@ struct EpShared {
       double Tp[NTP][32];         // upper triangle of T per element
       double Us[KU ? S : 1][32];  // u at the element's DOFs
     } a;                          // while the blocks of K_e are built
-    double Rs[KU ? kEpWarps : 1][KU ? S : 1][32];  // then: each warp's part of R_e
+    double Rs[KU ? W : 1][KU ? S : 1][32];  // then: each warp's part of R_e
   } x;
-  unsigned long long mxs[kEpWarps][32];
+  unsigned long long mxs[W][32];
 };
 
 // One tile (32 elements, 4 warps) of the element pass; every thread of the
 // block calls it (it synchronises the block).
 // KU: V_e holds K_e u_e + the load (else the load only: the fused K + R
 // assembly forms K u from the assembled rows in the row gather)
-template <int DIM, int QD, int NB, bool MASS, bool STORE_K, bool KU = true>
+template <int DIM, int QD, int NB, bool MASS, bool STORE_K, bool KU = true, int W = kEpWarps>
 __device__ __forceinline__ void simplex_element_tile(
-    EpShared<DIM, QD, NB, KU> &sh, int64_t tile, int64_t E, const double *__restrict__ pts,
+    EpShared<DIM, QD, NB, KU, W> &sh, int64_t tile, int64_t E, const double *__restrict__ pts,
     const int32_t *__restrict__ cv, const int32_t *__restrict__ enode,
     const SimplexTables *__restrict__ tab, const KeLayout &L, const gfgpu_form &form,
     const SlotPtrs &slots, const double *__restrict__ fsrc, double fscale,
     const double *__restrict__ u, double *__restrict__ out, int *__restrict__ err) {
-  using SH = EpShared<DIM, QD, NB, KU>;
+  using SH = EpShared<DIM, QD, NB, KU, W>;
   constexpr int NV = SH::NV, M = SH::M;
   constexpr int S = SH::S, RS = (S + 3) & ~3;
   auto &s_gval = sh.s_gval;
@@ -222,8 +222,8 @@ __device__ __forceinline__ void simplex_element_tile(
     const double Jc0 = Gs[SH::KX + 0][lane], Jc2 = Gs[SH::KX + 2][lane];
 #pragma unroll
     for (int p = 0; p < M; ++p) {
-      const int pos = p % kEpWarps;
-      if (((p / kEpWarps) & 1 ? kEpWarps - 1 - pos : pos) != wid) continue;  // warp-uniform
+      const int pos = p % W;
+      if (((p / W) & 1 ? W - 1 - pos : pos) != wid) continue;  // warp-uniform
       const int a = p / NV, v = p % NV;
       double s0 = 0.0, ub[QD];
       if constexpr (QD > 1) {
@@ -245,7 +245,7 @@ __device__ __forceinline__ void simplex_element_tile(
   __syncthreads();
   // ---- u at the element's DOFs
   if constexpr (KU) {
-    for (int j = wid; j < NB; j += kEpWarps) {
+    for (int j = wid; j < NB; j += W) {
       const int nd = active ? __ldg(enode + e * NB + j) : 0;
 #pragma unroll
       for (int b = 0; b < QD; ++b)
@@ -281,7 +281,7 @@ __device__ __forceinline__ void simplex_element_tile(
     // ---- scalar fields: warp w builds rows r = w, w + 4, ... in registers,
     // adds each into R_e = K_e u_e (no threshold, as the reference's vector
     // assembly) and writes it with 32-byte stores
-    for (int r = wid; r < S; r += kEpWarps) {
+    for (int r = wid; r < S; r += W) {
       const int i = r;
       double row[RS];
 #pragma unroll
@@ -338,7 +338,7 @@ __device__ __forceinline__ void simplex_element_tile(
     for (int i = 0; i < NB; ++i) {
 #pragma unroll
       for (int j = i; j < NB; ++j, ++pidx) {
-        if (pidx % kEpWarps != wid) continue;  // warp-uniform
+        if (pidx % W != wid) continue;  // warp-uniform
         const int pij = i * NB + j;
         const double mij = MASS ? cm * s_mass[pij] : 0.0;
         double B[QD][QD];
@@ -358,12 +358,13 @@ __device__ __forceinline__ void simplex_element_tile(
 #pragma unroll
             for (int a = 0; a < QD; ++a)
 #pragma unroll
-              for (int b = 0; b < QD; ++b) B[a][b] += gv * tp(a, v, b, w);
+              for (int b = 0; b < QD; ++b)
+                if (i != j || b >= a) B[a][b] += gv * tp(a, v, b, w);
           }
         }
-        // a diagonal block holds the same terms in another order below its
-        // diagonal: take the mirror of the upper entries (K_e symmetric bit
-        // for bit)
+        // a diagonal block would hold the same terms in another order below
+        // its diagonal: it takes the mirror of its upper entries instead (K_e
+        // symmetric bit for bit)
         if (i == j) {
 #pragma unroll
           for (int a = 0; a < QD; ++a)
@@ -407,11 +408,11 @@ __device__ __forceinline__ void simplex_element_tile(
       for (int c = 0; c < S; ++c) Rs[wid][c][lane] = Rp[c];
       __syncthreads();
     }
-    for (int r = wid; r < S; r += kEpWarps) {
+    for (int r = wid; r < S; r += W) {
       double rv = load_of(r / QD, r % QD);
       if constexpr (KU) {
 #pragma unroll
-        for (int k = 0; k < kEpWarps; ++k) rv += Rs[k][r][lane];
+        for (int k = 0; k < W; ++k) rv += Rs[k][r][lane];
       }
       if (active) o[L.off_vec + r] = rv;
     }
@@ -419,7 +420,7 @@ __device__ __forceinline__ void simplex_element_tile(
   if (wid == 0 && active) {
     unsigned long long m = mxs[0][lane];
 #pragma unroll
-    for (int k = 1; k < kEpWarps; ++k) m = mxs[k][lane] > m ? mxs[k][lane] : m;
+    for (int k = 1; k < W; ++k) m = mxs[k][lane] > m ? mxs[k][lane] : m;
     const double mxd = abs_of_key(m);
     if (!isfinite(mxd)) set_err(err, ERR_NAN);
     if (STORE_K) o[L.off_thr] = mxd * 1e-14;
@@ -430,16 +431,22 @@ __device__ __forceinline__ void simplex_element_tile(
 
 namespace {
 
-template <int DIM, int QD, int NB, bool MASS, bool STORE_K, bool KU>
-__global__ void __launch_bounds__(kEpThreads) simplex_element_pass(
+// W warps share the tile's 32 elements (W threads per element): the rows of
+// T and the node-pair blocks of K_e are dealt to the warps, each computed by
+// one warp whatever W is, so K_e and the loads are the same bits for every W
+// (the per-warp parts of K_e u_e of a KU pass are summed in warp order and
+// depend on W: KU passes keep the default)
+template <int DIM, int QD, int NB, bool MASS, bool STORE_K, bool KU, int W = kEpWarps>
+__global__ void __launch_bounds__(32 * W) simplex_element_pass(
     int64_t E, const double *__restrict__ pts, const int32_t *__restrict__ cv,
     const int32_t *__restrict__ enode, const SimplexTables *__restrict__ tab, KeLayout L,
     gfgpu_form form, SlotPtrs slots, const double *__restrict__ fsrc, double fscale,
     const double *__restrict__ u, double *__restrict__ out, int *__restrict__ err,
     int64_t tile0) {
-  __shared__ EpShared<DIM, QD, NB, KU> sh;
-  simplex_element_tile<DIM, QD, NB, MASS, STORE_K, KU>(sh, tile0 + blockIdx.x, E, pts, cv, enode,
-                                                   tab, L, form, slots, fsrc, fscale, u, out, err);
+  __shared__ EpShared<DIM, QD, NB, KU, W> sh;
+  simplex_element_tile<DIM, QD, NB, MASS, STORE_K, KU, W>(sh, tile0 + blockIdx.x, E, pts, cv,
+                                                      enode, tab, L, form, slots, fsrc, fscale, u,
+                                                      out, err);
 }
 
 }  // namespace
@@ -650,7 +657,6 @@ int build_simplex_tables(Plan &P, std::string &errmsg) {
 cudaError_t launch_simplex_element_pass(Plan &P, bool with_u, int64_t tile0, int64_t tile1,
                                         bool ku) {
   if (P.n_elements == 0) return cudaSuccess;
-  const int threads = kEpThreads;
   const int64_t ntiles = (P.n_elements + 31) / 32;  // 32 elements per block
   if (tile1 < 0 || tile1 > ntiles) tile1 = ntiles;
   if (tile1 <= tile0) return cudaSuccess;
@@ -668,16 +674,25 @@ cudaError_t launch_simplex_element_pass(Plan &P, bool with_u, int64_t tile0, int
     }
     if (T.kind == GFGPU_TERM_MASS) mass = true;
   }
-#define GFGPU_EP1(D, Q, N, MS, KUV)                                                            \
-  simplex_element_pass<D, Q, N, MS, true, KUV><<<blocks, threads, 0, P.stream>>>(              \
+#define GFGPU_EP1(D, Q, N, MS, KUV, WV)                                                        \
+  simplex_element_pass<D, Q, N, MS, true, KUV, WV><<<blocks, 32 * WV, 0, P.stream>>>(          \
       P.n_elements, P.d_points, P.d_cv, P.d_enode, P.d_stab, P.lay, P.form, sp, fsrc, fscale,   \
       with_u ? P.slot_ptr[GFGPU_SLOT_U] : nullptr, P.d_elem, P.d_err, tile0)
+  // the K pass runs with the plan's threads per element (autotuned); a KU
+  // pass with the default
+  const int w = ku ? kEpWarps : P.tune.ep_threads;
+#define GFGPU_EPW(D, Q, N, MS)                                                                 \
+  do {                                                                                         \
+    if (w == 2) GFGPU_EP1(D, Q, N, MS, false, 2);                                              \
+    else if (w == 8) GFGPU_EP1(D, Q, N, MS, false, 8);                                         \
+    else GFGPU_EP1(D, Q, N, MS, false, 4);                                                     \
+  } while (0)
 #define GFGPU_EP(D, Q, N)                                                                      \
   do {                                                                                         \
-    if (mass && ku) GFGPU_EP1(D, Q, N, true, true);                                            \
-    else if (mass) GFGPU_EP1(D, Q, N, true, false);                                            \
-    else if (ku) GFGPU_EP1(D, Q, N, false, true);                                              \
-    else GFGPU_EP1(D, Q, N, false, false);                                                     \
+    if (mass && ku) GFGPU_EP1(D, Q, N, true, true, 4);                                         \
+    else if (mass) GFGPU_EPW(D, Q, N, true);                                                   \
+    else if (ku) GFGPU_EP1(D, Q, N, false, true, 4);                                           \
+    else GFGPU_EPW(D, Q, N, false);                                                            \
   } while (0)
   const int d = P.dim, k = P.degree, q = P.qdim;
   if (d == 2 && k == 1 && q == 1) GFGPU_EP(2, 1, 3);
@@ -690,6 +705,7 @@ cudaError_t launch_simplex_element_pass(Plan &P, bool with_u, int64_t tile0, int
   else if (d == 3 && k == 2 && q == 3) GFGPU_EP(3, 3, 10);
   else return cudaErrorInvalidValue;
 #undef GFGPU_EP
+#undef GFGPU_EPW
 #undef GFGPU_EP1
   P.launches++;
   return cudaGetLastError();

@@ -91,7 +91,21 @@ enum : int {
 
 constexpr int kHostChunks = 16;  // gather chunks of gfgpu_assemble_host
 
+// Launch configuration of a plan's kernels (gfgpu_set_launch, gfgpu_tune).
+// ep_threads: threads per element of the element pass that stores K_e:
+// affine simplices 2, 4 or 8 (warps sharing a tile of 32 elements, one lane
+// per element in each), Gauss-point and parallelepiped hexahedra 128, 256
+// or 512 (the CTA of one element).  gather_warps: warps per block of the row
+// gather (one warp per DOF node), 2, 4 or 8.  Every choice computes each
+// entry with the same operations in the same order: the results are the
+// same bits.
+struct LaunchConfig {
+  int ep_threads = 0;
+  int gather_warps = 4;
+};
+
 struct Plan {
+  LaunchConfig tune;
   // discretisation
   int dim = 0, kind = 0, degree = 0, qdim = 0, nb = 0, nbg = 0, nq = 0;
   int64_t n_points = 0, n_elements = 0, n_dof = 0, n_nodes = 0;

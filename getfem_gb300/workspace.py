@@ -209,6 +209,25 @@ class GaWorkspace:
         g.order0 += low.order0
         return low.max_order
 
+    def tune(self, reps: int = 3):
+        """Autotunes the launch configuration (threads per element of the
+        element pass, warps per block of the row gather) of the K + R plan
+        of every group (gfgpu_tune) and returns {group index: (ep_threads,
+        gather_warps)}; later plans of the same element family on this GPU
+        model start with it.  Results are the same bits for every
+        configuration."""
+        lib = L.lib()
+        out = {}
+        for i, g in enumerate(self.groups):
+            if not g.order1:
+                continue
+            h = self._plan(g, g.order1)
+            self._upload(h, g.order1, need_u=True)
+            best = L.Launch()
+            L.check(lib.gfgpu_tune(h, int(reps), C.byref(best)))
+            out[i] = (best.ep_threads, best.gather_warps)
+        return out
+
     def clear_expressions(self):
         self._destroy()
         self.groups = []

@@ -455,6 +455,42 @@ typedef struct {
 int gfgpu_assemble_vector_noalloc(const gfgpu_noalloc_args *args, const gfgpu_form *form,
                                   void *cuda_stream);
 
+/* ------------------------------------------------------------------ */
+/* Launch configuration and autotuning.                                 */
+/* ------------------------------------------------------------------ */
+
+/* Threads per element of the element pass that stores K_e, and warps per
+   block of the row gather (one warp per DOF node).  Candidates:
+     ep_threads    affine simplices 2, 4, 8 (warps sharing a 32-element
+                   tile: that many threads per element); Gauss-point and
+                   parallelepiped hexahedra 128, 256, 512 (the CTA of one
+                   element);
+     gather_warps  2, 4, 8.
+   Every candidate computes each entry with the same operations in the same
+   order: K and R are the same bits whatever the configuration.  (The
+   reference has no launch configuration; ga_exec runs one element at a
+   time, compile_and_exec.cc:8750-8869.) */
+typedef struct {
+  int32_t ep_threads;
+  int32_t gather_warps;
+} gfgpu_launch;
+int gfgpu_get_launch(gfgpu_plan *plan, gfgpu_launch *launch);
+/* GFGPU_E_INVALID for a value that is not a candidate of the plan's kernels. */
+int gfgpu_set_launch(gfgpu_plan *plan, const gfgpu_launch *launch);
+/* Times every candidate on the plan's own order-2 assembly (K and R; the
+   pattern is built first if needed): the element-pass candidates, then the
+   gather candidates with the best element pass, `reps` profiled assemblies
+   each (median of the CUDA-event times).  Keeps the fastest in the plan,
+   records it for plans of the same family on this GPU model (element kind,
+   dimension, degree, qdim, kernel), and returns it in *best (may be NULL). */
+int gfgpu_tune(gfgpu_plan *plan, int32_t reps, gfgpu_launch *best);
+/* The recorded configurations: written to / read from a text file (one
+   line per family: "<family>|<GPU name> <ep_threads> <gather_warps>").
+   Plans created after gfgpu_tune_load (or a gfgpu_tune of the same family)
+   start with the recorded configuration. */
+int gfgpu_tune_save(const char *path);
+int gfgpu_tune_load(const char *path);
+
 /* Number of kernel launches issued by the plan since creation. */
 int64_t gfgpu_launch_count(gfgpu_plan *plan);
 
