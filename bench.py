@@ -621,6 +621,8 @@ def main():
     ap.add_argument("--ref-nx", type=int, default=12)
     ap.add_argument("--cpu-nx", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile-run", action="store_true",
+                    help="short run for profilers: the timed steps and one profiled step only")
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the default launch configuration (no gfgpu_tune)")
     ap.add_argument("--no-extra", action="store_true",
@@ -697,6 +699,20 @@ def main():
     launches = lib.gfgpu_launch_count(h) - launches0
     L.check(lib.gfgpu_sync(h))
     ms = e0.elapsed_time(e1) / args.steps
+
+    if args.profile_run:
+        # a short run for profilers (ncu launch lists and captures): the
+        # timed steps and one profiled step, nothing else
+        L.check(lib.gfgpu_assemble(h, 2, flags | L.PROFILE, None))
+        t = (C.c_float * 2)()
+        L.check(lib.gfgpu_kernel_times(h, t, 2))
+        L.check(lib.gfgpu_sync(h))
+        if rank == 0:
+            print(json.dumps({"profile_run": True, "workload": workload_config(args.nx, E, mf.nb_dof(), nnz),
+                              "ms_per_step": ms, "kernels_ms": {"element_pass": t[0],
+                                                                "row_gather": t[1]},
+                              "launch": [launch.ep_threads, launch.gather_warps]}), flush=True)
+        return
 
     # a longer run of the same step (about a second) with its own clock
     # record, for the steadiness of the figure above

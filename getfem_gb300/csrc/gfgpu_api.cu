@@ -1202,6 +1202,10 @@ namespace {
 // The host-buffer assembly of gfgpu_assemble_host (upper = false: the full
 // CSR values) and gfgpu_assemble_host_upper (upper = true: the values of
 // the entries with column >= row, in the order of gfgpu_pattern_upper).
+// the smallest element range of the chunked host-buffer assembly: 3 waves
+// of the simplex pass's blocks (152 SMs x 6 resident blocks of 32 elements)
+constexpr int64_t kMinRangeTiles = 3 * 152 * 6;
+
 int assemble_host(gfgpu_plan *P, const double *u, double *vals, double *vec, bool upper) {
   int rc;
   if (u && (rc = gfgpu_set_data(P, GFGPU_SLOT_U, u, P->n_dof, 0))) return rc;
@@ -1255,13 +1259,17 @@ int assemble_host(gfgpu_plan *P, const double *u, double *vals, double *vec, boo
   for (int c = 0; c < kHostChunks; ++c) {
     const int64_t n0 = P->n_nodes * c / kHostChunks, n1 = P->n_nodes * (c + 1) / kHostChunks;
     if (P->affine_simplex) {
-      const int64_t need = c == kHostChunks - 1 ? (P->n_elements + 31) / 32
-                                                : (P->h_chunk_eend[c] + 31) / 32;
+      const int64_t ntiles = (P->n_elements + 31) / 32;
+      const int64_t need = c == kHostChunks - 1 ? ntiles : (P->h_chunk_eend[c] + 31) / 32;
+      // each range launch covers at least kMinRangeTiles tiles (a few waves
+      // of blocks: a range of less than a wave leaves SMs idle), so it may
+      // run ahead of the next chunks' needs
       if (need > tiles_done) {
-        cudaError_t ce = launch_simplex_element_pass(*P, true, tiles_done, need, false);
+        const int64_t upto = std::min(ntiles, std::max(need, tiles_done + kMinRangeTiles));
+        cudaError_t ce = launch_simplex_element_pass(*P, true, tiles_done, upto, false);
         if (ce != cudaSuccess) P->upper_out = false;
         GF_CUDA(ce);
-        tiles_done = need;
+        tiles_done = upto;
       }
     }
     cudaError_t ce = launch_gather_chunk(*P, vec != nullptr, c);

@@ -358,14 +358,13 @@ __device__ __forceinline__ void simplex_element_tile(
 #pragma unroll
             for (int a = 0; a < QD; ++a)
 #pragma unroll
-              for (int b = 0; b < QD; ++b)
-                if (i != j || b >= a) B[a][b] += gv * tp(a, v, b, w);
+              for (int b = 0; b < QD; ++b) B[a][b] += gv * tp(a, v, b, w);
           }
         }
-        // a diagonal block would hold the same terms in another order below
-        // its diagonal: it takes the mirror of its upper entries instead (K_e
-        // symmetric bit for bit)
-        if (i == j) {
+        // a diagonal block holds the same terms in another order below its
+        // diagonal: it stores the mirror of its upper entries (K_e symmetric
+        // bit for bit)
+        if (i == j && L.mirror_diag) {
 #pragma unroll
           for (int a = 0; a < QD; ++a)
 #pragma unroll
@@ -557,6 +556,7 @@ int fill_simplex_tables(int dim, int K, int qdim, const std::string &im, Simplex
   lay.off_thr = lay.off_vec + lay.rowstride;
   lay.stride = lay.off_thr + 4;
   lay.linear = true;
+  lay.mirror_diag = true;
   return GFGPU_OK;
 }
 

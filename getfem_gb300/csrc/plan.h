@@ -67,6 +67,10 @@ struct KeLayout {
   int rowstride = 0, off_vec = 0, off_thr = 0, stride = 0;
   int blk = 0, rowblk = 0;
   bool linear = true;  // R = K_full u + sum V_e (else R = sum V_e)
+  // affine simplices: the diagonal node blocks of K_e store the mirror of
+  // their upper entries (K_e symmetric bit for bit).  A run-time flag on
+  // purpose: the block arithmetic stays that of every other block.
+  bool mirror_diag = false;
 };
 
 // offset of K_e[(li,a), c] (c = lj*qd + b) within the node row block of li
