@@ -1203,8 +1203,18 @@ namespace {
 // CSR values) and gfgpu_assemble_host_upper (upper = true: the values of
 // the entries with column >= row, in the order of gfgpu_pattern_upper).
 // the smallest element range of the chunked host-buffer assembly: 3 waves
-// of the simplex pass's blocks (152 SMs x 6 resident blocks of 32 elements)
-constexpr int64_t kMinRangeTiles = 3 * 152 * 6;
+// of the simplex pass's blocks (SMs x 6 resident blocks of 32 elements)
+int64_t min_range_tiles() {
+  static int64_t tiles = 0;
+  if (!tiles) {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      sms = 132;
+    tiles = int64_t(3) * 6 * sms;
+  }
+  return tiles;
+}
 
 int assemble_host(gfgpu_plan *P, const double *u, double *vals, double *vec, bool upper) {
   int rc;
@@ -1261,11 +1271,11 @@ int assemble_host(gfgpu_plan *P, const double *u, double *vals, double *vec, boo
     if (P->affine_simplex) {
       const int64_t ntiles = (P->n_elements + 31) / 32;
       const int64_t need = c == kHostChunks - 1 ? ntiles : (P->h_chunk_eend[c] + 31) / 32;
-      // each range launch covers at least kMinRangeTiles tiles (a few waves
+      // each range launch covers at least min_range_tiles() tiles (a few waves
       // of blocks: a range of less than a wave leaves SMs idle), so it may
       // run ahead of the next chunks' needs
       if (need > tiles_done) {
-        const int64_t upto = std::min(ntiles, std::max(need, tiles_done + kMinRangeTiles));
+        const int64_t upto = std::min(ntiles, std::max(need, tiles_done + min_range_tiles()));
         cudaError_t ce = launch_simplex_element_pass(*P, true, tiles_done, upto, false);
         if (ce != cudaSuccess) P->upper_out = false;
         GF_CUDA(ce);

@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(128) pattern_kernel(
       const int lj = c / qd, b = c % qd;
       unsigned m = 0u;
       for (int a = 0; a < qd; ++a)
-        if (abs_greater(Ke[int64_t(li) * L.rowblk + ke_in_rowblk(L, a, c)], thr))
+        if (abs_greater(Ke[int64_t(li) * L.rowblk + ke_sym_in_rowblk(L, li, a, c)], thr))
           m |= 1u << (a * qd + b);
       if (m) atomicOr(&bits[ljs[lj]], m);
     }
@@ -305,6 +305,9 @@ __device__ __forceinline__ void gather_node(
       const unsigned long long tb = abs_key(thr0);
       // the node's first element stores into the zeroed accumulators (an
       // element touches each accumulator once): no FP64 add for it
+      // a diagonal node block (lj == li) is read from its upper half, as
+      // ke_sym_in_rowblk reads it: K is symmetric bit for bit
+      const int li0 = adjl[k];
       auto add_block = [&](auto first) {
 #pragma unroll
         for (int r = 0; r < R; ++r) {
@@ -314,9 +317,13 @@ __device__ __forceinline__ void gather_node(
             const unsigned sb = sl0[r] >= 0 ? bits[sl0[r]] : 0u;
             const int c0 = L.blk ? (c / QD) * L.blk + b : c;
             const int cstep = L.blk ? QD : L.rowstride;
+            const bool dblk = L.blk && c / QD == li0;
 #pragma unroll
             for (int a = 0; a < QD; ++a) {
-              const double x = Kb[c0 + a * cstep];
+              // (a, b) of the block at c0 - b + a*QD + b; its mirror (b, a)
+              // at c0 - b + b*QD + a
+              const int off = (dblk && a > b) ? c0 - b + b * QD + a : c0 + a * cstep;
+              const double x = Kb[off];
               if (abs_greater(x, tb)) {
                 if ((sb >> (a * QD + b)) & 1u) {
                   double &dst = acc[(sl0[r] * QD + a) * QD + b];

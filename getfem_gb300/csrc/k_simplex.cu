@@ -361,15 +361,6 @@ __device__ __forceinline__ void simplex_element_tile(
               for (int b = 0; b < QD; ++b) B[a][b] += gv * tp(a, v, b, w);
           }
         }
-        // a diagonal block holds the same terms in another order below its
-        // diagonal: it stores the mirror of its upper entries (K_e symmetric
-        // bit for bit)
-        if (i == j && L.mirror_diag) {
-#pragma unroll
-          for (int a = 0; a < QD; ++a)
-#pragma unroll
-            for (int b = 0; b < a; ++b) B[a][b] = B[b][a];
-        }
 #pragma unroll
         for (int a = 0; a < QD; ++a)
 #pragma unroll
@@ -556,7 +547,6 @@ int fill_simplex_tables(int dim, int K, int qdim, const std::string &im, Simplex
   lay.off_thr = lay.off_vec + lay.rowstride;
   lay.stride = lay.off_thr + 4;
   lay.linear = true;
-  lay.mirror_diag = true;
   return GFGPU_OK;
 }
 

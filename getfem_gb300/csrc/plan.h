@@ -67,11 +67,20 @@ struct KeLayout {
   int rowstride = 0, off_vec = 0, off_thr = 0, stride = 0;
   int blk = 0, rowblk = 0;
   bool linear = true;  // R = K_full u + sum V_e (else R = sum V_e)
-  // affine simplices: the diagonal node blocks of K_e store the mirror of
-  // their upper entries (K_e symmetric bit for bit).  A run-time flag on
-  // purpose: the block arithmetic stays that of every other block.
-  bool mirror_diag = false;
 };
+
+// Offset of the entry (a, c = lj*qd + b) of local node li's rows that the
+// pattern build and the row gather use.  In the node-block layout a diagonal
+// node block (lj == li) is read from its upper half (a > b reads (b, a)): the
+// simplex pass computes its two halves as the same terms summed in another
+// order, and this makes every assembled K symmetric bit for bit.
+__host__ __device__ __forceinline__ int ke_sym_in_rowblk(const KeLayout &L, int li, int a, int c) {
+  if (L.blk) {
+    const int lj = c / L.qd, b = c % L.qd;
+    return lj * L.blk + ((lj == li && a > b) ? b * L.qd + a : a * L.qd + b);
+  }
+  return a * L.rowstride + c;
+}
 
 // offset of K_e[(li,a), c] (c = lj*qd + b) within the node row block of li
 __host__ __device__ __forceinline__ int ke_in_rowblk(const KeLayout &L, int a, int c) {
