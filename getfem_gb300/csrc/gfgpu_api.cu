@@ -739,10 +739,14 @@ void gfgpu_plan_destroy(gfgpu_plan *P) {
   for (int i = 0; i < GFGPU_MAX_SLOTS; ++i) dfree(P->slot_own[i]);
   for (int i = 0; i < 4; ++i)
     if (P->ev[i]) cudaEventDestroy(P->ev[i]);
-  for (int c = 0; c < kHostChunks; ++c)
+  for (int c = 0; c < kHostChunks; ++c) {
     if (P->chunk_ev[c]) cudaEventDestroy(P->chunk_ev[c]);
+    if (P->range_ev[c]) cudaEventDestroy(P->range_ev[c]);
+  }
   for (cudaStream_t cs : P->copy_stream)
     if (cs) cudaStreamDestroy(cs);
+  for (cudaStream_t gs : P->gather_stream)
+    if (gs) cudaStreamDestroy(gs);
   delete P;
 }
 
@@ -1199,10 +1203,7 @@ int gfgpu_sync(gfgpu_plan *P) {
 
 namespace {
 
-// The host-buffer assembly of gfgpu_assemble_host (upper = false: the full
-// CSR values) and gfgpu_assemble_host_upper (upper = true: the values of
-// the entries with column >= row, in the order of gfgpu_pattern_upper).
-// the smallest element range of the chunked host-buffer assembly: 3 waves
+// the smallest element range of the chunked host-buffer assembly: one wave
 // of the simplex pass's blocks (SMs x 6 resident blocks of 32 elements)
 int64_t min_range_tiles() {
   static int64_t tiles = 0;
@@ -1211,10 +1212,22 @@ int64_t min_range_tiles() {
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
       sms = 132;
-    tiles = int64_t(3) * 6 * sms;
+    tiles = int64_t(6) * sms;
   }
   return tiles;
 }
+
+// Launches made while it lives go to stream s instead of the plan's stream.
+struct StreamScope {
+  Plan &P;
+  cudaStream_t saved;
+  StreamScope(Plan &p, cudaStream_t s) : P(p), saved(p.stream) { P.stream = s; }
+  ~StreamScope() { P.stream = saved; }
+};
+
+// The host-buffer assembly of gfgpu_assemble_host (upper = false: the full
+// CSR values) and gfgpu_assemble_host_upper (upper = true: the values of
+// the entries with column >= row, in the order of gfgpu_pattern_upper).
 
 int assemble_host(gfgpu_plan *P, const double *u, double *vals, double *vec, bool upper) {
   int rc;
@@ -1245,21 +1258,32 @@ int assemble_host(gfgpu_plan *P, const double *u, double *vals, double *vec, boo
   const std::vector<int64_t> &hptr = upper ? P->h_urowptr : P->h_rowptr;
   double *dvals = upper ? P->d_uvals : P->d_vals;
   // The element pass, then the row gather in chunks of DOF nodes; the rows
-  // of each chunk (contiguous in the CSR) are copied to the host on a second
-  // stream while the next chunk is gathered.  (Writing the values from the
-  // gather straight into page-locked host memory was 2.5x slower: its
-  // stores are 8-byte scattered.)
+  // of each chunk (contiguous in the CSR) are copied to the host while the
+  // next chunks are gathered.  (Writing the values from the gather straight
+  // into page-locked host memory was 2.5x slower: its stores are 8-byte
+  // scattered.)
   if (!P->copy_stream[0]) {
-    // two copy streams (two copy engines), chunks alternating between them
+    // two copy streams (two copy engines), chunks alternating between them;
+    // gather streams at the device's highest priority
+    int prio_lo = 0, prio_hi = 0;
+    GF_CUDA(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
     GF_CUDA(cudaStreamCreateWithFlags(&P->copy_stream[0], cudaStreamNonBlocking));
     GF_CUDA(cudaStreamCreateWithFlags(&P->copy_stream[1], cudaStreamNonBlocking));
-    for (int c = 0; c < kHostChunks; ++c)
+    for (cudaStream_t &gs : P->gather_stream)
+      GF_CUDA(cudaStreamCreateWithPriority(&gs, cudaStreamNonBlocking, prio_hi));
+    for (int c = 0; c < kHostChunks; ++c) {
       GF_CUDA(cudaEventCreateWithFlags(&P->chunk_ev[c], cudaEventDisableTiming));
+      GF_CUDA(cudaEventCreateWithFlags(&P->range_ev[c], cudaEventDisableTiming));
+    }
   }
   GF_CUDA(cudaMemsetAsync(P->d_err, 0, sizeof(int), P->stream));
-  // Affine simplices: the element pass runs in element ranges, each just far
-  // enough for the next gather chunk (h_chunk_eend), so the copies of the
-  // first chunks overlap the element pass of the later ones.
+  // Affine simplices: the element pass runs on the plan's stream in element
+  // ranges, each far enough for the next gather chunk (h_chunk_eend).  Chunk
+  // c's gather waits for its range and runs on gather stream c % 3: the
+  // gathers' blocks take SMs ahead of the element pass's (priority), so the
+  // copies of the first chunks start early, and the three streams fill each
+  // other's launch tails.  Every chunk writes its own rows: the results do
+  // not depend on the order the streams run in.
   int64_t tiles_done = 0;
   P->r_from_rows = P->affine_simplex;
   if (P->affine_hex) GF_CUDA(launch_affine_hex_pass(*P, true));
@@ -1271,9 +1295,9 @@ int assemble_host(gfgpu_plan *P, const double *u, double *vals, double *vec, boo
     if (P->affine_simplex) {
       const int64_t ntiles = (P->n_elements + 31) / 32;
       const int64_t need = c == kHostChunks - 1 ? ntiles : (P->h_chunk_eend[c] + 31) / 32;
-      // each range launch covers at least min_range_tiles() tiles (a few waves
-      // of blocks: a range of less than a wave leaves SMs idle), so it may
-      // run ahead of the next chunks' needs
+      // each range launch covers at least min_range_tiles() tiles (a range
+      // of less than a wave leaves SMs idle), so it may run ahead of the
+      // next chunks' needs
       if (need > tiles_done) {
         const int64_t upto = std::min(ntiles, std::max(need, tiles_done + min_range_tiles()));
         cudaError_t ce = launch_simplex_element_pass(*P, true, tiles_done, upto, false);
@@ -1282,11 +1306,18 @@ int assemble_host(gfgpu_plan *P, const double *u, double *vals, double *vec, boo
         tiles_done = upto;
       }
     }
-    cudaError_t ce = launch_gather_chunk(*P, vec != nullptr, c);
+    cudaStream_t gs = P->gather_stream[c % kGatherStreams];
+    GF_CUDA(cudaEventRecord(P->range_ev[c], P->stream));
+    GF_CUDA(cudaStreamWaitEvent(gs, P->range_ev[c], 0));
+    cudaError_t ce;
+    {
+      StreamScope on_gs(*P, gs);
+      ce = launch_gather_chunk(*P, vec != nullptr, c);
+    }
     if (ce != cudaSuccess) P->upper_out = false;
     GF_CUDA(ce);
     cudaStream_t cs = P->copy_stream[c & 1];
-    GF_CUDA(cudaEventRecord(P->chunk_ev[c], P->stream));
+    GF_CUDA(cudaEventRecord(P->chunk_ev[c], gs));
     GF_CUDA(cudaStreamWaitEvent(cs, P->chunk_ev[c], 0));
     const int64_t r0 = hptr[size_t(n0 * qd)], r1 = hptr[size_t(n1 * qd)];
     if (r1 > r0)
@@ -1298,6 +1329,9 @@ int assemble_host(gfgpu_plan *P, const double *u, double *vals, double *vec, boo
                               cs));
   }
   P->upper_out = false;
+  // later work on the plan's stream follows every gather
+  for (int c = kHostChunks - kGatherStreams; c < kHostChunks; ++c)
+    GF_CUDA(cudaStreamWaitEvent(P->stream, P->chunk_ev[c], 0));
   GF_CUDA(cudaStreamSynchronize(P->copy_stream[0]));
   GF_CUDA(cudaStreamSynchronize(P->copy_stream[1]));
   P->last_want_R = vec != nullptr;

@@ -102,7 +102,8 @@ enum : int {
   LAW_NH = 1    // compressible neo-Hookean PK2 term
 };
 
-constexpr int kHostChunks = 16;  // gather chunks of gfgpu_assemble_host
+constexpr int kHostChunks = 16;    // gather chunks of gfgpu_assemble_host
+constexpr int kGatherStreams = 3;  // streams the chunks' gathers rotate over
 
 // Launch configuration of a plan's kernels (gfgpu_set_launch, gfgpu_tune).
 // ep_threads: threads per element of the element pass that stores K_e:
@@ -235,8 +236,13 @@ struct Plan {
   int32_t *d_corder = nullptr;
   std::vector<int32_t> h_corder;
   std::vector<int64_t> h_cbucket;
+  // gfgpu_assemble_host: the chunks' row gathers on kGatherStreams streams
+  // of the device's highest priority (their blocks go ahead of the element
+  // pass's ranges on the plan's stream), the copies on two copy streams
   cudaStream_t copy_stream[2] = {nullptr, nullptr};
+  cudaStream_t gather_stream[kGatherStreams] = {};
   cudaEvent_t chunk_ev[kHostChunks] = {};
+  cudaEvent_t range_ev[kHostChunks] = {};
   // upper triangle of a symmetric K (gfgpu_assemble_host_upper): row
   // pointers (device and host), the entries of each row left of its
   // diagonal, the values; built for the pattern of build number upper_build
