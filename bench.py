@@ -747,24 +747,31 @@ def main():
     nnz_u = C.c_int64()
     L.check(lib.gfgpu_pattern_upper(h, C.byref(nnz_u), None, None))
     nnz_u = nnz_u.value
-    e2e_steps = max(3, min(args.steps, 20))
+    # every call is synchronous (the values are in host memory when it
+    # returns); the figure is the mean over the steps, and the per-call
+    # median and maximum are reported beside it (single calls on the shared
+    # host occasionally take tens of ms)
+    e2e_steps = max(20, min(args.steps, 50))
 
     def host_loop(fn, out_h):
-        for _ in range(2):
+        for _ in range(3):
             L.check(fn(h, C.c_void_p(u_h.data_ptr()), C.c_void_p(out_h.data_ptr()),
                        C.c_void_p(vec_h.data_ptr())))
         barrier()
+        calls = []
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
+            tc = time.perf_counter()
             L.check(fn(h, C.c_void_p(u_h.data_ptr()), C.c_void_p(out_h.data_ptr()),
                        C.c_void_p(vec_h.data_ptr())))
+            calls.append(1e3 * (time.perf_counter() - tc))
         barrier()
-        return 1e3 * (time.perf_counter() - t0) / e2e_steps
+        return 1e3 * (time.perf_counter() - t0) / e2e_steps, calls
     vals_h = torch.empty(nnz, dtype=torch.float64).pin_memory()
-    e2e_full_ms = host_loop(lib.gfgpu_assemble_host, vals_h)
+    e2e_full_ms, full_calls = host_loop(lib.gfgpu_assemble_host, vals_h)
     del vals_h
     uvals_h = torch.empty(nnz_u, dtype=torch.float64).pin_memory()
-    e2e_ms = host_loop(lib.gfgpu_assemble_host_upper, uvals_h)
+    e2e_ms, upper_calls = host_loop(lib.gfgpu_assemble_host_upper, uvals_h)
     del uvals_h
 
     ms, e2e_ms, value, e2e = combine_ranks(dist, world, E, ms, e2e_ms, "cuda")
@@ -788,9 +795,10 @@ def main():
     names = ["element_pass", "row_gather"]
     dom = int(np.argmax(kt))
     dom_gbs = step_bytes / (kt[dom] * 1e-3) / 1e9
-    fp64_peak, dmma_peak = C.c_double(), C.c_double()
+    fp64_peak, dmma_peak, mixed_peak = C.c_double(), C.c_double(), C.c_double()
     L.check(lib.gfgpu_fp64_peak(0, C.byref(fp64_peak)))
     L.check(lib.gfgpu_fp64_peak(1, C.byref(dmma_peak)))
+    L.check(lib.gfgpu_fp64_peak(2, C.byref(mixed_peak)))
     # FP64 flops the element pass executes per element (from its loop
     # structure): the node-pair blocks i <= j of the symmetric K_e (2 per
     # reference-tensor term per component pair), the load term, T (a multiply
@@ -859,18 +867,23 @@ def main():
                  "peak_tflops": fp64_peak.value, "frac": ep_tflops / fp64_peak.value,
                  "flops_per_element": ep_flops,
                  "peak_source": "gfgpu_fp64_peak FMA microbenchmark, this run",
-                 "dmma_peak_tflops": dmma_peak.value},
+                 "dmma_peak_tflops": dmma_peak.value,
+                 "fma_and_dmma_warps_tflops": mixed_peak.value},
         "steady": {"steps": steady_steps, "ms_per_step": steady_ms,
                    "elements_per_s": E / (steady_ms * 1e-3), "clocks": steady.summary()},
         "step_hbm_frac": step_bytes / (ms * 1e-3) / 1e9 / hbm_peak,
         "e2e": {"value": e2e, "unit": "elements/s", "h2d_bytes_per_step": 8 * mf.nb_dof(),
                 "d2h_bytes_per_step": 8 * nnz_u + 8 * mf.nb_dof(), "ms_per_step": e2e_ms,
                 "api": "gfgpu_assemble_host_upper (u in; the upper triangle of the "
-                       "bit-symmetric K, nnz_upper values, and R out)", "nnz_upper": nnz_u},
+                       "bit-symmetric K, nnz_upper values, and R out)", "nnz_upper": nnz_u,
+                "steps": e2e_steps, "median_ms_per_call": float(np.median(upper_calls)),
+                "max_ms_per_call": float(np.max(upper_calls))},
         "e2e_full_values": {"value": world * E / (e2e_full_ms * 1e-3), "unit": "elements/s",
                             "h2d_bytes_per_step": 8 * mf.nb_dof(),
                             "d2h_bytes_per_step": 8 * nnz + 8 * mf.nb_dof(),
-                            "ms_per_step": e2e_full_ms, "api": "gfgpu_assemble_host"},
+                            "ms_per_step": e2e_full_ms, "api": "gfgpu_assemble_host",
+                            "median_ms_per_call": float(np.median(full_calls)),
+                            "max_ms_per_call": float(np.max(full_calls))},
         "gpu_launches": int(launches), "cpu_baseline": cpu, "clocks": sampler.summary(),
     }
     if not args.no_extra and world == 1:

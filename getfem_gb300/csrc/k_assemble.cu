@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(128) pattern_kernel(
       const int lj = c / qd, b = c % qd;
       unsigned m = 0u;
       for (int a = 0; a < qd; ++a)
-        if (abs_greater(Ke[int64_t(li) * L.rowblk + ke_sym_in_rowblk(L, li, a, c)], thr))
+        if (abs_greater(Ke[ke_sym_entry(L, li, a, c)], thr))
           m |= 1u << (a * qd + b);
       if (m) atomicOr(&bits[ljs[lj]], m);
     }
@@ -250,10 +250,37 @@ __device__ __forceinline__ void gather_node(
   }
   __syncwarp();
   const int nchunk = blk / 2;  // 16-byte chunks of the row block
+  // node blocks of kBlk doubles (the simplex pass's vector layouts, at most
+  // 64 chunks: nb <= 10 for 3 components): lane-invariant node block j and
+  // part of the lane's chunks lane and lane + 32
+  constexpr int kBlk = QD == 2 ? 4 : 12, kCpb = kBlk / 2;
+  static_assert(kMaxNb * 12 / 2 <= 2 * kWarp, "node-block row chunks exceed two per lane");
+  int cj[2], cpart[2];
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const int c = lane + kWarp * r;
+    cj[r] = c < nchunk ? c / kCpb : -1;
+    cpart[r] = c - (c / kCpb) * kCpb;
+  }
+  // the rows of local node li of element k into stage k % kGatherBufs: the
+  // contiguous row block (row layout), or its nb node blocks (li, j), those
+  // with j < li taken from the stored (j, li)
   auto issue = [&](int k) {
-    const double *src = elem + int64_t(adjs[k]) * L.stride + int64_t(adjl[k]) * blk;
+    const double *Ke = elem + int64_t(adjs[k]) * L.stride;
     double *dst = Kbuf + (k % kGatherBufs) * blk;
-    for (int c = lane; c < nchunk; c += kWarp) cp_async16(dst + 2 * c, src + 2 * c);
+    const int li = adjl[k];
+    if (L.blk) {
+#pragma unroll
+      for (int r = 0; r < 2; ++r) {
+        const int j = cj[r];
+        if (j < 0) continue;
+        const int lo = j < li ? j : li, hi = j < li ? li : j;
+        cp_async16(dst + 2 * (lane + kWarp * r), Ke + ke_block(nb, lo, hi) * kBlk + 2 * cpart[r]);
+      }
+    } else {
+      const double *src = Ke + int64_t(li) * blk;
+      for (int c = lane; c < nchunk; c += kWarp) cp_async16(dst + 2 * c, src + 2 * c);
+    }
   };
   // per-lane data of an element: slots of the columns the lane handles,
   // threshold, and the element vector entry of component `lane`
@@ -304,9 +331,10 @@ __device__ __forceinline__ void gather_node(
       const double *Kb = Kbuf + (k % kGatherBufs) * blk;
       const unsigned long long tb = abs_key(thr0);
       // the node's first element stores into the zeroed accumulators (an
-      // element touches each accumulator once): no FP64 add for it
-      // a diagonal node block (lj == li) is read from its upper half, as
-      // ke_sym_in_rowblk reads it: K is symmetric bit for bit
+      // element touches each accumulator once): no FP64 add for it.  Node
+      // blocks are read as ke_sym_entry reads them: a block (li, lj) with
+      // lj < li (staged from (lj, li)) transposed, a diagonal block from its
+      // upper half; K is symmetric bit for bit
       const int li0 = adjl[k];
       auto add_block = [&](auto first) {
 #pragma unroll
@@ -315,14 +343,15 @@ __device__ __forceinline__ void gather_node(
           if (c < S) {
             const int b = c % QD;
             const unsigned sb = sl0[r] >= 0 ? bits[sl0[r]] : 0u;
-            const int c0 = L.blk ? (c / QD) * L.blk + b : c;
+            const int lj = c / QD;
+            const int c0 = L.blk ? lj * L.blk + b : c;
             const int cstep = L.blk ? QD : L.rowstride;
-            const bool dblk = L.blk && c / QD == li0;
+            const bool lower = L.blk && lj < li0, dblk = L.blk && lj == li0;
 #pragma unroll
             for (int a = 0; a < QD; ++a) {
-              // (a, b) of the block at c0 - b + a*QD + b; its mirror (b, a)
-              // at c0 - b + b*QD + a
-              const int off = (dblk && a > b) ? c0 - b + b * QD + a : c0 + a * cstep;
+              // (a, b) of the block at c0 - b + a*QD + b; its transpose
+              // (b, a) at c0 - b + b*QD + a
+              const int off = (lower || (dblk && a > b)) ? c0 - b + b * QD + a : c0 + a * cstep;
               const double x = Kb[off];
               if (abs_greater(x, tb)) {
                 if ((sb >> (a * QD + b)) & 1u) {
@@ -436,10 +465,11 @@ __device__ __forceinline__ void gather_node(
 // Warps take the nodes i0, i0 + 1, ... < i1 of `order` (or the nodes i
 // themselves when order is null).
 // BW: the largest block (warps) the instance is compiled for; the register
-// budget follows it (a 4-warp instance keeps the budget that lets 10
-// blocks of the common buckets share an SM)
+// budget follows it: 40 resident warps per SM (10 blocks of 4 warps, the
+// shared-memory limit of the common buckets), 47 registers per thread, no
+// spills
 template <int QD, int R, bool UP = false, int BW = 4>
-__global__ void __launch_bounds__(32 * BW) gather_kernel(
+__global__ void __launch_bounds__(32 * BW, 40 / BW) gather_kernel(
     int64_t i0, int64_t i1, const int32_t *__restrict__ order, KeLayout L,
     const int32_t *__restrict__ adj_ptr, const int32_t *__restrict__ adj,
     const double *__restrict__ elem, int ms, int mad, const int64_t *__restrict__ nptr,

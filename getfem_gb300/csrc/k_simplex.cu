@@ -326,8 +326,8 @@ __device__ __forceinline__ void simplex_element_tile(
     // ---- vector fields: node pairs (i <= j) dealt round-robin to the 4
     // warps.  K_e is symmetric (G[i,j,v,w] = G[j,i,w,v], T symmetric), so
     // the block K_e[(i,.),(j,.)] = sum_t g_t T[(.,v_t),(.,w_t)] (+ mass) is
-    // computed once and stored with its transpose as whole 32-byte sectors
-    // (node-block layout); each warp accumulates its blocks' part of
+    // computed and stored once, as whole 32-byte sectors (upper node-block
+    // layout); each warp accumulates its blocks' part of
     // R_e = K_e u_e in registers, and the parts are summed in warp order.
     constexpr int BLK = QD == 2 ? 4 : 12;
     double Rp[S];
@@ -373,20 +373,15 @@ __device__ __forceinline__ void simplex_element_tile(
             mx = kv > mx ? kv : mx;
           }
         if (STORE_K && active) {
-          double4_32a *dij = reinterpret_cast<double4_32a *>(o + (i * NB + j) * BLK);
-          double4_32a *dji = reinterpret_cast<double4_32a *>(o + (j * NB + i) * BLK);
+          // upper node-block layout: block (i,j), i <= j, only (the row
+          // gather reads (j,i) as its transpose)
+          double4_32a *dij = reinterpret_cast<double4_32a *>(o + ke_block(NB, i, j) * BLK);
           if constexpr (QD == 2) {
             dij[0] = make_double4_32a(B[0][0], B[0][1], B[1][0], B[1][1]);
-            if (i != j) dji[0] = make_double4_32a(B[0][0], B[1][0], B[0][1], B[1][1]);
           } else {
             dij[0] = make_double4_32a(B[0][0], B[0][1], B[0][2], B[1][0]);
             dij[1] = make_double4_32a(B[1][1], B[1][2], B[2][0], B[2][1]);
             dij[2] = make_double4_32a(B[2][2], 0.0, 0.0, 0.0);
-            if (i != j) {
-              dji[0] = make_double4_32a(B[0][0], B[1][0], B[2][0], B[0][1]);
-              dji[1] = make_double4_32a(B[1][1], B[2][1], B[0][2], B[1][2]);
-              dji[2] = make_double4_32a(B[2][2], 0.0, 0.0, 0.0);
-            }
           }
         }
       }
@@ -543,7 +538,7 @@ int fill_simplex_tables(int dim, int K, int qdim, const std::string &im, Simplex
   lay.rowstride = (s + 3) & ~3;
   lay.blk = qd == 1 ? 0 : (qd == 2 ? 4 : 12);
   lay.rowblk = qd == 1 ? lay.rowstride : nb * lay.blk;
-  lay.off_vec = qd == 1 ? s * lay.rowstride : nb * nb * lay.blk;
+  lay.off_vec = qd == 1 ? s * lay.rowstride : (nb * (nb + 1) / 2) * lay.blk;
   lay.off_thr = lay.off_vec + lay.rowstride;
   lay.stride = lay.off_thr + 4;
   lay.linear = true;

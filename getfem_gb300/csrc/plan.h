@@ -56,12 +56,14 @@ struct UpperOut {
 // stride is even, so every element block and every row is 16-byte aligned.
 // Two layouts of K_e:
 //   rows (blk == 0): row (li,a) at (li*qd + a) * rowstride;
-//   node blocks (blk > 0, vector fields of the simplex pass): the qd x qd
-//         block of local nodes (i,j) at (i*nb + j) * blk, entry (a,b) at
-//         a*qd + b; blk = 4 (qd 2) or 12 (qd 3, 9 entries and 3 zeros), so
-//         every block is whole 32-byte sectors.
-// Either way the rows of local node li are the rowblk doubles at
-// li * rowblk.
+//   upper node blocks (blk > 0, vector fields of the simplex pass): K_e is
+//         symmetric and only its node blocks (i,j) with i <= j are stored,
+//         block (i,j) at ke_block(nb, i, j) * blk (row by row: (0,0) (0,1)
+//         .. (0,nb-1) (1,1) ..), entry (a,b) at a*qd + b; blk = 4 (qd 2) or
+//         12 (qd 3, 9 entries and 3 zeros), so every block is whole 32-byte
+//         sectors.  Block (i,j), i > j, is block (j,i) transposed.
+// rowblk: the doubles of one local node's rows (row layout) or of its nb
+// node blocks (node-block layout), the row gather's staging unit.
 struct KeLayout {
   int nb = 0, qd = 0, s = 0;
   int rowstride = 0, off_vec = 0, off_thr = 0, stride = 0;
@@ -69,22 +71,25 @@ struct KeLayout {
   bool linear = true;  // R = K_full u + sum V_e (else R = sum V_e)
 };
 
-// Offset of the entry (a, c = lj*qd + b) of local node li's rows that the
-// pattern build and the row gather use.  In the node-block layout a diagonal
-// node block (lj == li) is read from its upper half (a > b reads (b, a)): the
-// simplex pass computes its two halves as the same terms summed in another
-// order, and this makes every assembled K symmetric bit for bit.
-__host__ __device__ __forceinline__ int ke_sym_in_rowblk(const KeLayout &L, int li, int a, int c) {
-  if (L.blk) {
-    const int lj = c / L.qd, b = c % L.qd;
-    return lj * L.blk + ((lj == li && a > b) ? b * L.qd + a : a * L.qd + b);
-  }
-  return a * L.rowstride + c;
+// index of the stored node block (i,j), i <= j, of the upper node-block layout
+__host__ __device__ __forceinline__ int ke_block(int nb, int i, int j) {
+  return i * nb - (i * (i - 1)) / 2 + (j - i);
 }
 
-// offset of K_e[(li,a), c] (c = lj*qd + b) within the node row block of li
-__host__ __device__ __forceinline__ int ke_in_rowblk(const KeLayout &L, int a, int c) {
-  return L.blk ? (c / L.qd) * L.blk + a * L.qd + c % L.qd : a * L.rowstride + c;
+// Offset from the element's base of the entry K_e[(li,a), c] (c = lj*qd + b)
+// that the pattern build and the row gather use.  Node blocks: a block below
+// the diagonal is read transposed from its mirror, and a diagonal block
+// (lj == li) from its upper half (a > b reads (b, a)): the simplex pass
+// computes the two halves of a diagonal block as the same terms summed in
+// another order, and this makes every assembled K symmetric bit for bit.
+__host__ __device__ __forceinline__ int ke_sym_entry(const KeLayout &L, int li, int a, int c) {
+  if (L.blk) {
+    const int lj = c / L.qd, b = c % L.qd;
+    const bool tr = lj < li || (lj == li && a > b);
+    const int blk = lj < li ? ke_block(L.nb, lj, li) : ke_block(L.nb, li, lj);
+    return blk * L.blk + (tr ? b * L.qd + a : a * L.qd + b);
+  }
+  return li * L.rowblk + a * L.rowstride + c;
 }
 
 struct SlotPtrs {

@@ -386,8 +386,10 @@ int gfgpu_sync(gfgpu_plan *plan);
    pass, times[1] = row gather.  Waits for the stream. */
 int gfgpu_kernel_times(gfgpu_plan *plan, float *times, int32_t n);
 
-/* Throughput microbenchmark of this GPU's FP64 FMA pipe (kind 0) or FP64
-   tensor pipe (kind 1, mma.sync m8n8k4 f64), in TFLOP/s; used as the
+/* Throughput microbenchmark of this GPU's FP64 FMA pipe (kind 0), FP64
+   tensor pipe (kind 1, mma.sync m8n8k4 f64), or both at once (kind 2: half
+   the warps on each; near the sum of the two when they do not share issue
+   resources, near either alone when they do), in TFLOP/s; used as the
    compute roofline of the FP64 kernels. */
 int gfgpu_fp64_peak(int32_t kind, double *tflops);
 
