@@ -408,6 +408,133 @@ __global__ void __launch_bounds__(kGpWarps * 32) gauss_potential_kernel(
   }
 }
 
+// Potentials and element-coefficient derivatives (modes 0 and 1) of scalar
+// isotropic forms on parallelepiped hexahedra, kEw elements per warp: the
+// per-point reference gradients Gr(m) = sum_j u_j dphi_j/dxi_m of the warp's
+// elements share every table load (one load feeds kEw FMAs; with one element
+// per warp the kernel waited on those loads), and each element's sums are
+// formed with the same operations in the same order as
+// gauss_potential_kernel's (the same bits).  Forms with GRADGRAD terms only,
+// coefficients constant or per element.
+constexpr int kEw = 4;
+
+template <int NB>
+__global__ void __launch_bounds__(kGpWarps * 32) affine_scalar_potential_kernel(
+    int64_t E, int nq, int mode, int wslot, const double *__restrict__ pts,
+    const int32_t *__restrict__ cv, const int32_t *__restrict__ enode,
+    const double *__restrict__ hgradT, const double *__restrict__ ggrad,
+    const double *__restrict__ hw, gfgpu_form form, SlotPtrs slots, double *__restrict__ out_e,
+    int *__restrict__ err) {
+  constexpr int DIM = 3, NBG = 8;
+  __shared__ double us_all[kGpWarps][NB][kEw];
+  __shared__ double B_all[kGpWarps][kEw][9];
+  __shared__ double det_all[kGpWarps][kEw];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t e0 = (int64_t(blockIdx.x) * kGpWarps + w) * kEw;
+  if (e0 >= E) return;
+  const int ne = E - e0 < kEw ? int(E - e0) : kEw;
+  double(*us)[kEw] = us_all[w];
+  const double *u = slots.p[GFGPU_SLOT_U];
+  for (int z = lane; z < NB * kEw; z += 32) {
+    const int j = z / kEw, k = z - j * kEw;
+    us[j][k] = k < ne ? u[enode[(e0 + k) * NB + j]] : 0.0;
+  }
+  // geometry of element e0 + k on lane k (K from the first point's geometric
+  // gradients: the Jacobian is constant)
+  if (lane < kEw) {
+    double B[9], det = 0.0;
+    if (lane < ne) {
+      double K[9];
+#pragma unroll
+      for (int d = 0; d < DIM; ++d)
+#pragma unroll
+        for (int m = 0; m < DIM; ++m) {
+          double s = 0.0;
+#pragma unroll
+          for (int v = 0; v < NBG; ++v)
+            s = fma(pts[int64_t(cv[(e0 + lane) * NBG + v]) * DIM + d], ggrad[v * DIM + m], s);
+          K[d + DIM * m] = s;
+        }
+      geo_inverse<DIM>(K, B, det);
+      if (det == 0.0) set_err(err, ERR_JACOBIAN);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) B[k] = 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) B_all[w][lane][k] = B[k];
+    det_all[w][lane] = det;
+  }
+  __syncwarp();
+  double acc[kEw];
+#pragma unroll
+  for (int k = 0; k < kEw; ++k) acc[k] = 0.0;
+  for (int q0 = 0; q0 < nq; q0 += 32) {
+    const int q = q0 + lane;
+    const bool act = q < nq;
+    const int qq = act ? q : 0;
+    double Gr[kEw][DIM];
+#pragma unroll
+    for (int k = 0; k < kEw; ++k)
+#pragma unroll
+      for (int m = 0; m < DIM; ++m) Gr[k][m] = 0.0;
+    for (int j = 0; j < NB; ++j) {
+      double r[DIM];
+#pragma unroll
+      for (int m = 0; m < DIM; ++m) r[m] = hgradT[int64_t(j * DIM + m) * nq + qq];
+#pragma unroll
+      for (int k = 0; k < kEw; ++k) {
+        const double uj = us[j][k];
+#pragma unroll
+        for (int m = 0; m < DIM; ++m) Gr[k][m] = fma(uj, r[m], Gr[k][m]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kEw; ++k) {
+      const double *B = B_all[w][k];
+      const double det = det_all[w][k];
+      const double wJ = (act && det != 0.0) ? fabs(det) * hw[qq] : 0.0;
+      double Gu[DIM];
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) {
+        double s = 0.0;
+#pragma unroll
+        for (int m = 0; m < DIM; ++m) s = fma(B[d + DIM * m], Gr[k][m], s);
+        Gu[d] = s;
+      }
+      const int64_t e = e0 + k;
+      const int64_t ec = k < ne ? e : e0;
+      double psi = 0.0, de = 0.0;
+      for (int t = 0; t < form.n_terms; ++t) {
+        const gfgpu_term &T = form.terms[t];
+        const double sc = T.scale;
+        const double c1 = coef_val(T.c[1], slots, ec, nullptr, nullptr, NB, nq) * sc;
+        double v = 0.0, gg = 0.0;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+          const double Dk = c1 * Gu[d];
+          v += Dk * Gu[d];
+          gg += Gu[d] * Gu[d];
+        }
+        psi += v;
+        double fe, fn;
+        coef_dfac(T.c[1], wslot, fe, fn);
+        de += sc * gg * fe;
+      }
+      if (!act) psi = de = 0.0;
+      acc[k] += (mode == 0 ? psi : de) * wJ;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < kEw; ++k) {
+    const double tot = warp_sum(acc[k]);
+    if (lane == 0 && k < ne) {
+      if (!isfinite(tot) && mode == 1) set_err(err, ERR_NAN);
+      out_e[e0 + k] = tot;
+    }
+  }
+}
+
 // Sum of n values in a fixed order (one block): deterministic.
 __global__ void __launch_bounds__(1024) ordered_sum(const double *__restrict__ v, int64_t n,
                                                     double *__restrict__ out) {
@@ -452,10 +579,41 @@ cudaError_t launch_gp(Plan &P, int mode, int wslot, const SlotPtrs &sp, double *
   return cudaGetLastError();
 }
 
+// The forms affine_scalar_potential_kernel takes: GRADGRAD terms only, with
+// constant or per-element coefficients and no c0 / c2 part.
+bool affine_scalar_potential_ok(const Plan &P, int mode) {
+  if (P.kind != HEX || !P.parallelepiped || P.law != LAW_ISO || P.qdim != 1 || P.dim != 3 ||
+      mode > 1 || P.form.n_terms < 1)
+    return false;
+  if (P.degree != 1 && P.degree != 2 && P.degree != 4) return false;
+  for (int t = 0; t < P.form.n_terms; ++t) {
+    const gfgpu_term &T = P.form.terms[t];
+    if (T.kind != GFGPU_TERM_GRADGRAD) return false;
+    if (T.c[0].kind != GFGPU_COEF_NONE || T.c[2].kind != GFGPU_COEF_NONE) return false;
+    if (T.c[1].kind != GFGPU_COEF_CONST && T.c[1].kind != GFGPU_COEF_ELEMENT) return false;
+  }
+  return true;
+}
+
+template <int NB>
+cudaError_t launch_asp(Plan &P, int mode, int wslot, const SlotPtrs &sp, double *oe) {
+  const int64_t per_block = int64_t(kGpWarps) * kEw;
+  const unsigned blocks = unsigned((P.n_elements + per_block - 1) / per_block);
+  affine_scalar_potential_kernel<NB><<<blocks, kGpWarps * 32, 0, P.stream>>>(
+      P.n_elements, P.nq, mode, wslot, P.d_points, P.d_cv, P.d_enode, P.d_hgradT, P.d_ggrad,
+      P.d_hw, P.form, sp, oe, P.d_err);
+  return cudaGetLastError();
+}
+
 cudaError_t dispatch_gp(Plan &P, int mode, int wslot, double *oe, double *on, double *ox) {
   SlotPtrs sp;
   for (int i = 0; i < GFGPU_MAX_SLOTS; ++i) sp.p[i] = P.slot_ptr[i];
   const int k = P.degree, q = P.qdim;
+  if (!on && affine_scalar_potential_ok(P, mode)) {
+    if (k == 4) return launch_asp<125>(P, mode, wslot, sp, oe);
+    if (k == 2) return launch_asp<27>(P, mode, wslot, sp, oe);
+    return launch_asp<8>(P, mode, wslot, sp, oe);
+  }
   if (P.law == LAW_NH) {
     if (P.kind == HEX && k == 2) return launch_gp<3, 3, 27, 8, LAW_NH>(P, mode, wslot, sp, oe, on, ox);
     if (P.kind == HEX && k == 1) return launch_gp<3, 3, 8, 8, LAW_NH>(P, mode, wslot, sp, oe, on, ox);
