@@ -467,6 +467,8 @@ int gfgpu_plan_create(const gfgpu_space *space, const gfgpu_form *form, void *cu
     }
     if (S.kind == GFGPU_HEX) {
       P->parallelepiped = mesh_is_parallelepiped(S.points, S.cvpts, S.n_elements);
+      P->axis_aligned =
+          P->parallelepiped && mesh_is_axis_aligned(S.points, S.cvpts, S.n_elements);
       P->h_cvpts.assign(S.cvpts, S.cvpts + S.n_elements * 8);
     }
     if (!P->affine_simplex) {
@@ -986,6 +988,8 @@ int gfgpu_set_points(gfgpu_plan *P, const double *points, int64_t n, int32_t on_
       hp = tmp.data();
     }
     P->parallelepiped = mesh_is_parallelepiped(hp, P->h_cvpts.data(), P->n_elements);
+    P->axis_aligned =
+        P->parallelepiped && mesh_is_axis_aligned(hp, P->h_cvpts.data(), P->n_elements);
   }
   return GFGPU_OK;
 }

@@ -391,6 +391,24 @@ bool mesh_is_parallelepiped(const double *pts, const int64_t *cv, int64_t E) {
   return true;
 }
 
+// True when every element is a box whose edges from vertex 0 (to vertices 1,
+// 2 and 4) each have exactly one nonzero coordinate difference, on distinct
+// axes: the Jacobian from those edges is a permuted diagonal matrix.
+bool mesh_is_axis_aligned(const double *pts, const int64_t *cv, int64_t E) {
+  for (int64_t e = 0; e < E; ++e) {
+    const int64_t *c = cv + e * 8;
+    int axes = 0;
+    for (int d = 0; d < 3; ++d) {
+      int nz = 0, ax = 0;
+      for (int k = 0; k < 3; ++k)
+        if (pts[c[1 << d] * 3 + k] - pts[c[0] * 3 + k] != 0.0) ++nz, ax = k;
+      if (nz != 1 || (axes & (1 << ax))) return false;
+      axes |= 1 << ax;
+    }
+  }
+  return true;
+}
+
 // Reference tensors (long double sums over the Gauss points of the
 // reference-tabulated values) and the upper-triangle entry list.
 void build_affine_hex_tables(Plan &P) {

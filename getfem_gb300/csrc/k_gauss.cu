@@ -535,6 +535,123 @@ __global__ void __launch_bounds__(kGpWarps * 32) affine_scalar_potential_kernel(
   }
 }
 
+// The same potentials through the reference tensors of the parallelepiped
+// plan (G_00, G_11, G_22, G_01, G_02, G_12: sum_q w_q of the products of
+// reference derivatives, summed on the host from the reference's tabulated
+// gradients): sum_q w_q |J| |grad u|^2 = |J| sum_p M_p u^T G_p u with
+// M = B^T B and the Jacobian K from the element's edge vectors (x_{e_m} -
+// x_0, exact differences).  On axis-aligned elements K, B and M are diagonal
+// (exact zeros) and only G_00, G_11, G_22 enter (NP = 3): 4 FP64 operations
+// per element and upper-triangle entry (a multiply and three FMAs), 31.5 k per
+// Q4 element against 49 k through the Gauss points; otherwise NP = 6.  EQ
+// elements per block share every table load; per-thread partial sums, then
+// warp and block sums in a fixed order.
+constexpr int kQfThreads = 256;
+
+template <int NB, int NP, int EQ>
+__global__ void __launch_bounds__(kQfThreads) affine_scalar_quadform_kernel(
+    int64_t E, int mode, int wslot, const double *__restrict__ pts,
+    const int32_t *__restrict__ cv, const int32_t *__restrict__ enode,
+    const double *__restrict__ tabs, const int32_t *__restrict__ tri, gfgpu_form form,
+    SlotPtrs slots, double *__restrict__ out_e, int *__restrict__ err) {
+  constexpr int DIM = 3, NT = NB * (NB + 1) / 2, NN = NB * NB;
+  constexpr int NW = kQfThreads / 32;
+  __shared__ double us[EQ][NB];
+  __shared__ double mc[EQ][NP];
+  __shared__ double cfs[EQ];
+  __shared__ double part[NW][EQ][NP];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int64_t e0 = int64_t(blockIdx.x) * EQ;
+  const int ne = E - e0 < EQ ? int(E - e0) : EQ;
+  const double *u = slots.p[GFGPU_SLOT_U];
+  for (int z = tid; z < NB * EQ; z += kQfThreads) {
+    const int k = z / NB, j = z - k * NB;
+    us[k][j] = k < ne ? u[enode[(e0 + k) * NB + j]] : 0.0;
+  }
+  if (tid < EQ) {
+    const int k = tid;
+    double m[NP], cf = 0.0;
+#pragma unroll
+    for (int p = 0; p < NP; ++p) m[p] = 0.0;
+    if (k < ne) {
+      const int64_t e = e0 + k;
+      const int32_t *c = cv + e * 8;
+      double K[9], B[9], det = 0.0;
+#pragma unroll
+      for (int mm = 0; mm < DIM; ++mm)
+#pragma unroll
+        for (int d = 0; d < DIM; ++d)
+          K[d + DIM * mm] = pts[int64_t(c[1 << mm]) * DIM + d] - pts[int64_t(c[0]) * DIM + d];
+      geo_inverse<DIM>(K, B, det);
+      if (det == 0.0) set_err(err, ERR_JACOBIAN);
+      const double J = det == 0.0 ? 0.0 : fabs(det);
+      // M_mn = sum_d B(d,m) B(d,n), in the table order 00 11 22 01 02 12
+#pragma unroll
+      for (int p = 0; p < NP; ++p) {
+        const int pm = p < 3 ? p : (p == 5 ? 1 : 0), pn = p < 3 ? p : (p == 3 ? 1 : 2);
+        double sum = 0.0;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) sum = fma(B[d + DIM * pm], B[d + DIM * pn], sum);
+        m[p] = J * sum;
+      }
+      for (int t = 0; t < form.n_terms; ++t) {
+        const gfgpu_term &T = form.terms[t];
+        if (mode == 0) {
+          cf += coef_val(T.c[1], slots, e, nullptr, nullptr, NB, 1) * T.scale;
+        } else {
+          double fe, fn;
+          coef_dfac(T.c[1], wslot, fe, fn);
+          cf += T.scale * fe;
+        }
+      }
+    }
+#pragma unroll
+    for (int p = 0; p < NP; ++p) mc[k][p] = m[p];
+    cfs[k] = cf;
+  }
+  __syncthreads();
+  double Q[EQ][NP];
+#pragma unroll
+  for (int k = 0; k < EQ; ++k)
+#pragma unroll
+    for (int p = 0; p < NP; ++p) Q[k][p] = 0.0;
+  for (int ent = tid; ent < NT; ent += kQfThreads) {
+    const int rc = tri[ent];
+    const int r = rc >> 16, c = rc & 0xffff, idx = r * NB + c;
+    const double two = r == c ? 1.0 : 2.0;
+    double g[NP];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) g[p] = two * tabs[p * NN + idx];
+#pragma unroll
+    for (int k = 0; k < EQ; ++k) {
+      const double pr = us[k][r] * us[k][c];
+#pragma unroll
+      for (int p = 0; p < NP; ++p) Q[k][p] = fma(g[p], pr, Q[k][p]);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < EQ; ++k)
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      const double v = warp_sum(Q[k][p]);
+      if (lane == 0) part[wid][k][p] = v;
+    }
+  __syncthreads();
+  if (tid < EQ && tid < ne) {
+    const int k = tid;
+    double s2 = 0.0;
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      double q = 0.0;
+      for (int w = 0; w < NW; ++w) q += part[w][k][p];
+      s2 = fma(mc[k][p], q, s2);
+    }
+    const double tot = cfs[k] * s2;
+    if (!isfinite(tot) && mode == 1) set_err(err, ERR_NAN);
+    out_e[e0 + k] = tot;
+  }
+}
+
 // Sum of n values in a fixed order (one block): deterministic.
 __global__ void __launch_bounds__(1024) ordered_sum(const double *__restrict__ v, int64_t n,
                                                     double *__restrict__ out) {
@@ -609,6 +726,28 @@ cudaError_t dispatch_gp(Plan &P, int mode, int wslot, double *oe, double *on, do
   SlotPtrs sp;
   for (int i = 0; i < GFGPU_MAX_SLOTS; ++i) sp.p[i] = P.slot_ptr[i];
   const int k = P.degree, q = P.qdim;
+  if (!on && affine_scalar_potential_ok(P, mode) && P.affine_hex && P.d_aff && P.d_tri) {
+    // reference tensors of the parallelepiped plan: 3 of them on an
+    // axis-aligned mesh (8 elements per block), else 6 (4 per block)
+#define QFK(NBV, NPV, EQV)                                                                    \
+  affine_scalar_quadform_kernel<NBV, NPV, EQV>                                               \
+      <<<unsigned((P.n_elements + EQV - 1) / EQV), kQfThreads, 0, P.stream>>>(               \
+          P.n_elements, mode, wslot, P.d_points, P.d_cv, P.d_enode, P.d_aff, P.d_tri, P.form, \
+          sp, oe, P.d_err)
+#define QFN(NBV)              \
+  do {                        \
+    if (P.axis_aligned)       \
+      QFK(NBV, 3, 8);         \
+    else                      \
+      QFK(NBV, 6, 4);         \
+  } while (0)
+    if (k == 4) QFN(125);
+    else if (k == 2) QFN(27);
+    else QFN(8);
+#undef QFN
+#undef QFK
+    return cudaGetLastError();
+  }
   if (!on && affine_scalar_potential_ok(P, mode)) {
     if (k == 4) return launch_asp<125>(P, mode, wslot, sp, oe);
     if (k == 2) return launch_asp<27>(P, mode, wslot, sp, oe);

@@ -166,6 +166,9 @@ struct Plan {
   // gfgpu_set_points): the Jacobian is constant, and the affine_hex kernels
   // apply
   bool parallelepiped = false;
+  // every element an axis-aligned box (edge vectors with one nonzero
+  // component each): the off-diagonal metric terms are exactly zero
+  bool axis_aligned = false;
   std::vector<int64_t> h_cvpts;  // E x 8 vertex ids of the hexahedra, for that check
   // parallelepiped hexahedra: reference tensors (7 x nb x nb)
   bool affine_hex = false;
@@ -330,6 +333,7 @@ cudaError_t launch_shape_gradient(Plan &P, double *d_out);
 // parallelepiped hexahedra (k_affine_hex.cu)
 bool affine_hex_form_ok(const gfgpu_form &f, int qdim);
 bool mesh_is_parallelepiped(const double *pts, const int64_t *cv, int64_t E);
+bool mesh_is_axis_aligned(const double *pts, const int64_t *cv, int64_t E);
 bool affine_hex_available(int degree);
 void build_affine_hex_tables(Plan &P);
 void build_affine_hex_sumfac(Plan &P);
