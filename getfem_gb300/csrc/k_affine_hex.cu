@@ -193,6 +193,110 @@ __global__ void __launch_bounds__(T) affine_hex_kernel(
   }
 }
 
+// Vector-only pass (matrix-free R = K u) of a GRADGRAD-only form through the
+// reference tensors: R_e[r] = sum_p c_p (G_p u_e)[r], c_p = c1 |J| M_p, with
+// K from the element's edge vectors (exact differences).  On an axis-aligned
+// mesh (NP = 3) only G_00, G_11, G_22 enter: 3 FMAs per element and entry
+// instead of forming each entry of K_e from 7 tables (8 operations) and
+// multiplying.  Thread r walks column r of each table (tables symmetric:
+// coalesced loads) for EQ elements of the block at once, so each table load
+// feeds EQ FMAs.
+template <int NB, int NP, int EQ>
+__global__ void __launch_bounds__(128) affine_scalar_apply_kernel(
+    int64_t E, const double *__restrict__ pts, const int32_t *__restrict__ cv,
+    const int32_t *__restrict__ enode, const double *__restrict__ tabs, KeLayout L,
+    gfgpu_form form, SlotPtrs slots, double *__restrict__ out, int *__restrict__ err) {
+  constexpr int NN = NB * NB;
+  static_assert(NB <= 128, "one thread per row");
+  __shared__ double us[EQ][NB];
+  __shared__ double cfs[EQ][NP];
+  const int tid = threadIdx.x;
+  const int64_t e0 = int64_t(blockIdx.x) * EQ;
+  const int ne = E - e0 < EQ ? int(E - e0) : EQ;
+  const double *u = slots.p[GFGPU_SLOT_U];
+  for (int z = tid; z < NB * EQ; z += 128) {
+    const int k = z / NB, j = z - k * NB;
+    us[k][j] = (k < ne && u) ? u[enode[(e0 + k) * NB + j]] : 0.0;
+  }
+  if (tid < EQ) {
+    const int k = tid;
+    double m[NP];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) m[p] = 0.0;
+    if (k < ne) {
+      const int64_t e = e0 + k;
+      const int32_t *c = cv + e * 8;
+      double K[9], B[9];
+#pragma unroll
+      for (int mm = 0; mm < 3; ++mm)
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+          K[d + 3 * mm] = pts[int64_t(c[1 << mm]) * 3 + d] - pts[int64_t(c[0]) * 3 + d];
+      const double a0 = K[4] * K[8] - K[5] * K[7];
+      const double a1 = K[5] * K[6] - K[3] * K[8];
+      const double a2 = K[3] * K[7] - K[4] * K[6];
+      const double det = K[0] * a0 + K[1] * a1 + K[2] * a2;
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+          B[i + 3 * j] = (K[i1 + 3 * j1] * K[i2 + 3 * j2] - K[i1 + 3 * j2] * K[i2 + 3 * j1]) / det;
+        }
+      if (det == 0.0) set_err(err, ERR_JACOBIAN);
+      const double J = det == 0.0 ? 0.0 : fabs(det);
+      double c1 = 0.0;
+      for (int t = 0; t < form.n_terms; ++t) {
+        const gfgpu_term &Tm = form.terms[t];
+        const gfgpu_coef &cc = Tm.c[1];
+        const double v = cc.kind == GFGPU_COEF_CONST     ? cc.value
+                         : cc.kind == GFGPU_COEF_ELEMENT ? cc.value * slots.p[cc.slot][e]
+                                                         : 0.0;
+        c1 += Tm.scale * v;
+      }
+      const double cJ = c1 * J;
+      // M_mn = sum_d B(d,m) B(d,n), table order 00 11 22 01 02 12
+#pragma unroll
+      for (int p = 0; p < NP; ++p) {
+        const int pm = p < 3 ? p : (p == 5 ? 1 : 0), pn = p < 3 ? p : (p == 3 ? 1 : 2);
+        double sum = 0.0;
+        for (int d = 0; d < 3; ++d) sum += B[d + 3 * pm] * B[d + 3 * pn];
+        m[p] = cJ * sum;
+      }
+    }
+#pragma unroll
+    for (int p = 0; p < NP; ++p) cfs[k][p] = m[p];
+  }
+  __syncthreads();
+  if (tid >= NB) return;
+  const int r = tid;
+  double acc[EQ][NP];
+#pragma unroll
+  for (int k = 0; k < EQ; ++k)
+#pragma unroll
+    for (int p = 0; p < NP; ++p) acc[k][p] = 0.0;
+  for (int c = 0; c < NB; ++c) {
+    double g[NP];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) g[p] = tabs[p * NN + c * NB + r];
+#pragma unroll
+    for (int k = 0; k < EQ; ++k) {
+      const double uc = us[k][c];
+#pragma unroll
+      for (int p = 0; p < NP; ++p) acc[k][p] = fma(g[p], uc, acc[k][p]);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < EQ; ++k) {
+    if (k >= ne) break;
+    double v = cfs[k][0] * acc[k][0];
+#pragma unroll
+    for (int p = 1; p < NP; ++p) v = fma(cfs[k][p], acc[k][p], v);
+    if (!isfinite(v)) set_err(err, ERR_NAN);
+    out[(e0 + k) * L.stride + L.off_vec + r] = v;
+  }
+}
+
 // 1D tables of the sum factorisation: values and derivatives of the 1D
 // basis at the 1D Gauss points (N[q][a], D[q][a]), the 1D weights, and the
 // tensor index a + P1 (b + P1 c) of each local DOF
@@ -559,6 +663,37 @@ cudaError_t launch_affine_hex_pass(Plan &P, bool want_K) {
 #undef SFK
     P.launches++;
     return cudaGetLastError();
+  }
+  if (!want_K) {
+    // a GRADGRAD-only form: the vector through the reference tensors, several
+    // elements per block
+    bool gg = P.form.n_terms > 0;
+    for (int t = 0; t < P.form.n_terms; ++t) gg &= P.form.terms[t].kind == GFGPU_TERM_GRADGRAD;
+    if (gg) {
+#define APK(NBV, NPV, EQV)                                                                    \
+  affine_scalar_apply_kernel<NBV, NPV, EQV>                                                  \
+      <<<unsigned((P.n_elements + EQV - 1) / EQV), 128, 0, P.stream>>>(                     \
+          P.n_elements, P.d_points, P.d_cv, P.d_enode, P.d_aff, P.lay, P.form, sp, P.d_elem, \
+          P.d_err)
+#define APN(NBV)          \
+  do {                    \
+    if (P.axis_aligned)   \
+      APK(NBV, 3, 8);     \
+    else                  \
+      APK(NBV, 6, 4);     \
+  } while (0)
+      switch (P.nb) {
+        case 8: APN(8); break;
+        case 27: APN(27); break;
+        case 64: APN(64); break;
+        case 125: APN(125); break;
+        default: return cudaErrorInvalidValue;
+      }
+#undef APN
+#undef APK
+      P.launches++;
+      return cudaGetLastError();
+    }
   }
   // the K pass with the plan's threads per element (autotuned)
   const int tk = P.tune.ep_threads;
