@@ -49,16 +49,22 @@ constexpr int kAffTables = 7;  // G_00, G_11, G_22, G_01, G_02, G_12, Mhat
 // (cofactor / det) on lanes 0-8, M = B^T B upper triangle (00, 11, 22, 01,
 // 02, 12) on lanes 0-5.  Writes g[0..8] = K, g[9..17] = B, g[18..23] = M,
 // g[24] = |det| (0 for a degenerate element, which sets ERR_JACOBIAN).
+// edges: K from the edge vectors x_{e_m} - x_0 (exact differences: an
+// axis-aligned element gets exact zeros off the diagonal of K, B and M)
 __device__ __forceinline__ void parallelepiped_geometry(int lane, int64_t e,
                                                         const double *__restrict__ pts,
                                                         const int32_t *__restrict__ cv,
                                                         const double *__restrict__ ggrad0,
-                                                        double *g, int *err) {
+                                                        double *g, int *err, bool edges = false) {
   if (lane < 9) {
     const int d = lane % 3, m = lane / 3;
-    double s = 0.0;
-    for (int v = 0; v < 8; ++v) s += pts[int64_t(cv[e * 8 + v]) * 3 + d] * ggrad0[v * 3 + m];
-    g[lane] = s;
+    if (edges) {
+      g[lane] = pts[int64_t(cv[e * 8 + (1 << m)]) * 3 + d] - pts[int64_t(cv[e * 8]) * 3 + d];
+    } else {
+      double s = 0.0;
+      for (int v = 0; v < 8; ++v) s += pts[int64_t(cv[e * 8 + v]) * 3 + d] * ggrad0[v * 3 + m];
+      g[lane] = s;
+    }
   }
   __syncwarp();
   if (lane < 9) {
@@ -89,7 +95,10 @@ __device__ __forceinline__ void parallelepiped_geometry(int lane, int64_t e,
 
 // T threads per element (the CTA of the element); every entry and row is
 // computed by one thread in the same order whatever T is (same bits).
-template <int NB, bool WANT_K, int T = kAffThreads>
+// AX: an axis-aligned mesh (the host checks every element exactly): K from
+// the edge vectors, the off-diagonal metric terms exact zeros, and K_e from
+// G_00, G_11, G_22 (and the mass table when the form has a mass term) only.
+template <int NB, bool WANT_K, int T = kAffThreads, bool AX = false>
 __global__ void __launch_bounds__(T) affine_hex_kernel(
     int64_t E, const double *__restrict__ pts, const int32_t *__restrict__ cv,
     const int32_t *__restrict__ enode, const double *__restrict__ tabs,
@@ -114,7 +123,7 @@ __global__ void __launch_bounds__(T) affine_hex_kernel(
     fs[j] = src_slot >= 0 ? slots.p[src_slot][n] : 0.0;
   }
   if (wid == 0) {
-    parallelepiped_geometry(lane, e, pts, cv, ggrad0, geo, err);
+    parallelepiped_geometry(lane, e, pts, cv, ggrad0, geo, err, AX);
     if (lane == 0) {
       smax = 0ull;
       const double J = geo[24];
@@ -141,6 +150,9 @@ __global__ void __launch_bounds__(T) affine_hex_kernel(
   double c[kAffTables];
 #pragma unroll
   for (int p = 0; p < kAffTables; ++p) c[p] = cp[p];
+  // a mass term (block-uniform, from the form)
+  bool hasm = false;
+  for (int t = 0; t < form.n_terms; ++t) hasm |= form.terms[t].kind == GFGPU_TERM_MASS;
   double *o = out + e * L.stride;
   if constexpr (WANT_K) {
     unsigned long long mx = 0ull;
@@ -149,8 +161,14 @@ __global__ void __launch_bounds__(T) affine_hex_kernel(
       const int r = rc >> 16, col = rc & 0xffff;
       const int idx = r * NB + col;
       double v = c[0] * tabs[idx];
+      if constexpr (AX) {
+        v = fma(c[1], tabs[NN + idx], v);
+        v = fma(c[2], tabs[2 * NN + idx], v);
+        if (hasm) v = fma(c[6], tabs[6 * NN + idx], v);
+      } else {
 #pragma unroll
-      for (int p = 1; p < kAffTables; ++p) v = fma(c[p], tabs[p * NN + idx], v);
+        for (int p = 1; p < kAffTables; ++p) v = fma(c[p], tabs[p * NN + idx], v);
+      }
       o[r * L.rowstride + col] = v;
       if (r != col) o[col * L.rowstride + r] = v;
       const unsigned long long bits = abs_key(v);
@@ -174,8 +192,14 @@ __global__ void __launch_bounds__(T) affine_hex_kernel(
         k = o[col * L.rowstride + r];
       } else {
         k = c[0] * tabs[idx];
+        if constexpr (AX) {
+          k = fma(c[1], tabs[NN + idx], k);
+          k = fma(c[2], tabs[2 * NN + idx], k);
+          if (hasm) k = fma(c[6], tabs[6 * NN + idx], k);
+        } else {
 #pragma unroll
-        for (int p = 1; p < kAffTables; ++p) k = fma(c[p], tabs[p * NN + idx], k);
+          for (int p = 1; p < kAffTables; ++p) k = fma(c[p], tabs[p * NN + idx], k);
+        }
       }
       s = fma(k, us[col], s);
       if (src_slot >= 0) sf = fma(tabs[6 * NN + idx], fs[col], sf);
@@ -697,10 +721,17 @@ cudaError_t launch_affine_hex_pass(Plan &P, bool want_K) {
   }
   // the K pass with the plan's threads per element (autotuned)
   const int tk = P.tune.ep_threads;
-#define AFFK(NB, TT)                                                                           \
-  affine_hex_kernel<NB, true, TT><<<grid, TT, 0, P.stream>>>(                                  \
+#define AFFKX(NB, TT, AXV)                                                                     \
+  affine_hex_kernel<NB, true, TT, AXV><<<grid, TT, 0, P.stream>>>(                             \
       P.n_elements, P.d_points, P.d_cv, P.d_enode, P.d_aff, P.d_tri, P.d_ggrad, P.lay, P.form, \
       sp, P.d_elem, P.d_err)
+#define AFFK(NB, TT)              \
+  do {                            \
+    if (P.axis_aligned)           \
+      AFFKX(NB, TT, true);        \
+    else                          \
+      AFFKX(NB, TT, false);       \
+  } while (0)
 #define AFF(NB)                                                                                \
   do {                                                                                         \
     if (want_K && tk == 128) AFFK(NB, 128);                                                    \
@@ -720,6 +751,7 @@ cudaError_t launch_affine_hex_pass(Plan &P, bool want_K) {
   }
 #undef AFF
 #undef AFFK
+#undef AFFKX
   P.launches++;
   return cudaGetLastError();
 }
