@@ -227,6 +227,108 @@ void spmv(const Plan &P, const double *x, double *y, const double *w, double *pa
   }
 }
 
+// CG of a small system in one block (n <= kCgSmallMax): the same recurrence
+// and stop rule, every step on the device (no host round trip per
+// iteration; the multi-kernel loop spent ~45 us per iteration on launches
+// and the stop-test read at 4225 unknowns).  Dot products: per-thread
+// partials over rows tid, tid + 1024, ..., then a warp tree and a tree over
+// the 32 warps, in a fixed order.  The loop is bounded by maxiter.
+constexpr int kCgSmallThreads = 1024;
+constexpr int64_t kCgSmallMax = 32768;
+
+__device__ __forceinline__ double block_sum_1024(double v, double *sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();  // sh free (a previous sum's readers are done)
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  double t = sh[lane];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  return t;  // every thread holds the total
+}
+
+__global__ void __launch_bounds__(kCgSmallThreads, 1) cg_small_kernel(
+    int64_t n, const int64_t *__restrict__ rowptr, const int32_t *__restrict__ colidx,
+    const double *__restrict__ vals, const double *__restrict__ b, double *__restrict__ x,
+    double *__restrict__ r, double *__restrict__ p, double *__restrict__ q, double *z,
+    const double *__restrict__ dinv, double resmax, int64_t maxiter, double *__restrict__ out) {
+  __shared__ double sh[32];
+  const int tid = threadIdx.x;
+  constexpr int T = kCgSmallThreads;
+  auto spmv = [&](const double *v, double *y) {
+    for (int64_t i = tid; i < n; i += T) {
+      double s = 0.0;
+      for (int64_t k = rowptr[i]; k < rowptr[i + 1]; ++k) s = fma(vals[k], v[colidx[k]], s);
+      y[i] = s;
+    }
+  };
+  double bb = 0.0;
+  for (int64_t i = tid; i < n; i += T) bb = fma(b[i], b[i], bb);
+  const double rhsn = sqrt(fabs(block_sum_1024(bb, sh)));
+  int64_t nit = 0;
+  double res = 0.0;
+  if (rhsn == 0.0) {
+    for (int64_t i = tid; i < n; i += T) x[i] = 0.0;
+  } else {
+    // r = b - A x; z = P r; rho = z.r; p = z
+    spmv(x, q);
+    __syncthreads();
+    double rr = 0.0, zr = 0.0;
+    for (int64_t i = tid; i < n; i += T) {
+      const double ri = b[i] - q[i];
+      r[i] = ri;
+      const double zi = dinv ? dinv[i] * ri : ri;
+      if (dinv) z[i] = zi;
+      p[i] = zi;
+      rr = fma(ri, ri, rr);
+      zr = fma(zi, ri, zr);
+    }
+    rr = block_sum_1024(rr, sh);
+    double rho = dinv ? block_sum_1024(zr, sh) : rr;
+    const double *zz = dinv ? z : r;
+    for (;;) {
+      res = sqrt(rr);
+      if (isnan(res) || res <= rhsn * resmax || nit >= maxiter) break;
+      if (nit > 0) {
+        const double rho_old = rho;
+        rho = dinv ? zr : rr;
+        const double beta = rho / rho_old;
+        for (int64_t i = tid; i < n; i += T) p[i] = fma(beta, p[i], zz[i]);
+        __syncthreads();
+      }
+      // q = A p; alpha = rho / q.p; x += alpha p; r -= alpha q; z = P r
+      spmv(p, q);
+      double qp = 0.0;
+      for (int64_t i = tid; i < n; i += T) qp = fma(q[i], p[i], qp);
+      qp = block_sum_1024(qp, sh);
+      const double alpha = rho / qp;
+      rr = 0.0;
+      zr = 0.0;
+      for (int64_t i = tid; i < n; i += T) {
+        x[i] = fma(alpha, p[i], x[i]);
+        const double ri = fma(-alpha, q[i], r[i]);
+        r[i] = ri;
+        rr = fma(ri, ri, rr);
+        if (dinv) {
+          const double zi = dinv[i] * ri;
+          z[i] = zi;
+          zr = fma(zi, ri, zr);
+        }
+      }
+      rr = block_sum_1024(rr, sh);
+      if (dinv) zr = block_sum_1024(zr, sh);
+      ++nit;
+    }
+  }
+  if (tid == 0) {
+    out[0] = double(nit);
+    out[1] = rhsn == 0.0 ? 0.0 : res / rhsn;
+    out[2] = res;
+  }
+}
+
 struct CgScratch {
   double *r = nullptr, *p = nullptr, *q = nullptr, *z = nullptr, *dinv = nullptr;
   double *part = nullptr, *part2 = nullptr, *sc = nullptr;
@@ -341,7 +443,29 @@ extern "C" int gfgpu_cg(gfgpu_plan *plan, const double *b, double *x, double res
   }
   SOLVE_CUDA(cudaMemsetAsync(P->d_err, 0, sizeof(int), st));
   const unsigned eb = unsigned((n + 255) / 256);
-  double h[2];
+  double h[3];
+  if (n <= kCgSmallMax) {
+    // one block runs the whole solve
+    if (precond == 1)
+      diag_inverse<<<eb, 256, 0, st>>>(n, P->d_rowptr, P->d_colidx, P->d_vals, W.dinv, P->d_err);
+    cg_small_kernel<<<1, kCgSmallThreads, 0, st>>>(n, P->d_rowptr, P->d_colidx, P->d_vals, b, x,
+                                                   W.r, W.p, W.q, W.z,
+                                                   precond == 1 ? W.dinv : nullptr, resmax,
+                                                   maxiter, W.sc);
+    SOLVE_CUDA(cudaGetLastError());
+    SOLVE_CUDA(cudaMemcpyAsync(h, W.sc, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    SOLVE_CUDA(cudaStreamSynchronize(st));
+    P->launches += precond == 1 ? 2 : 1;
+    if (iterations) *iterations = int64_t(h[0]);
+    if (residual) *residual = h[1];
+    int rc = read_err(*P);
+    if (rc) return rc;
+    if (std::isnan(h[2])) {
+      set_last_error("gfgpu_cg: residual is NaN");
+      return GFGPU_E_NAN;
+    }
+    return GFGPU_OK;
+  }
   // ||b||
   dot_kernel<<<vb, kSolveThreads, 0, st>>>(n, b, b, W.part);
   finish_sum<<<1, kSolveThreads, 0, st>>>(W.part, vb, W.sc + 4);
