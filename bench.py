@@ -822,11 +822,14 @@ def main():
     # DRAM bytes per launch of the dominant kernel: from one ncu capture of
     # the same kernel on the 20^3 x 6 mesh, scaled by the element count
     traffic = None
+    fp64_ncu = None
     prof = os.path.join(ROOT, "profiles", "dram_bytes_per_element.json")
     if os.path.exists(prof):
         try:
-            traffic = float(_json.load(open(prof))[names[dom]]) * E
-        except (ValueError, TypeError, KeyError):
+            rec = _json.load(open(prof))
+            traffic = float(rec[names[dom]]) * E
+            fp64_ncu = rec.get("fp64_pipe_active", {}).get(names[dom])
+        except (ValueError, TypeError, KeyError, AttributeError):
             traffic = None
     cpu = None
     if not args.no_cpu:
@@ -864,6 +867,7 @@ def main():
                      "peak": hbm_peak, "unit": "GB/s", "frac": dom_gbs / hbm_peak,
                      "traffic": traffic, "algorithmic_bytes": step_bytes,
                      "peak_source": peak_source,
+                     "fp64_pipe_active_ncu": fp64_ncu,
                      "limiter": "FP64 pipe and issue latency, not HBM: measured FP64 FMA "
                                 f"{fp64_peak.value:.2f} TFLOP/s is 0.19 flop per HBM byte; "
                                 "the fp64 object gives the element pass's FP64 fraction"},
