@@ -247,3 +247,38 @@ def test_parallelepiped_scalar_potential_and_coefficient_gradient(shear, degree)
     Eo = oracle_problem(mesh, mf, mim, grp.order0, slots_of(ws)).potential(2)
     assert abs(float(E) - Eo) <= RTOL * abs(Eo), (float(E), Eo)
     assert abs(float(E) - float(kappa.grad @ kappa)) <= RTOL * abs(float(E))
+
+
+def test_points_moved_onto_parallelepipeds():
+    """A potential plan made on a jittered (non-parallelepiped) Q2 mesh whose
+    vertices are then moved onto the regular lattice (gfgpu_set_points): the
+    plan has no reference tensors, and the energy and dE/dkappa go through the
+    Gauss-point sums with several elements per warp.  Both match the oracle
+    at the moved points, and E = sum_e kappa_e dE/dkappa_e."""
+    from oracle import gfref
+    torch = _torch()
+    rng = np.random.default_rng(31)
+    nx = 3
+    jit = rng.uniform(-0.1 / nx, 0.1 / nx, ((nx + 1) ** 3, 3))
+    mesh = g.Mesh.regular_unit(3, nx, "hex", jitter=jit)
+    regular = g.Mesh.regular_unit(3, nx, "hex")
+    mf = g.MeshFem(mesh, 1, degree=2)
+    mim = g.MeshIm(mesh, "IM_GAUSS_PARALLELEPIPED(3,5)")
+    u0 = rng.standard_normal(mf.nb_dof())
+    k0 = np.exp(rng.normal(0, 0.5, mesh.nb_convex()))
+    ws = g.GaWorkspace()
+    ws.add_fem_variable("u", mf, U=u0)
+    ws.add_fem_constant("kappa", g.MeshFem(mesh, 1, degree=0), k0)
+    ws.add_expression("kappa*Grad_u.Grad_u", mim)
+    pot = g.Potential(ws)
+    dev = torch.device("cuda")
+    u = torch.tensor(u0, device=dev)
+    kappa = torch.tensor(k0, device=dev, requires_grad=True)
+    X = torch.tensor(regular.points.ravel(), device=dev)
+    E = pot(u, points=X, kappa=kappa)
+    E.backward()
+    grp = ws.groups[0]
+    Eo = gfref.Problem(3, mesh.kind, 2, 1, mim.im, regular.points, mesh.cvpts, mf.dofs,
+                       mf.nb_dof(), grp.order0, slots_of(ws)).potential(4)
+    assert abs(float(E) - Eo) <= RTOL * abs(Eo), (float(E), Eo)
+    assert abs(float(E) - float(kappa.grad @ kappa)) <= RTOL * abs(float(E))
