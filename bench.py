@@ -489,7 +489,7 @@ def bench_batched(steps, n_meshes=512, lo=1e3, hi=2e5):
     out = {"workload": f"{n_meshes} meshes, element counts log-uniform in [{lo:g}, {hi:g}], "
                        "P1/P2 tri Poisson and P1/P2 tet elasticity, K + R per mesh",
            "meshes": n_meshes, "elements": int(E_total), "setup_s": setup_s,
-           "grid_elem_pass": grids[0], "grid_gather": grids[1],
+           "grid_elem_pass": grids[0], "gather_launches": grids[1],
            "ms_plain": t_plain, "ms_batched": t_batch, "ms_graph_replay": t_graph,
            "elements_per_s_plain": E_total / (t_plain * 1e-3),
            "elements_per_s_batched": E_total / (t_batch * 1e-3),

@@ -1,13 +1,14 @@
-"""Batched assembly of many independent meshes in one persistent launch.
+"""Batched assembly of many independent meshes in a few launches.
 
 A GetFEM user assembling many small problems calls ga_workspace::assembly
 once per workspace; here the K + R assembly of every workspace of a batch
-runs as one persistent element-pass launch and one row-gather launch per
-component count (gfgpu_batch_assemble), which a CUDA graph can capture and
-replay (coefficients changed in place between replays are picked up).
+runs as one persistent element-pass launch per element type and one
+row-gather launch per component count and valence class
+(gfgpu_batch_assemble), which a CUDA graph can capture and replay
+(coefficients changed in place between replays are picked up).
 
     b = Batch([ws1, ws2, ...])       # affine-simplex workspaces
-    b.tune()                         # grid sizes by measurement
+    b.tune()                         # element-pass grid by measurement
     b.assemble()                     # every K and R, on the device
     g = b.graph(pre=perturb)         # torch.cuda.CUDAGraph of pre() + assemble
     g.replay()
@@ -54,6 +55,8 @@ class Batch:
         L.check(L.lib().gfgpu_batch_sync(self.h, _stream_ptr(stream)))
 
     def tune(self, stream=None):
+        """Element-pass grid (tuned) and the number of row-gather launches
+        (one per component count and valence class)."""
         ge, gg = C.c_int32(), C.c_int32()
         L.check(L.lib().gfgpu_batch_tune(self.h, _stream_ptr(stream), C.byref(ge), C.byref(gg)))
         return ge.value, gg.value

@@ -44,6 +44,16 @@ struct gfgpu_batch_s {
   size_t gwarp[4] = {};
   int grid_ep = 0, grid_ga = 0;
   int *d_err = nullptr;
+  // the gather by valence class (per component count): nodes of every mesh
+  // whose valence bucket has at most 2^c adjacent elements, as item << 32 |
+  // node, with the class's slot and adjacency maxima
+  struct GatherClass {
+    int64_t *d_list = nullptr;
+    int64_t n = 0;
+    int ms = 1, mad = 1;
+    size_t wb = 0;
+  };
+  std::vector<GatherClass> gclass[4];
 };
 
 namespace {
@@ -1063,7 +1073,6 @@ int gfgpu_batch_create(gfgpu_plan *const *plans, int32_t n, gfgpu_batch **out) {
     B->elements += P.n_elements;
     gitems[it.qd].push_back(it);
     node0[it.qd].push_back(node0[it.qd].back() + P.n_nodes);
-    B->gwarp[it.qd] = std::max(B->gwarp[it.qd], batch_gather_warp_bytes(it));
     B->plans.push_back(plans[i]);
   }
   auto upload = [&](void *dst, const void *src, size_t bytes) -> int {
@@ -1092,6 +1101,50 @@ int gfgpu_batch_create(gfgpu_plan *const *plans, int32_t n, gfgpu_batch **out) {
     if ((rc = upload(B->d_node0[q], node0[q].data(), node0[q].size() * sizeof(int64_t))))
       return fail(rc, "");
   }
+  // the class lists: every node of every mesh by its own valence (class c:
+  // at most 2^c adjacent elements), in mesh order, with the class maxima of
+  // slots and adjacent elements
+  for (int q = 1; q <= 3; ++q) {
+    auto &cls = B->gclass[q];
+    std::vector<std::vector<int64_t>> lists;
+    for (size_t item = 0; item < gitems[q].size(); ++item) {
+      const BatchItem &it = gitems[q][item];
+      std::vector<int32_t> aptr(size_t(it.n_nodes + 1));
+      std::vector<int64_t> nptr(size_t(it.n_nodes + 1));
+      if ((rc = [&]() -> int {
+            GF_CUDA(cudaMemcpy(aptr.data(), it.adj_ptr, aptr.size() * sizeof(int32_t),
+                               cudaMemcpyDeviceToHost));
+            GF_CUDA(cudaMemcpy(nptr.data(), it.nptr, nptr.size() * sizeof(int64_t),
+                               cudaMemcpyDeviceToHost));
+            return GFGPU_OK;
+          }()))
+        return fail(rc, "");
+      for (int64_t node = 0; node < it.n_nodes; ++node) {
+        const int mad = std::max(1, aptr[size_t(node + 1)] - aptr[size_t(node)]);
+        const int ms = std::max<int64_t>(1, nptr[size_t(node + 1)] - nptr[size_t(node)]);
+        int c = 0;
+        while ((1 << c) < mad) ++c;
+        if (cls.size() <= size_t(c)) {
+          cls.resize(size_t(c) + 1);
+          lists.resize(size_t(c) + 1);
+        }
+        cls[size_t(c)].ms = std::max(cls[size_t(c)].ms, ms);
+        cls[size_t(c)].mad = std::max(cls[size_t(c)].mad, mad);
+        lists[size_t(c)].push_back((int64_t(item) << 32) | node);
+      }
+    }
+    for (size_t c = 0; c < cls.size(); ++c) {
+      auto &k = cls[c];
+      k.n = int64_t(lists[c].size());
+      if (!k.n) continue;
+      for (const BatchItem &it : gitems[q])
+        k.wb = std::max(k.wb, batch_gather_class_bytes(it, k.ms, k.mad));
+      B->gwarp[q] = std::max(B->gwarp[q], k.wb);
+      if ((rc = dalloc(&k.d_list, lists[c].size()))) return fail(rc, "");
+      if ((rc = upload(k.d_list, lists[c].data(), lists[c].size() * sizeof(int64_t))))
+        return fail(rc, "");
+    }
+  }
   size_t gmax = 0;
   for (int q = 1; q <= 3; ++q) gmax = std::max(gmax, B->gwarp[q]);
   cudaError_t ce = batch_gather_attr(4 * gmax);
@@ -1101,7 +1154,8 @@ int gfgpu_batch_create(gfgpu_plan *const *plans, int32_t n, gfgpu_batch **out) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   B->grid_ep = 8 * std::max(sms, 1);
-  B->grid_ga = 8 * std::max(sms, 1);
+  for (int q = 1; q <= 3; ++q)
+    for (const auto &k : B->gclass[q]) B->grid_ga += k.n > 0;
   *out = B;
   return GFGPU_OK;
 }
@@ -1114,21 +1168,27 @@ static int batch_element_passes(gfgpu_batch *B, cudaStream_t st, int grid_ep) {
   return GFGPU_OK;
 }
 
-static int batch_launch(gfgpu_batch *B, cudaStream_t st, int grid_ep, int grid_ga) {
+// the row gathers of a batch: one launch per component count and valence
+// class
+static int batch_gathers(gfgpu_batch *B, cudaStream_t st) {
+  for (int q = 1; q <= 3; ++q)
+    for (const auto &k : B->gclass[q])
+      if (k.n)
+        GF_CUDA(launch_batch_gather_list(B->d_gitems[q], k.d_list, k.n, q, k.ms, k.mad, k.wb, st));
+  return GFGPU_OK;
+}
+
+static int batch_launch(gfgpu_batch *B, cudaStream_t st, int grid_ep) {
   // a fresh error word for this assembly (a memset node in a captured graph)
   GF_CUDA(cudaMemsetAsync(B->d_err, 0, sizeof(int), st));
   int rc = batch_element_passes(B, st, grid_ep);
   if (rc) return rc;
-  for (int q = 1; q <= 3; ++q)
-    if (B->gn[q])
-      GF_CUDA(launch_batch_gather(B->d_gitems[q], B->d_node0[q], B->gn[q], B->gnodes[q], q,
-                                  grid_ga, B->gwarp[q], st));
-  return GFGPU_OK;
+  return batch_gathers(B, st);
 }
 
 int gfgpu_batch_assemble(gfgpu_batch *B, void *stream) {
   if (!B) return GFGPU_E_INVALID;
-  return batch_launch(B, static_cast<cudaStream_t>(stream), B->grid_ep, B->grid_ga);
+  return batch_launch(B, static_cast<cudaStream_t>(stream), B->grid_ep);
 }
 
 int gfgpu_batch_tune(gfgpu_batch *B, void *stream, int32_t *grid_ep, int32_t *grid_ga) {
@@ -1141,10 +1201,10 @@ int gfgpu_batch_tune(gfgpu_batch *B, void *stream, int32_t *grid_ep, int32_t *gr
   GF_CUDA(cudaEventCreate(&e0));
   GF_CUDA(cudaEventCreate(&e1));
   const int mult[] = {1, 2, 4, 8, 16, 32};
-  float best_ep = 1e30f, best_ga = 1e30f;
+  float best_ep = 1e30f;
   for (int m : mult) {
     const int g = m * std::max(sms, 1);
-    float t_ep = 0, t_ga = 0;
+    float t_ep = 0;
     for (int rep = 0; rep < 3; ++rep) {
       GF_CUDA(cudaEventRecord(e0, st));
       int rc = batch_element_passes(B, st, g);
@@ -1154,21 +1214,16 @@ int gfgpu_batch_tune(gfgpu_batch *B, void *stream, int32_t *grid_ep, int32_t *gr
       float t;
       GF_CUDA(cudaEventElapsedTime(&t, e0, e1));
       t_ep = rep == 0 ? t : std::min(t_ep, t);
-      GF_CUDA(cudaEventRecord(e0, st));
-      for (int q = 1; q <= 3; ++q)
-        if (B->gn[q])
-          GF_CUDA(launch_batch_gather(B->d_gitems[q], B->d_node0[q], B->gn[q], B->gnodes[q], q, g,
-                                      B->gwarp[q], st));
-      GF_CUDA(cudaEventRecord(e1, st));
-      GF_CUDA(cudaEventSynchronize(e1));
-      GF_CUDA(cudaEventElapsedTime(&t, e0, e1));
-      t_ga = rep == 0 ? t : std::min(t_ga, t);
     }
     if (t_ep < best_ep) best_ep = t_ep, B->grid_ep = g;
-    if (t_ga < best_ga) best_ga = t_ga, B->grid_ga = g;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  // the gathers are one launch per component count and valence class
+  int nga = 0;
+  for (int q = 1; q <= 3; ++q)
+    for (const auto &k : B->gclass[q]) nga += k.n > 0;
+  B->grid_ga = nga;
   if (grid_ep) *grid_ep = B->grid_ep;
   if (grid_ga) *grid_ga = B->grid_ga;
   return GFGPU_OK;
@@ -1193,6 +1248,7 @@ void gfgpu_batch_destroy(gfgpu_batch *B) {
   for (int q = 0; q < 4; ++q) {
     dfree(B->d_gitems[q]);
     dfree(B->d_node0[q]);
+    for (auto &k : B->gclass[q]) dfree(k.d_list);
   }
   dfree(B->d_err);
   delete B;

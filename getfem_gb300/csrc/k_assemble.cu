@@ -549,30 +549,24 @@ __global__ void __launch_bounds__(256) vector_gather_kernel(
   if (bad) set_err(err, ERR_NAN);
 }
 
-// Persistent row gather over the DOF nodes of every mesh of a batch (R = 1:
-// rows of at most 32 columns); warp w of the grid takes nodes w, w + warps, ...
+// Row gather of a batch by valence class: warp w takes entry w of `list`
+// (item << 32 | DOF node of the item's mesh); every node of a class has at
+// most ms slots and mad adjacent elements, so a launch reserves only its own
+// class's shared memory (as the single-mesh gather's valence buckets do).
 template <int QD>
-__global__ void __launch_bounds__(128) batch_gather_kernel(
-    const BatchItem *__restrict__ items, const int64_t *__restrict__ node0, int nitems,
-    int64_t nnodes, size_t warp_bytes) {
+__global__ void __launch_bounds__(128) batch_gather_list_kernel(
+    const BatchItem *__restrict__ items, const int64_t *__restrict__ list, int64_t n, int ms,
+    int mad, size_t warp_bytes) {
   extern __shared__ __align__(16) double dsm[];
   const int wib = threadIdx.x >> 5;
+  const int64_t g = blockIdx.x * int64_t(blockDim.x >> 5) + wib;
+  if (g >= n) return;
   char *base = reinterpret_cast<char *>(dsm) + wib * warp_bytes;
-  const int64_t nw = int64_t(gridDim.x) * (blockDim.x >> 5);
-  for (int64_t g = blockIdx.x * int64_t(blockDim.x >> 5) + wib; g < nnodes; g += nw) {
-    int lo = 0, hi = nitems - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (node0[mid] <= g) lo = mid;
-      else hi = mid - 1;
-    }
-    const BatchItem &it = items[lo];
-    if (it.qd != QD) continue;
-    __syncwarp();
-    gather_node<QD, 1>(base, g - node0[lo], it.L, it.adj_ptr, it.adj, it.elem, it.ms, it.mad,
-                       it.nptr, it.nbits, it.slotmap, it.rowptr, it.vals, true, true, it.vec,
-                       it.err, it.ncol, it.u);
-  }
+  const int64_t code = list[g];
+  const BatchItem &it = items[code >> 32];
+  gather_node<QD, 1>(base, code & 0xffffffffll, it.L, it.adj_ptr, it.adj, it.elem, ms, mad,
+                     it.nptr, it.nbits, it.slotmap, it.rowptr, it.vals, true, true, it.vec, it.err,
+                     it.ncol, it.u);
 }
 
 size_t pattern_smem(int cap) { return size_t(kWarpsPerBlock) * (3 * cap + kMaxLocal) * sizeof(int); }
@@ -737,27 +731,28 @@ cudaError_t launch_upper_fill(Plan &P, int32_t *d_ucol) {
   return cudaGetLastError();
 }
 
-size_t batch_gather_warp_bytes(const BatchItem &it) {
-  return gather_warp_bytes(it.ms, it.qd, it.L.rowblk, it.mad);
+size_t batch_gather_class_bytes(const BatchItem &it, int ms, int mad) {
+  return gather_warp_bytes(ms, it.qd, it.L.rowblk, mad);
 }
 
-cudaError_t launch_batch_gather(const BatchItem *items, const int64_t *node0, int nitems,
-                               int64_t nnodes, int qd, int grid, size_t warp_bytes,
-                               cudaStream_t st) {
-  if (nnodes == 0) return cudaSuccess;
+cudaError_t launch_batch_gather_list(const BatchItem *items, const int64_t *list, int64_t n,
+                                     int qd, int ms, int mad, size_t warp_bytes,
+                                     cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
   const size_t smem = size_t(kWarpsPerBlock) * warp_bytes;
+  const unsigned blocks = unsigned((n + kWarpsPerBlock - 1) / kWarpsPerBlock);
   switch (qd) {
     case 1:
-      batch_gather_kernel<1><<<grid, kWarpsPerBlock * 32, smem, st>>>(items, node0, nitems, nnodes,
-                                                                       warp_bytes);
+      batch_gather_list_kernel<1><<<blocks, kWarpsPerBlock * 32, smem, st>>>(items, list, n, ms,
+                                                                              mad, warp_bytes);
       break;
     case 2:
-      batch_gather_kernel<2><<<grid, kWarpsPerBlock * 32, smem, st>>>(items, node0, nitems, nnodes,
-                                                                       warp_bytes);
+      batch_gather_list_kernel<2><<<blocks, kWarpsPerBlock * 32, smem, st>>>(items, list, n, ms,
+                                                                              mad, warp_bytes);
       break;
     case 3:
-      batch_gather_kernel<3><<<grid, kWarpsPerBlock * 32, smem, st>>>(items, node0, nitems, nnodes,
-                                                                       warp_bytes);
+      batch_gather_list_kernel<3><<<blocks, kWarpsPerBlock * 32, smem, st>>>(items, list, n, ms,
+                                                                              mad, warp_bytes);
       break;
     default: return cudaErrorInvalidValue;
   }
@@ -766,14 +761,16 @@ cudaError_t launch_batch_gather(const BatchItem *items, const int64_t *node0, in
 
 cudaError_t batch_gather_attr(size_t smem) {
   cudaError_t ce;
-  if ((ce = cudaFuncSetAttribute(batch_gather_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 int(smem))) != cudaSuccess)
+  if ((ce = cudaFuncSetAttribute(batch_gather_list_kernel<1>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem))) !=
+      cudaSuccess)
     return ce;
-  if ((ce = cudaFuncSetAttribute(batch_gather_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 int(smem))) != cudaSuccess)
+  if ((ce = cudaFuncSetAttribute(batch_gather_list_kernel<2>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem))) !=
+      cudaSuccess)
     return ce;
-  return cudaFuncSetAttribute(batch_gather_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              int(smem));
+  return cudaFuncSetAttribute(batch_gather_list_kernel<3>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
 }
 
 cudaError_t launch_gather_range(Plan &P, bool want_K, bool want_R, int64_t n0, int64_t n1) {

@@ -298,11 +298,9 @@ void simplex_source_of(const Plan &P, const double *&fsrc, double &fscale, bool 
 constexpr int kBatchElementTypes = 16;
 cudaError_t launch_batch_element_pass(const BatchItem *items, const int64_t *tile0, int nitems,
                                      int64_t ntiles, int grid, int etype, cudaStream_t st);
-size_t batch_gather_warp_bytes(const BatchItem &it);
-cudaError_t launch_batch_gather(const BatchItem *items, const int64_t *node0, int nitems,
-                               int64_t nnodes, int qd, int grid, size_t warp_bytes,
-                               cudaStream_t st);
-
+size_t batch_gather_class_bytes(const BatchItem &it, int ms, int mad);
+cudaError_t launch_batch_gather_list(const BatchItem *items, const int64_t *list, int64_t n,
+                                     int qd, int ms, int mad, size_t warp_bytes, cudaStream_t st);
 // kernels (k_simplex.cu)
 // tiles [tile0, tile1) of 32 elements (tile1 < 0: to the last element);
 // ku: V_e includes K_e u_e (false: the load only, K u formed by the gather)

@@ -364,12 +364,15 @@ typedef struct gfgpu_batch_s gfgpu_batch;
    whose data pointers change must be re-batched. */
 int gfgpu_batch_create(gfgpu_plan *const *plans, int32_t n, gfgpu_batch **out);
 /* K values and order-1 vectors of every plan of the batch: one persistent
-   element-pass launch over the elements of all meshes and one persistent
-   row-gather launch per component count, on `stream`.  Only kernel launches
-   are issued, so the call can be captured in a CUDA graph and replayed. */
+   element-pass launch per element type over the elements of all its meshes,
+   and one row-gather launch per component count and valence class (the DOF
+   nodes of all meshes with at most 2^c adjacent elements), on `stream`.
+   Only kernel launches are issued, so the call can be captured in a CUDA
+   graph and replayed. */
 int gfgpu_batch_assemble(gfgpu_batch *batch, void *cuda_stream);
-/* Times the two launches over grid sizes of 1, 2, 4, ..., 32 blocks per SM
-   and keeps the fastest of each (optional outputs: the chosen grids). */
+/* Times the element-pass launches over grid sizes of 1, 2, 4, ..., 32
+   blocks per SM and keeps the fastest (optional outputs: that grid, and the
+   number of row-gather launches, whose grids follow their node counts). */
 int gfgpu_batch_tune(gfgpu_batch *batch, void *cuda_stream, int32_t *grid_elem,
                      int32_t *grid_gather);
 /* Waits for `stream` and reports the batch's device error word. */
