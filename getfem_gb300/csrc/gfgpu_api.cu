@@ -1191,7 +1191,7 @@ int gfgpu_batch_assemble(gfgpu_batch *B, void *stream) {
   return batch_launch(B, static_cast<cudaStream_t>(stream), B->grid_ep);
 }
 
-int gfgpu_batch_tune(gfgpu_batch *B, void *stream, int32_t *grid_ep, int32_t *grid_ga) {
+int gfgpu_batch_tune(gfgpu_batch *B, void *stream, int32_t *grid_ep, int32_t *gather_launches) {
   if (!B) return GFGPU_E_INVALID;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   int dev = 0, sms = 0;
@@ -1225,7 +1225,7 @@ int gfgpu_batch_tune(gfgpu_batch *B, void *stream, int32_t *grid_ep, int32_t *gr
     for (const auto &k : B->gclass[q]) nga += k.n > 0;
   B->grid_ga = nga;
   if (grid_ep) *grid_ep = B->grid_ep;
-  if (grid_ga) *grid_ga = B->grid_ga;
+  if (gather_launches) *gather_launches = B->grid_ga;
   return GFGPU_OK;
 }
 

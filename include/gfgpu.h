@@ -374,7 +374,7 @@ int gfgpu_batch_assemble(gfgpu_batch *batch, void *cuda_stream);
    blocks per SM and keeps the fastest (optional outputs: that grid, and the
    number of row-gather launches, whose grids follow their node counts). */
 int gfgpu_batch_tune(gfgpu_batch *batch, void *cuda_stream, int32_t *grid_elem,
-                     int32_t *grid_gather);
+                     int32_t *gather_launches);
 /* Waits for `stream` and reports the batch's device error word. */
 int gfgpu_batch_sync(gfgpu_batch *batch, void *cuda_stream);
 int64_t gfgpu_batch_elements(gfgpu_batch *batch);
