@@ -232,9 +232,14 @@ void spmv(const Plan &P, const double *x, double *y, const double *w, double *pa
 // iteration; the multi-kernel loop spent ~45 us per iteration on launches
 // and the stop-test read at 4225 unknowns).  Dot products: per-thread
 // partials over rows tid, tid + 1024, ..., then a warp tree and a tree over
-// the 32 warps, in a fixed order.  The loop is bounded by maxiter.
+// the 32 warps, in a fixed order.  A launch runs at most `seg` iterations
+// and leaves the recurrence state in st[] (st[0] iterations, st[1] the
+// relative residual, st[2] ||r||, st[3] rho, st[4] r.r, st[5] z.r,
+// st[6] 1 when done, st[7] ||b||); the host launches again until done, so a
+// large maxiter never makes one long-running kernel.
 constexpr int kCgSmallThreads = 1024;
 constexpr int64_t kCgSmallMax = 32768;
+constexpr int64_t kCgSegment = 2000;  // ~20 ms of iterations at 4225 unknowns
 
 __device__ __forceinline__ double block_sum_1024(double v, double *sh) {
 #pragma unroll
@@ -253,7 +258,8 @@ __global__ void __launch_bounds__(kCgSmallThreads, 1) cg_small_kernel(
     int64_t n, const int64_t *__restrict__ rowptr, const int32_t *__restrict__ colidx,
     const double *__restrict__ vals, const double *__restrict__ b, double *__restrict__ x,
     double *__restrict__ r, double *__restrict__ p, double *__restrict__ q, double *z,
-    const double *__restrict__ dinv, double resmax, int64_t maxiter, double *__restrict__ out) {
+    const double *__restrict__ dinv, double resmax, int64_t maxiter, int resume, int64_t seg,
+    double *__restrict__ st) {
   __shared__ double sh[32];
   const int tid = threadIdx.x;
   constexpr int T = kCgSmallThreads;
@@ -264,68 +270,84 @@ __global__ void __launch_bounds__(kCgSmallThreads, 1) cg_small_kernel(
       y[i] = s;
     }
   };
-  double bb = 0.0;
-  for (int64_t i = tid; i < n; i += T) bb = fma(b[i], b[i], bb);
-  const double rhsn = sqrt(fabs(block_sum_1024(bb, sh)));
-  int64_t nit = 0;
-  double res = 0.0;
-  if (rhsn == 0.0) {
-    for (int64_t i = tid; i < n; i += T) x[i] = 0.0;
-  } else {
+  const double *zz = dinv ? z : r;
+  double rhsn, rho, rr, zr = 0.0, res = 0.0;
+  int64_t nit;
+  if (!resume) {
+    double bb = 0.0;
+    for (int64_t i = tid; i < n; i += T) bb = fma(b[i], b[i], bb);
+    rhsn = sqrt(fabs(block_sum_1024(bb, sh)));
+    nit = 0;
+    if (rhsn == 0.0) {
+      for (int64_t i = tid; i < n; i += T) x[i] = 0.0;
+      if (tid == 0) {
+        st[0] = 0.0, st[1] = 0.0, st[2] = 0.0, st[6] = 1.0, st[7] = 0.0;
+      }
+      return;
+    }
     // r = b - A x; z = P r; rho = z.r; p = z
     spmv(x, q);
     __syncthreads();
-    double rr = 0.0, zr = 0.0;
+    double r2 = 0.0, z2 = 0.0;
     for (int64_t i = tid; i < n; i += T) {
       const double ri = b[i] - q[i];
       r[i] = ri;
       const double zi = dinv ? dinv[i] * ri : ri;
       if (dinv) z[i] = zi;
       p[i] = zi;
-      rr = fma(ri, ri, rr);
-      zr = fma(zi, ri, zr);
+      r2 = fma(ri, ri, r2);
+      z2 = fma(zi, ri, z2);
     }
-    rr = block_sum_1024(rr, sh);
-    double rho = dinv ? block_sum_1024(zr, sh) : rr;
-    const double *zz = dinv ? z : r;
-    for (;;) {
-      res = sqrt(rr);
-      if (isnan(res) || res <= rhsn * resmax || nit >= maxiter) break;
-      if (nit > 0) {
-        const double rho_old = rho;
-        rho = dinv ? zr : rr;
-        const double beta = rho / rho_old;
-        for (int64_t i = tid; i < n; i += T) p[i] = fma(beta, p[i], zz[i]);
-        __syncthreads();
-      }
-      // q = A p; alpha = rho / q.p; x += alpha p; r -= alpha q; z = P r
-      spmv(p, q);
-      double qp = 0.0;
-      for (int64_t i = tid; i < n; i += T) qp = fma(q[i], p[i], qp);
-      qp = block_sum_1024(qp, sh);
-      const double alpha = rho / qp;
-      rr = 0.0;
-      zr = 0.0;
-      for (int64_t i = tid; i < n; i += T) {
-        x[i] = fma(alpha, p[i], x[i]);
-        const double ri = fma(-alpha, q[i], r[i]);
-        r[i] = ri;
-        rr = fma(ri, ri, rr);
-        if (dinv) {
-          const double zi = dinv[i] * ri;
-          z[i] = zi;
-          zr = fma(zi, ri, zr);
-        }
-      }
-      rr = block_sum_1024(rr, sh);
-      if (dinv) zr = block_sum_1024(zr, sh);
-      ++nit;
+    rr = block_sum_1024(r2, sh);
+    rho = dinv ? block_sum_1024(z2, sh) : rr;
+  } else {
+    nit = int64_t(st[0]);
+    rho = st[3], rr = st[4], zr = st[5], rhsn = st[7];
+  }
+  bool done = false;
+  for (int64_t k = 0;; ++k) {
+    res = sqrt(rr);
+    if (isnan(res) || res <= rhsn * resmax || nit >= maxiter) {
+      done = true;
+      break;
     }
+    if (k >= seg) break;
+    if (nit > 0) {
+      const double rho_old = rho;
+      rho = dinv ? zr : rr;
+      const double beta = rho / rho_old;
+      for (int64_t i = tid; i < n; i += T) p[i] = fma(beta, p[i], zz[i]);
+      __syncthreads();
+    }
+    // q = A p; alpha = rho / q.p; x += alpha p; r -= alpha q; z = P r
+    spmv(p, q);
+    double qp = 0.0;
+    for (int64_t i = tid; i < n; i += T) qp = fma(q[i], p[i], qp);
+    qp = block_sum_1024(qp, sh);
+    const double alpha = rho / qp;
+    double r2 = 0.0, z2 = 0.0;
+    for (int64_t i = tid; i < n; i += T) {
+      x[i] = fma(alpha, p[i], x[i]);
+      const double ri = fma(-alpha, q[i], r[i]);
+      r[i] = ri;
+      r2 = fma(ri, ri, r2);
+      if (dinv) {
+        const double zi = dinv[i] * ri;
+        z[i] = zi;
+        z2 = fma(zi, ri, z2);
+      }
+    }
+    rr = block_sum_1024(r2, sh);
+    if (dinv) zr = block_sum_1024(z2, sh);
+    ++nit;
   }
   if (tid == 0) {
-    out[0] = double(nit);
-    out[1] = rhsn == 0.0 ? 0.0 : res / rhsn;
-    out[2] = res;
+    st[0] = double(nit);
+    st[1] = res / rhsn;
+    st[2] = res;
+    st[3] = rho, st[4] = rr, st[5] = zr;
+    st[6] = done ? 1.0 : 0.0;
+    st[7] = rhsn;
   }
 }
 
@@ -443,19 +465,24 @@ extern "C" int gfgpu_cg(gfgpu_plan *plan, const double *b, double *x, double res
   }
   SOLVE_CUDA(cudaMemsetAsync(P->d_err, 0, sizeof(int), st));
   const unsigned eb = unsigned((n + 255) / 256);
-  double h[3];
+  double h[8];
   if (n <= kCgSmallMax) {
-    // one block runs the whole solve
-    if (precond == 1)
+    // one block runs the solve, kCgSegment iterations per launch
+    if (precond == 1) {
       diag_inverse<<<eb, 256, 0, st>>>(n, P->d_rowptr, P->d_colidx, P->d_vals, W.dinv, P->d_err);
-    cg_small_kernel<<<1, kCgSmallThreads, 0, st>>>(n, P->d_rowptr, P->d_colidx, P->d_vals, b, x,
-                                                   W.r, W.p, W.q, W.z,
-                                                   precond == 1 ? W.dinv : nullptr, resmax,
-                                                   maxiter, W.sc);
-    SOLVE_CUDA(cudaGetLastError());
-    SOLVE_CUDA(cudaMemcpyAsync(h, W.sc, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
-    SOLVE_CUDA(cudaStreamSynchronize(st));
-    P->launches += precond == 1 ? 2 : 1;
+      P->launches++;
+    }
+    for (int resume = 0;; resume = 1) {
+      cg_small_kernel<<<1, kCgSmallThreads, 0, st>>>(n, P->d_rowptr, P->d_colidx, P->d_vals, b,
+                                                     x, W.r, W.p, W.q, W.z,
+                                                     precond == 1 ? W.dinv : nullptr, resmax,
+                                                     maxiter, resume, kCgSegment, W.sc);
+      P->launches++;
+      SOLVE_CUDA(cudaGetLastError());
+      SOLVE_CUDA(cudaMemcpyAsync(h, W.sc, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
+      SOLVE_CUDA(cudaStreamSynchronize(st));
+      if (h[6] != 0.0) break;
+    }
     if (iterations) *iterations = int64_t(h[0]);
     if (residual) *residual = h[1];
     int rc = read_err(*P);

@@ -44,3 +44,23 @@ def test_poisson_cg_matches_reference(precond):
         assert abs(info["iterations"] - int(rec["cg_iterations"][0])) <= 3
         u2, info2 = solvers.solve_linear(ws, dofs, resmax=1e-12, precond=precond)
         assert torch.equal(u, u2) and info2["iterations"] == info["iterations"]
+
+
+@pytest.mark.gpu
+def test_cg_runs_past_one_launch_segment():
+    """A small system's CG runs in one block, at most 2000 iterations per
+    launch, the host relaunching from the saved recurrence state.  With
+    resmax = 0 the solve only stops when the residual is exactly zero (here
+    after more than one launch); the solution is that of the converged solve,
+    and the run is reproducible bit for bit."""
+    torch = pytest.importorskip("torch")
+    rec = load("p1tri_poisson_cg")
+    mesh, mf, mim, ws = build_case(rec)
+    dofs = solvers.boundary_dofs(mf)
+    u1, info1 = solvers.solve_linear(ws, dofs, resmax=1e-12)
+    u2, info2 = solvers.solve_linear(ws, dofs, resmax=0.0, maxiter=45000)
+    u3, info3 = solvers.solve_linear(ws, dofs, resmax=0.0, maxiter=45000)
+    assert info2["iterations"] > 2000 and info3["iterations"] == info2["iterations"]
+    assert torch.equal(u2, u3)
+    x1, x2 = u1.cpu().numpy(), u2.cpu().numpy()
+    assert np.abs(x2 - x1).max() <= 1e-9 * np.abs(x1).max()
