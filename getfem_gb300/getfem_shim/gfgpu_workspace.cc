@@ -49,6 +49,12 @@ namespace {
 struct PlanEntry {
   gfgpu_plan *plan = nullptr;
   std::vector<bgeot::size_type> cvs;  // the plan's elements, in order
+  // the CSR pattern on the host, copied when the plan's pattern is built or
+  // grows (its nnz changes: a repaired pattern only gains entries), not on
+  // every assembly
+  std::vector<int64_t> rowptr;
+  std::vector<int32_t> colidx;
+  std::vector<double> vals;
   ~PlanEntry() {
     if (plan) gfgpu_plan_destroy(plan);
   }
@@ -308,12 +314,15 @@ void assemble(getfem::ga_workspace &ws, size_t order, getfem::model_real_sparse_
       check(gfgpu_sync(E.plan), "matrix assembly");
       int64_t nr = 0, nnz = 0;
       check(gfgpu_pattern_size(E.plan, &nr, &nnz), "pattern");
-      std::vector<int64_t> rowptr(static_cast<size_t>(nr) + 1);
-      std::vector<int32_t> colidx(static_cast<size_t>(nnz));
-      std::vector<double> vals(static_cast<size_t>(nnz));
-      check(gfgpu_pattern_copy(E.plan, rowptr.data(), colidx.data()), "pattern copy");
-      check(gfgpu_copy_result(E.plan, GFGPU_RESULT_VALUES, vals.data()), "values copy");
-      add_csr(*K, off, rowptr, colidx, vals);
+      if (E.rowptr.size() != static_cast<size_t>(nr) + 1 ||
+          E.colidx.size() != static_cast<size_t>(nnz)) {
+        E.rowptr.assign(static_cast<size_t>(nr) + 1, 0);
+        E.colidx.assign(static_cast<size_t>(nnz), 0);
+        check(gfgpu_pattern_copy(E.plan, E.rowptr.data(), E.colidx.data()), "pattern copy");
+      }
+      E.vals.resize(static_cast<size_t>(nnz));
+      check(gfgpu_copy_result(E.plan, GFGPU_RESULT_VALUES, E.vals.data()), "values copy");
+      add_csr(*K, off, E.rowptr, E.colidx, E.vals);
     }
   }
 }
