@@ -1055,8 +1055,6 @@ int gfgpu_batch_create(gfgpu_plan *const *plans, int32_t n, gfgpu_batch **out) {
     it.err = B->d_err;
     it.adj_ptr = P.d_adj_ptr;
     it.adj = P.d_adj;
-    it.ms = P.max_slots < 1 ? 1 : P.max_slots;
-    it.mad = P.max_adj < 1 ? 1 : P.max_adj;
     it.nptr = P.d_nptr;
     it.nbits = P.d_nbits;
     it.slotmap = P.d_slotmap;

@@ -281,7 +281,6 @@ struct BatchItem {
   double *elem = nullptr;
   int *err = nullptr;
   const int32_t *adj_ptr = nullptr, *adj = nullptr;
-  int32_t ms = 1, mad = 1;
   const int64_t *nptr = nullptr;
   const uint16_t *nbits = nullptr;
   const int16_t *slotmap = nullptr;
