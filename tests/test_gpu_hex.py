@@ -233,7 +233,7 @@ def test_opt_in_sum_factorisation_high_order(case):
     assert 0.0 < err <= 1e-8, err
 
 
-@pytest.mark.parametrize("degree", [3, 4])
+@pytest.mark.parametrize("degree", [1, 3, 4])
 def test_vector_pass_axis_aligned(degree):
     """The vector-only pass of kappa*Grad_u.Grad_Test_u on an axis-aligned
     mesh goes through the three diagonal metric tables only (the off-diagonal

@@ -215,7 +215,8 @@ def test_points_moved_off_parallelepipeds():
     L.check(lib.gfgpu_sync(h1))
 
 
-@pytest.mark.parametrize("shear,degree", [(False, 2), (True, 2), (False, 4), (True, 4)])
+@pytest.mark.parametrize("shear,degree", [(False, 1), (True, 1), (False, 2), (True, 2),
+                                          (False, 4), (True, 4)])
 def test_parallelepiped_scalar_potential_and_coefficient_gradient(shear, degree):
     """kappa*Grad_u.Grad_u on parallelepiped hexahedra, where the potential
     and dE/dkappa go through the plan's reference tensors: the 3 diagonal
@@ -229,7 +230,7 @@ def test_parallelepiped_scalar_potential_and_coefficient_gradient(shear, degree)
         A = np.array([[1.0, 0.3, -0.2], [0.1, 0.9, 0.25], [-0.15, 0.05, 1.1]])
         mesh = g.Mesh(3, mesh.kind, np.ascontiguousarray(mesh.points @ A.T), mesh.cvpts)
     mf = g.MeshFem(mesh, 1, degree=degree)
-    im = "IM_GAUSS_PARALLELEPIPED(3,%d)" % (5 if degree == 2 else 9)
+    im = "IM_GAUSS_PARALLELEPIPED(3,%d)" % {1: 3, 2: 5, 4: 9}[degree]
     mim = g.MeshIm(mesh, im)
     u0 = rng.standard_normal(mf.nb_dof())
     k0 = np.exp(rng.normal(0, 0.5, mesh.nb_convex()))
