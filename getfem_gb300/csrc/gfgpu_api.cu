@@ -1195,9 +1195,17 @@ int gfgpu_batch_tune(gfgpu_batch *B, void *stream, int32_t *grid_ep, int32_t *ga
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaEvent_t e0, e1;
-  GF_CUDA(cudaEventCreate(&e0));
-  GF_CUDA(cudaEventCreate(&e1));
+  // the timing events, destroyed on every return
+  struct Events {
+    cudaEvent_t e[2] = {};
+    ~Events() {
+      for (cudaEvent_t x : e)
+        if (x) cudaEventDestroy(x);
+    }
+  } ev;
+  GF_CUDA(cudaEventCreate(&ev.e[0]));
+  GF_CUDA(cudaEventCreate(&ev.e[1]));
+  cudaEvent_t e0 = ev.e[0], e1 = ev.e[1];
   const int mult[] = {1, 2, 4, 8, 16, 32};
   float best_ep = 1e30f;
   for (int m : mult) {
@@ -1215,8 +1223,6 @@ int gfgpu_batch_tune(gfgpu_batch *B, void *stream, int32_t *grid_ep, int32_t *ga
     }
     if (t_ep < best_ep) best_ep = t_ep, B->grid_ep = g;
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   // the gathers are one launch per component count and valence class
   int nga = 0;
   for (int q = 1; q <= 3; ++q)

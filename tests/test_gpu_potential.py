@@ -74,6 +74,7 @@ def test_nh_adjoint_against_finite_differences(kind):
     E = pot(u, points=X, mu=mu)
     E.backward()
     gu, gX, gmu = u.grad.clone(), X.grad.clone(), mu.grad.clone()
+    E = E.detach()
 
     def energy(uu, XX, mm):
         with torch.no_grad():
