@@ -352,7 +352,7 @@ int gfgpu_cg(gfgpu_plan *plan, const double *b, double *x, double resmax, int64_
              int32_t precond, int64_t *iterations, double *residual);
 
 /* ------------------------------------------------------------------ */
-/* Batched assembly of many meshes (independent plans) in one launch.  */
+/* Batched assembly of many meshes (independent plans), few launches. */
 /* The reference assembles one mesh per ga_workspace::assembly call;   */
 /* a batch replaces a loop of such calls over independent workspaces.  */
 typedef struct gfgpu_batch_s gfgpu_batch;
@@ -367,8 +367,8 @@ int gfgpu_batch_create(gfgpu_plan *const *plans, int32_t n, gfgpu_batch **out);
    element-pass launch per element type over the elements of all its meshes,
    and one row-gather launch per component count and valence class (the DOF
    nodes of all meshes with at most 2^c adjacent elements), on `stream`.
-   Only kernel launches are issued, so the call can be captured in a CUDA
-   graph and replayed. */
+   Only kernel launches and a memset of the error word are issued, so the
+   call can be captured in a CUDA graph and replayed. */
 int gfgpu_batch_assemble(gfgpu_batch *batch, void *cuda_stream);
 /* Times the element-pass launches over grid sizes of 1, 2, 4, ..., 32
    blocks per SM and keeps the fastest (optional outputs: that grid, and the
