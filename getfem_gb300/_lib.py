@@ -16,7 +16,9 @@ OK, E_INVALID, E_UNSUPPORTED, E_CUDA, E_JACOBIAN, E_NAN, E_TIMEOUT, E_NOMEM, E_S
 SIMPLEX, HEX = 0, 1
 COEF_NONE, COEF_CONST, COEF_ELEMENT, COEF_NODAL = 0, 1, 2, 3
 TERM_GRADGRAD, TERM_MASS, TERM_SOURCE, TERM_NEOHOOKEAN, TERM_INTERNAL_P = 1, 2, 3, 4, 5
+TERM_GRADGRAD_TENSOR = 6
 MAX_TERMS = 8
+MAX_TENSOR = 81
 MAX_SLOTS = 8
 SLOT_U = 0
 REBUILD_PATTERN = 1
@@ -57,7 +59,8 @@ class Term(C.Structure):
 
 
 class Form(C.Structure):
-    _fields_ = [("n_terms", C.c_int32), ("terms", Term * MAX_TERMS)]
+    _fields_ = [("n_terms", C.c_int32), ("terms", Term * MAX_TERMS),
+                ("tensor", C.c_double * MAX_TENSOR)]
 
 
 class Space(C.Structure):

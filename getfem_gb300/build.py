@@ -19,8 +19,8 @@ LIB = os.path.join(HERE, "libgfgpu.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 HOST_SOURCES = ["host/refelem.cc", "gfgpu_host.cc"]
-CUDA_SOURCES = ["gfgpu_api.cu", "k_simplex.cu", "k_assemble.cu", "k_probe.cu", "k_noalloc.cu",
-                "k_hex.cu", "k_gauss.cu", "k_affine_hex.cu",
+CUDA_SOURCES = ["gfgpu_api.cu", "k_simplex.cu", "k_simplex_ten.cu", "k_assemble.cu",
+                "k_probe.cu", "k_noalloc.cu", "k_hex.cu", "k_gauss.cu", "k_affine_hex.cu",
                 "k_solve.cu", "k_dofs.cu"]
 # per-file nvcc flags: the Gauss-point kernels round like the reference's
 # sequence of products and sums (no implicit contraction; explicit fma only)
@@ -52,7 +52,7 @@ def build(verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     headers = []
     for root, _, files in os.walk(CSRC):
-        headers += [os.path.join(root, f) for f in files if f.endswith(".h")]
+        headers += [os.path.join(root, f) for f in files if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(HERE, "..", "include", "gfgpu.h"))
     jobs = []
     objs = []

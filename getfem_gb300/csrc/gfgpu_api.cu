@@ -6,6 +6,7 @@
 #include <map>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <exception>
 #include <new>
@@ -90,16 +91,46 @@ void dfree(T *&p) {
 
 namespace gfgpu {
 // The forms the affine-simplex element pass lowers: GRADGRAD / MASS with
-// constant or per-element coefficients, SOURCE with a field on the
+// constant or per-element coefficients, one GRADGRAD_TENSOR (a constant
+// symmetric D, constant or per-element factor), SOURCE with a field on the
 // variable's mesh_fem and a constant factor.
 bool simplex_form_supported(const gfgpu_form &f, int qdim, int dim, std::string &why) {
   if (f.n_terms < 1 || f.n_terms > GFGPU_MAX_TERMS) {
     why = "empty form";
     return false;
   }
-  int nsrc = 0;
+  int nsrc = 0, nten = 0;
   for (int t = 0; t < f.n_terms; ++t) {
     const gfgpu_term &T = f.terms[t];
+    if (T.kind == GFGPU_TERM_GRADGRAD_TENSOR) {
+      if (++nten > 1) {
+        why = "at most one anisotropic (tensor) gradient coupling";
+        return false;
+      }
+      if (qdim != 1 && qdim != dim) {
+        why = "qdim must be 1 or the mesh dimension";
+        return false;
+      }
+      if (T.c[0].kind != GFGPU_COEF_NONE && T.c[0].kind != GFGPU_COEF_CONST &&
+          T.c[0].kind != GFGPU_COEF_ELEMENT) {
+        why = "the tensor coupling's factor must be constant or per element";
+        return false;
+      }
+      if (T.c[0].kind == GFGPU_COEF_ELEMENT && (T.c[0].slot < 0 || T.c[0].slot >= GFGPU_MAX_SLOTS)) {
+        why = "bad coefficient slot";
+        return false;
+      }
+      const int nd = qdim * dim;
+      for (int r = 0; r < nd; ++r)
+        for (int c = 0; c < nd; ++c) {
+          const double x = f.tensor[r * nd + c];
+          if (!std::isfinite(x) || x != f.tensor[c * nd + r]) {
+            why = "the coupling tensor must be finite and symmetric, D[(a,k),(b,l)] == D[(b,l),(a,k)]";
+            return false;
+          }
+        }
+      continue;
+    }
     if (T.kind == GFGPU_TERM_GRADGRAD || T.kind == GFGPU_TERM_MASS) {
       int nc = T.kind == GFGPU_TERM_GRADGRAD ? 3 : 1;
       for (int k = 0; k < nc; ++k)
@@ -807,6 +838,11 @@ static int check_slots(Plan &P, bool need_u) {
     const gfgpu_term &T = P.form.terms[t];
     for (int k = 0; k < 3; ++k)
     {
+      if ((T.c[k].kind == GFGPU_COEF_ELEMENT || T.c[k].kind == GFGPU_COEF_NODAL) &&
+          (T.c[k].slot < 0 || T.c[k].slot >= GFGPU_MAX_SLOTS)) {
+        set_last_error("coefficient slot out of range");
+        return GFGPU_E_INVALID;
+      }
       if (T.c[k].kind == GFGPU_COEF_ELEMENT &&
           (!P.slot_ptr[T.c[k].slot] || P.slot_n[T.c[k].slot] != P.n_elements)) {
         set_last_error("per-element coefficient slot not set or of wrong size");
@@ -1031,6 +1067,9 @@ int gfgpu_batch_create(gfgpu_plan *const *plans, int32_t n, gfgpu_batch **out) {
     Plan &P = *plans[i];
     if (!P.affine_simplex)
       return fail(GFGPU_E_UNSUPPORTED, "gfgpu_batch_create: batches take affine-simplex plans");
+    if (form_has_tensor(P.form))
+      return fail(GFGPU_E_UNSUPPORTED,
+                  "gfgpu_batch_create: forms with an anisotropic coupling are not batched");
     if (P.nnz < 0)
       return fail(GFGPU_E_STATE, "gfgpu_batch_create: assemble each plan (order 2) first");
     if (!P.slot_ptr[GFGPU_SLOT_U] || P.slot_n[GFGPU_SLOT_U] != P.n_dof)

@@ -134,6 +134,10 @@ extern "C" int gfgpu_assemble_vector_noalloc(const gfgpu_noalloc_args *A, const 
     set_last_error("gfgpu_assemble_vector_noalloc: form not lowered on simplices: " + why);
     return GFGPU_E_UNSUPPORTED;
   }
+  if (form_has_tensor(*form)) {
+    set_last_error("gfgpu_assemble_vector_noalloc: anisotropic couplings need a plan");
+    return GFGPU_E_UNSUPPORTED;
+  }
   // data slots the element pass reads: u, every per-element coefficient,
   // the load field of a source term
   const bool has_elements = A->n_elements > 0;

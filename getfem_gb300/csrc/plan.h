@@ -305,6 +305,11 @@ cudaError_t launch_batch_gather_list(const BatchItem *items, const int64_t *list
 // ku: V_e includes K_e u_e (false: the load only, K u formed by the gather)
 cudaError_t launch_simplex_element_pass(Plan &P, bool with_u, int64_t tile0 = 0,
                                         int64_t tile1 = -1, bool ku = true);
+// (k_simplex_ten.cu) the same for forms with a GRADGRAD_TENSOR term, which
+// launch_simplex_element_pass hands over to it
+bool form_has_tensor(const gfgpu_form &f);
+cudaError_t launch_simplex_element_pass_tensor(Plan &P, bool with_u, int64_t tile0, int64_t tile1,
+                                               bool ku);
 cudaError_t launch_pattern_count(Plan &P);
 cudaError_t launch_pattern_fill(Plan &P);
 cudaError_t launch_gather(Plan &P, bool want_K, bool want_R);

@@ -435,6 +435,21 @@ Tensor eval(Ctx &C, const pga_tree_node n) {
     case GA_NODE_DIVERG_TEST: return eval_test(C, n, false, true);
     case GA_NODE_PARAMS:
       if (!n->children.empty() && n->children[0]->node_type == GA_NODE_OPERATOR) throw NHOp{};
+      if (n->children.size() >= 3 && n->children[0]->node_type == GA_NODE_RESHAPE) {
+        // Reshape(t, sizes...): the components keep their (Fortran) order;
+        // the sizes are the node's own, fixed by the semantic analysis
+        if (n->test_function_type != 0 && n->test_function_type != size_type(-1))
+          reject("Reshape of an expression with test functions");
+        Tensor A = eval(C, n->children[1]);
+        std::vector<size_t> sz;
+        for (size_t i = 0; i < n->tensor().sizes().size(); ++i) sz.push_back(n->tensor().sizes()[i]);
+        size_t total = 1;
+        for (size_t x : sz) total *= x;
+        if (total != A.size()) reject("Reshape sizes");
+        if (sz.size() == 1 && sz[0] == 1) sz.clear();
+        A.sz = sz;
+        return A;
+      }
       reject("function call " + (n->children.empty() ? std::string("?") : n->children[0]->name) +
              " on non-constant arguments");
     default:
@@ -549,10 +564,22 @@ struct TermSink {
     if (L->form.n_terms >= GFGPU_MAX_TERMS) reject("more than GFGPU_MAX_TERMS terms");
     L->form.terms[L->form.n_terms++] = t;
   }
+  // a GRADGRAD_TENSOR term with its tensor (one per form)
+  void push_tensor(const gfgpu_term &t, const std::vector<double> &D) {
+    for (int k = 0; k < L->form.n_terms; ++k)
+      if (L->form.terms[k].kind == GFGPU_TERM_GRADGRAD_TENSOR)
+        reject("more than one anisotropic gradient coupling in one form");
+    if (D.size() > size_t(GFGPU_MAX_TENSOR)) reject("coupling tensor too large");
+    push(t);
+    for (size_t i = 0; i < D.size(); ++i) L->form.tensor[i] = D[i];
+  }
 };
 
 // GRADGRAD / MASS terms of bilinear blocks (lv/lg x rv/rg), scaled by `sc`.
-void emit_bilinear(Ctx &C, TermSink &S, const Blocks &B, double sc) {
+// With allow_tensor, the gradient coupling of one coefficient source (the
+// constant part, or one per-element datum) may be a constant symmetric
+// anisotropic D[(a,k),(b,l)]: a GRADGRAD_TENSOR term.
+void emit_bilinear(Ctx &C, TermSink &S, const Blocks &B, double sc, bool allow_tensor) {
   const int Q = int(C.Q), N = int(C.N);
   // value-gradient couplings are not lowered
   for (const auto &kv : B.m) {
@@ -561,6 +588,7 @@ void emit_bilinear(Ctx &C, TermSink &S, const Blocks &B, double sc) {
   }
   // per coefficient source (constant = -1, else a data index): c0 c1 c2 cm
   std::map<int, std::array<double, 4>> coefs;
+  std::set<int> aniso;  // sources whose gradient coupling is not isotropic
   auto parts = [&](const Poly &p, int which, const char *what) {
     CoefParts cp = coef_parts(C, p, what);
     coefs[-1][which] += 0.0;
@@ -615,10 +643,44 @@ void emit_bilinear(Ctx &C, TermSink &S, const Blocks &B, double sc) {
             const auto ip = pred.find(m);
             const double g = ig == got.end() ? 0.0 : ig->second;
             const double p = ip == pred.end() ? 0.0 : ip->second;
-            if (!near(g, p, scale))
-              reject(k < 0 ? "anisotropic mass term" : "gradient coupling is not isotropic");
+            if (!near(g, p, scale)) {
+              if (k < 0) reject("anisotropic mass term");
+              // the source whose coupling is not isotropic: the constant, or
+              // one scalar coefficient datum
+              if (m.size() > 1 ||
+                  (m.size() == 1 && (C.syms[m[0]].kind != DATA || C.data[C.syms[m[0]].data].kind == 0)))
+                reject("gradient coupling is not isotropic");
+              aniso.insert(m.empty() ? -1 : C.syms[m[0]].data);
+            }
           }
         }
+  // an anisotropic source: its whole gradient coupling as the tensor
+  int ten_src = -2;
+  std::vector<double> Dten;
+  if (!aniso.empty()) {
+    if (!allow_tensor || (Q != 1 && Q != N)) reject("gradient coupling is not isotropic");
+    if (aniso.size() > 1) reject("anisotropic couplings from more than one coefficient");
+    ten_src = *aniso.begin();
+    const int ND = Q * N;
+    Dten.assign(size_t(ND) * ND, 0.0);
+    Mono key;
+    if (ten_src >= 0) key.push_back(C.sym(DATA, 0, 0, ten_src));
+    for (int a = 0; a < Q; ++a)
+      for (int k = 0; k < N; ++k)
+        for (int b = 0; b < Q; ++b)
+          for (int l = 0; l < N; ++l) {
+            const Poly got = block_at(B, a, k, b, l);
+            const auto it = got.find(key);
+            Dten[size_t(a * N + k) * ND + b * N + l] = it == got.end() ? 0.0 : it->second;
+          }
+    for (int r = 0; r < ND; ++r)
+      for (int c = 0; c < ND; ++c)
+        if (Dten[size_t(r) * ND + c] != Dten[size_t(c) * ND + r])
+          reject("anisotropic gradient coupling is not symmetric");
+    if (ten_src >= 0 && C.data[ten_src].kind != GFGPU_COEF_ELEMENT)
+      reject("anisotropic coupling scaled by a nodal field");
+    coefs[ten_src];  // the source gets its term below
+  }
   // terms: the constant part first, then per datum (GRADGRAD, then MASS)
   std::vector<int> order{-1};
   for (const auto &kv : coefs)
@@ -629,7 +691,13 @@ void emit_bilinear(Ctx &C, TermSink &S, const Blocks &B, double sc) {
     const auto &c = it->second;
     const int kind = src < 0 ? GFGPU_COEF_CONST : C.data[src].kind;
     const int slot = src < 0 ? 0 : S.slot_of(src);
-    if (c[0] != 0.0 || c[1] != 0.0 || c[2] != 0.0) {
+    if (src == ten_src) {
+      gfgpu_term t{};
+      t.kind = GFGPU_TERM_GRADGRAD_TENSOR;
+      t.scale = sc;
+      t.c[0] = src < 0 ? mkcoef(GFGPU_COEF_NONE, 0, 0.0) : mkcoef(kind, slot, 1.0);
+      S.push_tensor(t, Dten);
+    } else if (c[0] != 0.0 || c[1] != 0.0 || c[2] != 0.0) {
       gfgpu_term t{};
       t.kind = GFGPU_TERM_GRADGRAD;
       t.scale = sc;
@@ -906,12 +974,12 @@ std::vector<Lowered> lower_workspace(const getfem::ga_workspace &ws, size_t orde
     if (order == 2) {
       Blocks B;
       split_bilinear(C, P, T1V, T1G, T2V, T2G, B, nullptr);
-      emit_bilinear(C, S, B, 1.0);
+      emit_bilinear(C, S, B, 1.0, true);
     } else if (order == 1) {
       Blocks B;
       Poly rest;
       split_bilinear(C, P, T1V, T1G, UV, UG, B, &rest);
-      emit_bilinear(C, S, B, 1.0);
+      emit_bilinear(C, S, B, 1.0, true);
       emit_source(C, S, rest, 1.0);
     } else {
       // potential: the quadratic part B(u, u) by polarisation, and the
@@ -919,7 +987,8 @@ std::vector<Lowered> lower_workspace(const getfem::ga_workspace &ws, size_t orde
       Blocks B;
       Poly rest;
       split_bilinear(C, P, UV, UG, UV, UG, B, &rest);
-      if (!B.m.empty()) emit_bilinear(C, S, B, 1.0);
+      // (anisotropic couplings are not lowered for potentials)
+      if (!B.m.empty()) emit_bilinear(C, S, B, 1.0, false);
       // rest: monomials linear in u with a field datum (u takes the test
       // function's place for the source matcher)
       Poly lin;
@@ -960,7 +1029,13 @@ std::string to_json(const Lowered &L) {
         << ((c.kind == GFGPU_COEF_ELEMENT || c.kind == GFGPU_COEF_NODAL) ? L.slot_names[c.slot] : "")
         << "\"}";
     }
-    s << "]}";
+    s << "]";
+    if (T.kind == GFGPU_TERM_GRADGRAD_TENSOR) {
+      s << ", \"tensor\": [";
+      for (int i = 0; i < GFGPU_MAX_TENSOR; ++i) s << (i ? ", " : "") << L.form.tensor[i];
+      s << "]";
+    }
+    s << "}";
   }
   s << "]}";
   return s.str();

@@ -16,7 +16,10 @@ lowers an expression to the descriptor of include/gfgpu.h:
     affine in the variable, R(u; v) = a(u, v) - l(v), is identified by
     evaluating it on unit test/trial tensors; a(u, v) must be an isotropic
     gradient coupling D = c0 d_ak d_bl + c1 d_ab d_kl + c2 d_al d_kb plus a
-    mass term, each coefficient linear in the data fields; l must be a
+    mass term, each coefficient linear in the data fields, to which one
+    constant symmetric anisotropic coupling D[(a,k),(b,l)] may be added
+    (times a constant or one per-element field: (A*Grad_u).Grad_Test_u,
+    (Reshape(C,3,3,3,3):Grad_u):Grad_Test_u); l must be a
     field on the variable's mesh_fem times a constant.  Alternative
     spellings of the same weak form therefore lower identically, as the
     reference's own tests require of the CPU compiler
@@ -244,6 +247,13 @@ def _fun(name, args):
         return np.sum(a[0] * a[0])
     if name == "Transpose":
         return a[0].T
+    if name == "Reshape":
+        # components in Fortran order (first index fastest), as GetFEM
+        # stores every tensor
+        dims = [int(round(float(x))) for x in a[1:]]
+        if not dims or int(np.prod(dims)) != a[0].size:
+            raise ParseError("GWFL: Reshape to incompatible sizes")
+        return np.reshape(a[0].ravel(order="F"), dims, order="F")
     if name == "sqr":
         return a[0] * a[0]
     if name == "pow":
@@ -533,15 +543,32 @@ def _lower_linear(tree, var, dim, fields, has_test2, probe=None):
             raise L.UnsupportedExpression(L.E_UNSUPPORTED, "anisotropic mass term")
         c, ok = _iso_fit(gg, Q, N)
         if not ok:
-            raise L.UnsupportedExpression(L.E_UNSUPPORTED,
-                                          "gradient coupling is not isotropic")
-        return cm, c
+            # a constant anisotropic coupling D[(a,k),(b,l)] (test (a,k),
+            # trial (b,l)); K is symmetric only for a symmetric D
+            if Q != 1 and Q != N:
+                raise L.UnsupportedExpression(L.E_UNSUPPORTED,
+                                              "gradient coupling is not isotropic")
+            if not np.array_equal(gg, gg.T):
+                raise L.UnsupportedExpression(
+                    L.E_UNSUPPORTED, "anisotropic gradient coupling is not symmetric")
+            return cm, None, np.array(gg, dtype=float)
+        return cm, c, None
 
     parts = [("", base)] + [(nm, coeffs[nm]) for nm in scal_fields]
+    n_tensor = 0
     for nm, Bflat in parts:
-        cm, c = split(Bflat)
+        cm, c, Dt = split(Bflat)
+        if Dt is not None:
+            n_tensor += 1
+            if n_tensor > 1:
+                raise L.UnsupportedExpression(
+                    L.E_UNSUPPORTED, "anisotropic couplings from more than one coefficient")
         if nm == "":
-            if np.any(np.abs(c) > 0):
+            if Dt is not None:
+                t = _term(L.TERM_GRADGRAD_TENSOR, 1.0, [None, None, None])
+                t["tensor"] = Dt.ravel().tolist()
+                terms2.append(t)
+            elif np.any(np.abs(c) > 0):
                 terms2.append(_term(L.TERM_GRADGRAD, 1.0, [
                     _coef(L.COEF_CONST, 0, float(x)) if x != 0 else _coef(L.COEF_NONE)
                     for x in c]))
@@ -550,7 +577,14 @@ def _lower_linear(tree, var, dim, fields, has_test2, probe=None):
         else:
             f = fields[nm]
             kind = L.COEF_ELEMENT if f.kind == "element" else L.COEF_NODAL
-            if np.any(np.abs(c) > 0):
+            if Dt is not None:
+                if kind != L.COEF_ELEMENT:
+                    raise L.UnsupportedExpression(
+                        L.E_UNSUPPORTED, "anisotropic coupling scaled by a nodal field")
+                t = _term(L.TERM_GRADGRAD_TENSOR, 1.0, [_coef(kind, f.slot, 1.0), None, None])
+                t["tensor"] = Dt.ravel().tolist()
+                terms2.append(t)
+            elif np.any(np.abs(c) > 0):
                 terms2.append(_term(L.TERM_GRADGRAD, 1.0, [
                     _coef(kind, f.slot, float(x)) if x != 0 else _coef(L.COEF_NONE) for x in c]))
             if cm != 0:
@@ -685,6 +719,9 @@ def _lower_potential(tree, var, dim, fields) -> "Lowered":
                                       "potential terms independent of the variable")
     terms2, terms1 = _lower_linear(tree, var, dim, fields, False,
                                    probe=lambda f: _PolarProbe(tree, var, dim, f))
+    if any(t["kind"] == L.TERM_GRADGRAD_TENSOR for t in terms2):
+        raise L.UnsupportedExpression(L.E_UNSUPPORTED,
+                                      "anisotropic couplings in potentials are not lowered")
     # quadratic check: P(2u) = 4 B(u,u) + 2 L(u)
     rng = np.random.default_rng(99)
     Ur, GUr = rng.uniform(-1, 1, Q), rng.uniform(-1, 1, (Q, N))
@@ -891,6 +928,9 @@ def to_form(terms: list) -> L.Form:
     f = L.Form()
     if len(terms) > L.MAX_TERMS:
         raise L.UnsupportedExpression(L.E_UNSUPPORTED, "too many terms")
+    if sum(t["kind"] == L.TERM_GRADGRAD_TENSOR for t in terms) > 1:
+        raise L.UnsupportedExpression(L.E_UNSUPPORTED,
+                                      "more than one anisotropic gradient coupling in one form")
     f.n_terms = len(terms)
     for i, t in enumerate(terms):
         T = f.terms[i]
@@ -908,4 +948,7 @@ def to_form(terms: list) -> L.Form:
                 T.c[k].kind = c["kind"]
                 T.c[k].slot = c["slot"]
                 T.c[k].value = c["value"]
+        if t.get("tensor") is not None:
+            for k, x in enumerate(t["tensor"]):
+                f.tensor[k] = float(x)
     return f

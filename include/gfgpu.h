@@ -93,7 +93,21 @@ typedef enum {
      Gauss-point kernel, at most one such term per form.  Order 1 assembles
      the u residual and the p residual (gfgpu_copy_result
      GFGPU_RESULT_INTERNAL); order 2 needs GFGPU_CONDENSATION. */
-  GFGPU_TERM_INTERNAL_P = 5
+  GFGPU_TERM_INTERNAL_P = 5,
+  /* int (D : Grad_u) : Grad_Test_u with a constant, possibly anisotropic
+     tensor D[(a,k),(b,l)] (test component a, derivative k; trial component
+     b, derivative l): gfgpu_form.tensor holds its (qdim*dim)^2 entries,
+     row (a,k) = a*dim + k, column (b,l) = b*dim + l, and must be symmetric
+     (D[(a,k),(b,l)] == D[(b,l),(a,k)], so that K is).  The term is scaled
+     by scale * c[0] (c[0] NONE: 1; CONST or ELEMENT).  Examples:
+     (A*Grad_u).Grad_Test_u for a scalar field and a symmetric matrix A
+     (D[(0,k),(0,l)] = A[k,l]); (Reshape(C,3,3,3,3):Grad_u):Grad_Test_u
+     for a 3-D vector field and a stiffness C with major symmetry
+     (D[(a,k),(b,l)] = C[a,k,b,l]).  Plans on affine simplices only (the
+     Gauss-point and hexahedral kernels, batches and the allocation-free
+     entry reject it), at most one per form, orders 1 and 2 (not
+     potentials). */
+  GFGPU_TERM_GRADGRAD_TENSOR = 6
 } gfgpu_term_kind;
 
 typedef struct {
@@ -106,9 +120,13 @@ typedef struct {
 } gfgpu_term;
 
 #define GFGPU_MAX_TERMS 8
+/* entries of the constant tensor of a GFGPU_TERM_GRADGRAD_TENSOR term:
+   (qdim*dim)^2 <= 81 */
+#define GFGPU_MAX_TENSOR 81
 typedef struct {
   int32_t n_terms;
   gfgpu_term terms[GFGPU_MAX_TERMS];
+  double tensor[GFGPU_MAX_TENSOR]; /* D of the GRADGRAD_TENSOR term, if any */
 } gfgpu_form;
 
 /* Data slots.  Slot 0 is the variable u (n_dof values). */

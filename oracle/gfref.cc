@@ -519,6 +519,50 @@ void exec_range(Problem &P, int order, int64_t e0, int64_t e1, Outputs &out) {
               t[0] += v;
             }
           }
+        } else if (T.kind == GFGPU_TERM_GRADGRAD_TENSOR) {
+          // (D : Grad_u) : Grad_Test_u, D[(a,k),(b,l)] = tensor[(a*dim+k)*nd + b*dim+l]
+          const double c =
+              (T.c[0].kind == GFGPU_COEF_NONE ? 1.0 : coef_at(p, T.c[0], e, edofs, phi, nb)) * sc;
+          const double *D = p.form.tensor;
+          const int nd = qd * dim;
+          if (order == 2) {
+            for (int j = 0; j < nb; ++j)
+              for (int b = 0; b < qd; ++b)
+                for (int i = 0; i < nb; ++i)
+                  for (int a = 0; a < qd; ++a) {
+                    double v = 0;
+                    for (int k = 0; k < dim; ++k) {
+                      double w = 0;
+                      for (int l = 0; l < dim; ++l)
+                        w += D[(a * dim + k) * nd + b * dim + l] * g[j * dim + l];
+                      v += w * g[i * dim + k];
+                    }
+                    t[size_t(j * qd + b) * s + i * qd + a] += c * v;
+                  }
+          } else {
+            double Gu[9] = {0};
+            for (int j = 0; j < nb; ++j)
+              for (int b = 0; b < qd; ++b) {
+                double uj = p.slots[GFGPU_SLOT_U][edofs[j] + b];
+                for (int l = 0; l < dim; ++l) Gu[b * dim + l] += uj * g[j * dim + l];
+              }
+            // (D : Grad_u)[a,k]
+            double DG[9] = {0};
+            for (int r = 0; r < nd; ++r)
+              for (int q2 = 0; q2 < nd; ++q2) DG[r] += D[r * nd + q2] * Gu[q2];
+            if (order == 1) {
+              for (int i = 0; i < nb; ++i)
+                for (int a = 0; a < qd; ++a) {
+                  double v = 0;
+                  for (int k = 0; k < dim; ++k) v += DG[a * dim + k] * g[i * dim + k];
+                  t[i * qd + a] += c * v;
+                }
+            } else {
+              double v = 0;
+              for (int r = 0; r < nd; ++r) v += DG[r] * Gu[r];
+              t[0] += c * v;
+            }
+          }
         } else if (T.kind == GFGPU_TERM_MASS) {
           double c0 = coef_at(p, T.c[0], e, edofs, phi, nb) * sc;
           if (order == 2) {

@@ -36,7 +36,7 @@ class _Term(C.Structure):
 
 
 class _Form(C.Structure):
-    _fields_ = [("n_terms", C.c_int32), ("terms", _Term * 8)]
+    _fields_ = [("n_terms", C.c_int32), ("terms", _Term * 8), ("tensor", C.c_double * 81)]
 
 
 class _Problem(C.Structure):
@@ -103,6 +103,9 @@ class Problem:
                 c = t["c"][k]
                 if c is not None:
                     T.c[k].kind, T.c[k].slot, T.c[k].value = c["kind"], c["slot"], c["value"]
+            if t.get("tensor") is not None:
+                for k, x in enumerate(t["tensor"]):
+                    P.form.tensor[k] = float(x)
         for s, v in slots.items():
             a = np.ascontiguousarray(v, dtype=np.float64)
             self._keep.append(a)

@@ -77,6 +77,37 @@ CASES = [
 CASES.append(("p1tri_poisson_cg", 2, "PK", 1, 1, "IM_TRIANGLE(2)", 64,
               "Grad_u.Grad_Test_u - f*Test_u", {"f": "V"}, False, "zero"))
 EXTRA = {"p1tri_poisson_cg": ["solve=cg", "resmax=1e-12", "maxiter=100000"]}
+# Constant anisotropic gradient couplings: a symmetric matrix literal for
+# scalar fields, and a 4th-order stiffness with major and minor symmetry
+# (a fixed-size constant of 81 values, Reshape'd in the expression) for 3-D
+# elasticity
+CASES += [
+    ("p2tri_aniso_kappa", 2, "PK", 2, 1, "IM_TRIANGLE(4)", 5,
+     "kappa*([2,0.5;0.5,1]*Grad_u).Grad_Test_u + Grad_u.Grad_Test_u - f*Test_u",
+     {"kappa": "P0", "f": "V"}, True, "normal"),
+    ("p1tet_aniso_mass", 3, "PK", 1, 1, "IM_TETRAHEDRON(2)", 4,
+     "([3,0.5,0.25;0.5,2,0.125;0.25,0.125,1]*Grad_u).Grad_Test_u + u*Test_u",
+     {}, True, "normal"),
+    ("p2tet_aniso_elastic", 3, "PK", 2, 3, "IM_TETRAHEDRON(5)", 3,
+     "(Reshape(Cani,3,3,3,3):Grad_u):Grad_Test_u - f.Test_u",
+     {"Cani": "C", "f": "V"}, True, "normal"),
+]
+
+
+def stiffness_tensor(rng) -> np.ndarray:
+    """C[a,k,b,l] = S[V(a,k), V(b,l)] for a random symmetric positive
+    definite 6 x 6 (Voigt) matrix S: major and minor symmetry exactly."""
+    M = rng.uniform(-0.3, 0.3, (6, 6))
+    S = (M + M.T) / 2 + np.diag(rng.uniform(1.0, 3.0, 6))
+    voigt = {(0, 0): 0, (1, 1): 1, (2, 2): 2, (1, 2): 3, (2, 1): 3, (0, 2): 4, (2, 0): 4,
+             (0, 1): 5, (1, 0): 5}
+    C = np.zeros((3, 3, 3, 3))
+    for a in range(3):
+        for k in range(3):
+            for b in range(3):
+                for l in range(3):
+                    C[a, k, b, l] = S[voigt[a, k], voigt[b, l]]
+    return C
 # Mixed displacement / pressure forms with the pressure p an internal im_data
 # variable (one value per element Gauss point), condensed at order 2: the
 # formulation of the reference's condensation test (tests/test_condensation.cc,
@@ -161,7 +192,9 @@ def make_case(case, seed):
             sigma = 0.3 if cname == "mu" and ukind == "modes" else 0.2
             inputs[cname] = np.exp(rng.normal(0.0, sigma, ndof // qdim))
         elif ck == "C":
-            inputs[cname] = np.array([1.5])
+            # Cani: a stiffness, stored in GetFEM's (Fortran) component order
+            inputs[cname] = (stiffness_tensor(rng).ravel(order="F") if cname == "Cani"
+                             else np.array([1.5]))
     with tempfile.TemporaryDirectory() as td:
         ind = os.path.join(td, "in")
         outd = os.path.join(td, "out")

@@ -72,15 +72,20 @@ def _cpp_lower(cases):
     return out
 
 
-def _canon(kind, scale, field, coefs):
+def _canon(kind, scale, field, coefs, tensor=None):
     """A term with the overall scale folded into the coefficients of the
     GRADGRAD and MASS terms (scale 2, value 1 is the same term as scale 1,
-    value 2)."""
+    value 2); a GRADGRAD_TENSOR term carries its tensor (padded to
+    GFGPU_MAX_TENSOR entries)."""
     if kind in (L.TERM_GRADGRAD, L.TERM_MASS):
         coefs = [(k, v * scale if k else 0.0, d) for k, v, d in coefs]
         scale = 1.0
+    ten = ()
+    if kind == L.TERM_GRADGRAD_TENSOR:
+        t = list(tensor) + [0.0] * (L.MAX_TENSOR - len(tensor))
+        ten = tuple(round(float(x), 12) for x in t)
     return (kind, round(scale, 12), field,
-            tuple((k, round(v, 12), d) for k, v, d in coefs))
+            tuple((k, round(v, 12), d) for k, v, d in coefs), ten)
 
 
 def _canon_cpp(forms):
@@ -88,7 +93,8 @@ def _canon_cpp(forms):
     for f in forms:
         for t in f["terms"]:
             terms.append(_canon(t["kind"], t["scale"], t["field"],
-                                [(c["kind"], c["value"], c["data"]) for c in t["c"]]))
+                                [(c["kind"], c["value"], c["data"]) for c in t["c"]],
+                                t.get("tensor")))
     return sorted(terms)
 
 
@@ -104,7 +110,7 @@ def _canon_py(ws, terms):
                 data = by_slot[c["slot"]] if c["kind"] in (L.COEF_ELEMENT, L.COEF_NODAL) else ""
                 cs.append((c["kind"], c["value"], data))
         field = by_slot[t["field_slot"]] if t["kind"] == L.TERM_SOURCE else ""
-        out.append(_canon(t["kind"], t["scale"], field, cs))
+        out.append(_canon(t["kind"], t["scale"], field, cs, t.get("tensor")))
     return sorted(out)
 
 
@@ -141,7 +147,11 @@ UNSUPPORTED = [
     ("sin_of_data", 2, "PK", 1, 1, "IM_TRIANGLE(2)", "sin(kappa)*Grad_u.Grad_Test_u", "kappa:P0"),
     ("data_squared", 2, "PK", 1, 1, "IM_TRIANGLE(2)", "kappa*kappa*Grad_u.Grad_Test_u", "kappa:P0"),
     ("value_gradient", 2, "PK", 1, 1, "IM_TRIANGLE(2)", "Grad_u(1)*Test_u", ""),
-    ("anisotropic", 3, "PK", 1, 3, "IM_TETRAHEDRON(2)", "Grad_u(1,1)*Grad_Test_u(1,1)", ""),
+    ("anisotropic_unsymmetric", 3, "PK", 1, 3, "IM_TETRAHEDRON(2)",
+     "Grad_u(1,2)*Grad_Test_u(1,1)", ""),
+    ("anisotropic_potential", 2, "PK", 1, 1, "IM_TRIANGLE(2)", "([2,0.5;0.5,1]*Grad_u).Grad_u", ""),
+    ("two_anisotropic_sources", 2, "PK", 1, 1, "IM_TRIANGLE(2)",
+     "kappa*([2,0;0,1]*Grad_u).Grad_Test_u + ([1,0.5;0.5,1]*Grad_u).Grad_Test_u", "kappa:P0"),
     ("constant_source", 2, "PK", 1, 1, "IM_TRIANGLE(2)", "Grad_u.Grad_Test_u - 3*Test_u", ""),
     ("gradient_source", 2, "PK", 1, 1, "IM_TRIANGLE(2)", "Grad_u.Grad_Test_u - Grad_f.Grad_Test_u",
      "f:V"),
@@ -213,7 +223,7 @@ def _csr(res, n):
 
 
 SHIM_CASES = ["p1tri_poisson", "p2tri_elastic", "p2tet_elastic", "q2hex_elastic_nodal",
-              "q2hex_neohookean", "q4hex_laplace", "q1hex_nodal_kappa"]
+              "q2hex_neohookean", "q4hex_laplace", "q1hex_nodal_kappa", "p2tet_aniso_elastic"]
 
 
 @pytest.mark.gpu
