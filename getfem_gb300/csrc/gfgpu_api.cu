@@ -496,8 +496,11 @@ int gfgpu_plan_create(const gfgpu_space *space, const gfgpu_form *form, void *cu
         delete P;
         return rc;
       }
-    } else if (!gauss_form_supported(P->form, S.qdim, S.dim, P->law, why)) {
-      set_last_error("form not supported: " + why);
+    } else if (std::string gwhy; !gauss_form_supported(P->form, S.qdim, S.dim, P->law, gwhy)) {
+      // an anisotropic coupling is lowered by the simplex pass only: its
+      // reason is the one to report on simplices
+      set_last_error("form not supported: " +
+                     (S.kind == GFGPU_SIMPLEX && form_has_tensor(P->form) ? why : gwhy));
       delete P;
       return GFGPU_E_UNSUPPORTED;
     }
@@ -1064,6 +1067,7 @@ int gfgpu_batch_create(gfgpu_plan *const *plans, int32_t n, gfgpu_batch **out) {
   if (cudaMemset(B->d_err, 0, sizeof(int)) != cudaSuccess)
     return fail(GFGPU_E_CUDA, "gfgpu_batch_create: cudaMemset failed");
   for (int i = 0; i < n; ++i) {
+    if (!plans[i]) return fail(GFGPU_E_INVALID, "gfgpu_batch_create: null plan");
     Plan &P = *plans[i];
     if (!P.affine_simplex)
       return fail(GFGPU_E_UNSUPPORTED, "gfgpu_batch_create: batches take affine-simplex plans");
