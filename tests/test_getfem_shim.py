@@ -187,6 +187,87 @@ def test_cpp_and_python_reject_the_same_expressions():
         assert _py_rejects(c), c[0]
 
 
+def _stiffness81():
+    """A 3-D stiffness with major and minor symmetry, Fortran order."""
+    rng = np.random.default_rng(8)
+    M = rng.uniform(-0.3, 0.3, (6, 6))
+    S = (M + M.T) / 2 + np.diag(rng.uniform(1.0, 3.0, 6))
+    V = [[0, 5, 4], [5, 1, 3], [4, 3, 2]]
+    C = np.zeros((3, 3, 3, 3))
+    for a in range(3):
+        for k in range(3):
+            for b in range(3):
+                for l in range(3):
+                    C[a, k, b, l] = S[V[a][k], V[b][l]]
+    return C.ravel(order="F")
+
+
+def _cspec(name, vals):
+    return f"{name}:C=" + ";".join(repr(float(x)) for x in vals)
+
+
+TRI = (2, "PK", 1, 1, "IM_TRIANGLE(2)")
+TET3 = (3, "PK", 1, 3, "IM_TETRAHEDRON(2)")
+# spellings beyond the fixtures: (name, space, expr, data)
+SPELLINGS = [
+    ("lap_swapped", TRI, "Grad_Test_u.Grad_u", ""),
+    ("lap_scaled", TRI, "2*Grad_u.Grad_Test_u - 0.5*Grad_Test_u.Grad_u", ""),
+    ("kappa_inside", TRI, "(kappa*Grad_u).Grad_Test_u", "kappa:P0"),
+    ("kappa_right", TRI, "Grad_u.Grad_Test_u*kappa", "kappa:P0"),
+    ("mass_lap", TRI, "u*Test_u*3 + Grad_u.Grad_Test_u", ""),
+    ("aniso_literal", TRI, "([2,0.5;0.5,1]*Grad_u).Grad_Test_u", ""),
+    ("aniso_swapped", TRI, "Grad_Test_u.([2,0.5;0.5,1]*Grad_u)", ""),
+    ("aniso_tensor_product", TRI, "[2,0.5;0.5,1]:(Grad_u@Grad_Test_u)", ""),
+    ("aniso_reshaped_data", TRI, "(Reshape(A,2,2)*Grad_u).Grad_Test_u",
+     _cspec("A", [2.0, 0.5, 0.5, 1.0])),
+    ("aniso_kappa_plus_iso", TRI,
+     "kappa*([3,1;1,2]*Grad_u).Grad_Test_u + Grad_u.Grad_Test_u - f*Test_u", "kappa:P0,f:V"),
+    ("potential_mass_lap", TRI, "kappa*Grad_u.Grad_u + u*u", "kappa:P0"),
+    ("elastic_div", TET3, "lambda*Div_u*Div_Test_u + 2*mu*Sym(Grad_u):Grad_Test_u",
+     "lambda:P0,mu:P0"),
+    ("elastic_trace", TET3, "(lambda*Trace(Grad_u)*Id(3) + mu*(Grad_u+Grad_u')):Grad_Test_u",
+     "lambda:P0,mu:P0"),
+    ("elastic_sym_test", TET3, "(lambda*Div_u*Id(3)+2*mu*Sym(Grad_u)):Sym(Grad_Test_u)",
+     "lambda:P0,mu:P0"),
+    ("deviator", TET3, "Deviator(Sym(Grad_u)):Grad_Test_u", ""),
+    ("aniso_stiffness", TET3, "(Reshape(Cani,3,3,3,3):Grad_u):Grad_Test_u - f.Test_u",
+     _cspec("Cani", _stiffness81()) + ",f:V"),
+    ("aniso_separable", TET3,
+     "([2,0,0;0,1,0;0,0,1]*Grad_u*[1,0.5,0;0.5,1,0;0,0,1]):Grad_Test_u", ""),
+]
+
+
+def _py_ws(space, expr, data):
+    dim, gt, deg, qdim, im = space
+    mesh = g.Mesh.regular_unit(dim, 2, "simplex" if gt == "PK" else "hex")
+    mf = g.MeshFem(mesh, qdim, degree=deg)
+    ws = g.GaWorkspace()
+    ws.add_fem_variable("u", mf, U=np.zeros(mf.nb_dof()))
+    for spec in filter(None, data.split(",")):
+        nm, k = spec.split(":", 1)
+        if k == "P0":
+            ws.add_fem_constant(nm, g.MeshFem(mesh, 1, degree=0), np.ones(mesh.nb_convex()))
+        elif k == "V":
+            ws.add_fem_constant(nm, mf, np.ones(mf.nb_dof()))
+        elif k.startswith("C="):
+            ws.add_fixed_size_constant(nm, np.array([float(x) for x in k[2:].split(";")]))
+    ws.add_expression(expr, g.MeshIm(mesh, im))
+    return ws
+
+
+def test_cpp_and_python_lowerings_agree_on_more_spellings():
+    cases = [(nm, sp[0], 2, sp[1], sp[2], sp[3], sp[4], expr, data)
+             for nm, sp, expr, data in SPELLINGS]
+    cpp = _cpp_lower(cases)
+    for nm, sp, expr, data in SPELLINGS:
+        ws = _py_ws(sp, expr, data)
+        grp = ws.groups[0]
+        for order, terms in ((0, grp.order0), (1, grp.order1), (2, grp.order2)):
+            d = cpp[(nm, order)]
+            assert "error" not in d, (nm, order, d["error"])
+            assert _canon_cpp(d["forms"]) == _canon_py(ws, terms), (nm, order)
+
+
 # ------------------------------------------------------- drop-in (GPU)
 
 def _run_shim(rec, orders="2,1", extra=()):
