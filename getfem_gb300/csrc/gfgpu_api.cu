@@ -378,10 +378,14 @@ std::string family_key(const Plan &P) {
   k += "-d" + std::to_string(P.dim) + "-k" + std::to_string(P.kind) + "-p" +
        std::to_string(P.degree) + "-q" + std::to_string(P.qdim) + "-nq" + std::to_string(P.nq) +
        "-law" + std::to_string(P.law);
+  // forms with an anisotropic coupling run their own element-pass instances
+  if (P.affine_simplex && form_has_tensor(P.form)) k += "-tensor";
   return k + "|" + gpu_name();
 }
 
 std::vector<int> ep_candidates(const Plan &P) {
+  // (the anisotropic-coupling instances exist at 4 threads per element)
+  if (P.affine_simplex && form_has_tensor(P.form)) return {4};
   if (P.affine_simplex) return {2, 4, 8};
   return {128, 256, 512};
 }

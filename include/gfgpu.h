@@ -485,7 +485,8 @@ int gfgpu_assemble_vector_noalloc(const gfgpu_noalloc_args *args, const gfgpu_fo
 /* Threads per element of the element pass that stores K_e, and warps per
    block of the row gather (one warp per DOF node).  Candidates:
      ep_threads    affine simplices 2, 4, 8 (warps sharing a 32-element
-                   tile: that many threads per element); Gauss-point and
+                   tile: that many threads per element; 4 only for a form
+                   with a GRADGRAD_TENSOR term); Gauss-point and
                    parallelepiped hexahedra 128, 256, 512 (the CTA of one
                    element);
      gather_warps  2, 4, 8.
