@@ -268,6 +268,64 @@ def test_cpp_and_python_lowerings_agree_on_more_spellings():
             assert _canon_cpp(d["forms"]) == _canon_py(ws, terms), (nm, order)
 
 
+def _random_forms(n, seed=31):
+    """Seeded random weak forms built from the lowered families, with dyadic
+    coefficients (exact in both lowerings): (name, space, expr, data)."""
+    rng = np.random.default_rng(seed)
+
+    def c():
+        return f"{int(rng.integers(1, 16)) / 8:g}"
+    out = []
+    for i in range(n):
+        if i % 2 == 0:
+            dim = int(rng.choice([2, 3]))
+            space = TRI if dim == 2 else (3, "PK", 1, 1, "IM_TETRAHEDRON(2)")
+            parts = [f"{c()}*Grad_u.Grad_Test_u"]
+            if rng.random() < 0.5:
+                parts.append(f"kappa*Grad_u.Grad_Test_u*{c()}")
+            if rng.random() < 0.5:
+                parts.append(f"{c()}*u*Test_u")
+            if rng.random() < 0.6:
+                M = rng.integers(-4, 5, (dim, dim)) / 4
+                A = M + M.T + np.eye(dim) * 3
+                lit = ";".join(",".join(f"{x:g}" for x in row) for row in A)
+                scale = "kappa*" if rng.random() < 0.5 and "kappa" not in " ".join(parts) else ""
+                parts.append(f"{scale}([{lit}]*Grad_u).Grad_Test_u")
+            if rng.random() < 0.5:
+                parts.append("- f*Test_u")
+        else:
+            space = TET3
+            parts = [f"{c()}*Div_u*Div_Test_u"]
+            for t in ("Sym(Grad_u):Grad_Test_u", "Grad_u:Grad_Test_u", "Grad_u':Grad_Test_u",
+                      "lambda*Div_u*Div_Test_u", "mu*(Grad_u+Grad_u'):Grad_Test_u", "u.Test_u"):
+                if rng.random() < 0.4:
+                    parts.append(f"{c()}*{t}")
+            if rng.random() < 0.3:
+                parts.append("([2,0,0;0,1,0;0,0,1]*Grad_u*[1,0.5,0;0.5,1,0;0,0,1]):Grad_Test_u")
+            if rng.random() < 0.5:
+                parts.append("- f.Test_u")
+        expr = " + ".join(parts).replace("+ -", "-")
+        used = [d for d in ("kappa", "lambda", "mu") if d in expr]
+        has_f = "f*Test_u" in expr or "f.Test_u" in expr
+        data = ",".join([f"{d}:P0" for d in used] + (["f:V"] if has_f else []))
+        out.append((f"random_{i}", space, expr, data))
+    return out
+
+
+def test_cpp_and_python_lowerings_agree_on_random_forms():
+    forms = _random_forms(24)
+    cases = [(nm, sp[0], 2, sp[1], sp[2], sp[3], sp[4], expr, data)
+             for nm, sp, expr, data in forms]
+    cpp = _cpp_lower(cases)
+    for nm, sp, expr, data in forms:
+        ws = _py_ws(sp, expr, data)
+        grp = ws.groups[0]
+        for order, terms in ((1, grp.order1), (2, grp.order2)):
+            d = cpp[(nm, order)]
+            assert "error" not in d, (nm, expr, order, d["error"])
+            assert _canon_cpp(d["forms"]) == _canon_py(ws, terms), (nm, expr, order)
+
+
 # ------------------------------------------------------- drop-in (GPU)
 
 def _run_shim(rec, orders="2,1", extra=()):
