@@ -1053,6 +1053,11 @@ int gfgpu_batch_create(gfgpu_plan *const *plans, int32_t n, gfgpu_batch **out) {
     return GFGPU_E_INVALID;
   }
   *out = nullptr;
+  for (int i = 0; i < n; ++i)
+    if (!plans[i]) {
+      set_last_error("gfgpu_batch_create: null plan");
+      return GFGPU_E_INVALID;
+    }
   gfgpu_batch *B = new (std::nothrow) gfgpu_batch();
   if (!B) return GFGPU_E_NOMEM;
   auto fail = [&](int rc, const std::string &msg) {
@@ -1071,7 +1076,6 @@ int gfgpu_batch_create(gfgpu_plan *const *plans, int32_t n, gfgpu_batch **out) {
   if (cudaMemset(B->d_err, 0, sizeof(int)) != cudaSuccess)
     return fail(GFGPU_E_CUDA, "gfgpu_batch_create: cudaMemset failed");
   for (int i = 0; i < n; ++i) {
-    if (!plans[i]) return fail(GFGPU_E_INVALID, "gfgpu_batch_create: null plan");
     Plan &P = *plans[i];
     if (!P.affine_simplex)
       return fail(GFGPU_E_UNSUPPORTED, "gfgpu_batch_create: batches take affine-simplex plans");

@@ -31,3 +31,15 @@ def test_version_and_error_text():
     lib = L.lib()
     assert b"sm_103a" in lib.gfgpu_version()
     assert lib.gfgpu_last_error() is not None
+
+
+def test_host_checks_before_any_device_call():
+    """Argument mistakes are statuses, found before the library touches a
+    device (these calls run without a GPU)."""
+    lib = L.lib()
+    assert lib.gfgpu_plan_create(None, None, None, None) == L.E_INVALID
+    out = C.c_void_p()
+    plans = (C.c_void_p * 2)(None, None)
+    assert lib.gfgpu_batch_create(plans, 2, C.byref(out)) == L.E_INVALID
+    assert b"null plan" in lib.gfgpu_last_error()
+    assert lib.gfgpu_batch_create(None, 1, C.byref(out)) == L.E_INVALID

@@ -172,3 +172,22 @@ def test_noalloc_rejects_null_adjacency_without_elements():
     assert _status(args, _elasticity_form()) == L.E_INVALID
 
 
+
+
+def test_noalloc_refuses_an_anisotropic_coupling():
+    """The allocation-free pass has no anisotropic-coupling instances: a form
+    with a GRADGRAD_TENSOR term is refused, not assembled without it."""
+    args = _valid_args()
+    args.slots[1] = args.slots[3] = 1
+    form = _elasticity_form()
+    t = form.terms[2]
+    t.kind, t.scale = L.TERM_GRADGRAD_TENSOR, 1.0
+    for i in range(9):
+        form.tensor[i * 9 + i] = 1.0
+    form.n_terms = 3
+    assert _status(args, form) == L.E_UNSUPPORTED
+    assert b"anisotropic" in L.lib().gfgpu_last_error()
+    # an unsymmetric tensor is refused by the form check itself
+    form.tensor[1] = 0.5
+    assert _status(args, form) == L.E_UNSUPPORTED
+    assert b"symmetric" in L.lib().gfgpu_last_error()
