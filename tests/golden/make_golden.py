@@ -91,6 +91,13 @@ CASES += [
     ("p2tet_aniso_elastic", 3, "PK", 2, 3, "IM_TETRAHEDRON(5)", 3,
      "(Reshape(Cani,3,3,3,3):Grad_u):Grad_Test_u - f.Test_u",
      {"Cani": "C", "f": "V"}, True, "normal"),
+    # the same couplings on jittered (non-affine) hexahedra: they pin the
+    # oracle's per-point contraction for the hexahedral kernels
+    ("q2hex_aniso", 3, "QK", 2, 1, "IM_GAUSS_PARALLELEPIPED(3,5)", 2,
+     "([3,0.5,0.25;0.5,2,0.125;0.25,0.125,1]*Grad_u).Grad_Test_u - f*Test_u",
+     {"f": "V"}, True, "normal"),
+    ("q1hex_aniso_elastic", 3, "QK", 1, 3, "IM_GAUSS_PARALLELEPIPED(3,3)", 2,
+     "(Reshape(Cani,3,3,3,3):Grad_u):Grad_Test_u", {"Cani": "C"}, True, "normal"),
 ]
 
 
